@@ -1,0 +1,370 @@
+"""Benchmark of the Wilson-twisted-mass hot path on one GB300 (or N replicas).
+
+Workload (one "step" = one application of the FP64 Wilson-Dirac operator
+D on a 24^3 x 48 lattice, kappa = 0.150, antiperiodic in t, synthetic SU(3)
+links with mean plaquette 0.60 and a seeded Gaussian spinor): the lattice of
+the plain FP64 single-RHS configuration, timed over K applications.
+
+  value  -- device-resident: algorithmic bytes per apply (spinor in + 4
+            links (12 reals) + spinor out = 768 B/site) / kernel time, GB/s.
+  e2e    -- the same apply through the qcd_lib C entry point
+            qcd_applyWilsonTMOp on host (page-locked) buffers: each step
+            copies the input spinor host->device and the result back; the
+            gauge field is uploaded once beforehand (qcdgpu_gauge_upload).
+  solve  -- RHS-solves/s and latency percentiles of point-source solves to a
+            true residual of 1e-10: plain FP64 GPU solve vs mixed precision.
+
+Multi-GPU: the operator keeps the whole lattice on one GPU; N processes run
+N independent replicas (no collective) and value sums their throughput.
+
+--impl reference times the reference's CPU path (the oracle build of the
+reference where it exists, else the C restatement) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L_BENCH = (48, 24, 24, 24)  # t, x, y, z
+KAPPA = 0.150
+THETA = (3.141592653589793, 0.0, 0.0, 0.0)
+EPS_PLAQ_060 = 0.43374
+FLOPS_PER_SITE = 1320
+METRIC = "Dslash GB/s (% HBM peak); RHS-solves/s, p99 latency @1e-10 vs plain FP64 GPU"
+
+
+def bytes_per_site(prec: int, recon: int) -> int:
+    """compulsory HBM bytes per site of one apply: spinor in, 4 links, spinor out"""
+    if prec == 0:
+        return 192 + 4 * recon * 8 + 192
+    if prec == 1:
+        return 96 + 4 * recon * 4 + 96
+    return 52 + 4 * 12 * 2 + 52
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d["hbm_gbs"], "src": "measured"}
+    return {"hbm_gbs": 6800.0, "src": "fallback"}
+
+
+def profile_traffic(name: str):
+    """DRAM bytes per launch from the committed ncu summary, if present"""
+    p = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_launch:"):
+            return float(line.split(":")[1])
+    return None
+
+
+class ClockSampler:
+    """samples nvidia-smi SM clocks and throttle reasons in the background"""
+
+    QUERY = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------ CPU baseline
+def _cpu_worker(args):
+    """one process: time the oracle's FP64 operator on the bench lattice"""
+    budget_s, L = args
+    import numpy as np
+
+    sys.path.insert(0, ROOT)
+    from oracle.oracle import Oracle
+
+    orc = Oracle()
+    u = orc.gauge_synthetic(L, 0, EPS_PLAQ_060)
+    v = orc.gaussian_spinor(L, 1)
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        orc.dslash(v, u, L, THETA, kappa=KAPPA)
+        n += 1
+        if time.perf_counter() - t0 >= budget_s:
+            break
+    return n, time.perf_counter() - t0
+
+
+def cpu_baseline(budget_s: float, procs: int, L=L_BENCH) -> dict:
+    import multiprocessing as mp
+
+    from oracle.oracle import ORACLE_SO, build
+
+    if not os.path.exists(ORACLE_SO):
+        build(with_ref=False)
+    V = L[0] * L[1] * L[2] * L[3]
+    ctx = mp.get_context("spawn")
+    if procs == 1:
+        res = [_cpu_worker((budget_s, L))]
+    else:
+        with ctx.Pool(procs) as pool:
+            res = pool.map(_cpu_worker, [(budget_s, L)] * procs)
+    rate = sum(n / t for n, t in res)  # applies per second, all processes
+    gbs = rate * V * bytes_per_site(0, 12) / 1e9
+    applies = sum(n for n, _ in res)
+    return {"value": gbs, "unit": "GB/s", "cores": procs, "kind": "port",
+            "sample": f"{applies} FP64 D applies of {L[3]}^3x{L[0]} ({budget_s:.0f} s per process, "
+                      f"{procs} process(es), C restatement of qcd_applyWilsonTMOp at -O2)",
+            "applies_per_s": rate}
+
+
+# ------------------------------------------------------------- GPU parts
+def time_dslash(q, torch, fout, fin, g, steps, warmup, arith, stream):
+    lib = q.lib()
+    for _ in range(warmup):
+        q.dslash(fout, fin, g, KAPPA, 0.0, q.OP_D, arith)
+    torch.cuda.synchronize()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n0 = lib.qcdgpu_kernel_launches()
+    start.record(stream)
+    for _ in range(steps):
+        q.dslash(fout, fin, g, KAPPA, 0.0, q.OP_D, arith)
+    stop.record(stream)
+    torch.cuda.synchronize()
+    return start.elapsed_time(stop) / steps, lib.qcdgpu_kernel_launches() - n0
+
+
+def time_e2e(q, torch, steps, warmup, u_host, v_host):
+    """qcd_applyWilsonTMOp on host buffers; returns ms per step and bytes"""
+    import numpy as np
+
+    lib = q.lib()
+    geo = q.Geometry(L_BENCH, THETA)
+    u, v, Dv = q.GaugeField(geo), q.Vector(geo), q.Vector(geo)
+    u.a[:] = u_host
+    v.a[:] = v_host
+    assert lib.qcdgpu_gauge_upload(u.ref) == 0
+    m = 1.0 / (2.0 * KAPPA) - 4.0
+    for _ in range(warmup):
+        assert lib.qcd_applyWilsonTMOp(Dv.ref, v.ref, u.ref, m, 0.0) == 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        assert lib.qcd_applyWilsonTMOp(Dv.ref, v.ref, u.ref, m, 0.0) == 0
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3 / steps
+    out = np.array(Dv.a[:4])
+    nbytes = geo.V * 192
+    for o in (u, v, Dv):
+        o.close()
+    geo.close()
+    return ms, nbytes, nbytes, out
+
+
+def solve_bench(q, orc_check, g, L, n_rhs):
+    """point-source columns solved to 1e-10: plain FP64 vs mixed precision"""
+    out = {}
+    b, x = q.Field(L), q.Field(L)
+    for name, solver, prec in (("fp64_cgnr", q.SOLVER_CGNR, q.F64), ("mixed_cgnr_f16", q.SOLVER_CGNR, q.F16),
+                               ("mixed_cgnr_f32", q.SOLVER_CGNR, q.F32)):
+        lat, iters, res = [], [], []
+        for col in range(n_rhs):
+            b.point((0, 0, 0, 0), col // 3, col % 3)
+            q.sync()
+            t0 = time.perf_counter()
+            p = q.solve(x, b, g, KAPPA, 0.0, solver=solver, inner_prec=prec, tol=1e-10)
+            q.sync()
+            lat.append(time.perf_counter() - t0)
+            iters.append(p.iters)
+            res.append(p.true_residual)
+            if p.status != 0:
+                raise RuntimeError(f"{name} did not converge: {p.status} {p.true_residual}")
+        lat.sort()
+        out[name] = {"rhs_solves_per_s": n_rhs / sum(lat), "p50_ms": 1e3 * lat[len(lat) // 2],
+                     "p99_ms": 1e3 * lat[min(len(lat) - 1, int(0.99 * len(lat)))], "iters": iters,
+                     "max_true_residual": max(res)}
+    out["speedup_mixed_vs_fp64"] = out["mixed_cgnr_f16"]["rhs_solves_per_s"] / out["fp64_cgnr"]["rhs_solves_per_s"]
+    b.close()
+    x.close()
+    return out
+
+
+def run_ours(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+
+    import qcd_gb300 as q
+
+    torch.cuda.set_device(local_rank)
+    stream = torch.cuda.current_stream()
+    q.set_stream(stream.cuda_stream)
+    V = L_BENCH[0] * L_BENCH[1] * L_BENCH[2] * L_BENCH[3]
+    g = q.Gauge(L_BENCH, THETA).synthetic(1000 + rank, EPS_PLAQ_060)
+    plaq = g.plaquette()
+    fin, fout = q.Field(L_BENCH).gaussian(2000 + rank), q.Field(L_BENCH)
+    recon = g.recon
+    bps = bytes_per_site(0, recon)
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ms_native, launches = time_dslash(q, torch, fout, fin, g, args.steps, args.warmup, q.ARITH_F64, stream)
+    ms_df64 = None
+    try:
+        ms_df64, launches_df = time_dslash(q, torch, fout, fin, g, args.steps, args.warmup, q.ARITH_DF64, stream)
+    except q.QcdGpuError:
+        ms_df64 = None
+    clocks = sampler.stop()
+    # fastest FP64-accurate kernel is the product path
+    best_ms, arith = (ms_native, "f64") if ms_df64 is None or ms_native <= ms_df64 else (ms_df64, "df64")
+    if arith == "df64":
+        launches = launches_df
+    t = torch.tensor([best_ms], device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    # e2e through the C entry point with host buffers
+    u_host = g.store()
+    v_host = fin.store()
+    q.lib().qcdgpu_set_f64_arith(q.ARITH_DF64 if arith == "df64" else q.ARITH_F64)
+    e2e_steps = max(3, min(args.steps, 50))
+    ms_e2e, h2d, d2h, _ = time_e2e(q, torch, e2e_steps, max(1, args.warmup // 4), u_host, v_host)
+    solve = None
+    if not args.no_solve and rank == 0:
+        solve = solve_bench(q, None, g, L_BENCH, args.solve_rhs)
+    for f in (g, fin, fout):
+        f.close()
+    if rank != 0:
+        return None
+    peaks = measured_peaks()
+    gbs = V * bps / (ms_max * 1e-3) / 1e9
+    achieved_1 = V * bps / (best_ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": gbs * world, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if arith == "f64" else "f64 storage, df64 arithmetic",
+        "data": "synthetic (seeded SU(3) links exp(i eps H), plaquette %.4f; Gaussian spinor)" % plaq,
+        "config": {"workload": "FP64 Wilson-Dirac apply D psi, 24^3x48, kappa 0.150, theta_t = pi, 12-real links",
+                   "lattice_txyz": list(L_BENCH), "sites": V, "bytes_per_site": bps, "flops_per_site": FLOPS_PER_SITE,
+                   "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (working set %d MB vs 129 MB)" % (V * bps // 2**20)},
+        "gflops": V * FLOPS_PER_SITE / (ms_max * 1e-3) / 1e9 * world,
+        "roofline": {"bound": "hbm", "achieved": achieved_1, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved_1 / peaks["hbm_gbs"], "peak_source": peaks["src"],
+                     "traffic": profile_traffic("dslash_f64_24x24x24x48.txt")},
+        "kernels_ms": {"f64": ms_native, "df64": ms_df64},
+        "e2e": {"value": V * bps / (ms_e2e * 1e-3) / 1e9 * world, "unit": "GB/s", "ms_per_step": ms_e2e,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "path": "qcd_applyWilsonTMOp on page-locked host qcd_vector buffers, resident gauge"},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "solve": solve,
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(args.cpu_seconds, 1)
+    return line
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    ncores = os.cpu_count() or 1
+    cb = cpu_baseline(args.ref_seconds, ncores)
+    V = L_BENCH[0] * L_BENCH[1] * L_BENCH[2] * L_BENCH[3]
+    ms = 1e3 / cb["applies_per_s"]
+    return {"metric": METRIC, "value": cb["value"], "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "FP64 Wilson-Dirac apply D psi, 24^3x48, kappa 0.150, theta_t = pi",
+                       "lattice_txyz": list(L_BENCH), "sites": V, "bytes_per_site": bytes_per_site(0, 12),
+                       "parallelism": f"{ncores} CPU processes, one apply stream each"},
+            "impl": "reference", "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-solve", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--solve-rhs", type=int, default=4)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-seconds", type=float, default=20.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        if world > 1:
+            import torch
+
+            torch.distributed.init_process_group("nccl")
+        line = run_ours(args, rank, world, local_rank)
+        if world > 1:
+            import torch
+
+            torch.distributed.destroy_process_group()
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

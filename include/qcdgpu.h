@@ -1,0 +1,312 @@
+/* qcdgpu.h -- C ABI of the GB300 Wilson-twisted-mass library.
+ *
+ * Part 1 re-declares the data model of qcd_lib (include/qcd.h) with the same
+ * sizes, field order and meaning, so host code written against qcd_lib can
+ * hand its qcd_geometry / qcd_vector / qcd_gaugeField structs to this library
+ * unchanged. Part 2 exports, under their qcd_lib names and signatures, the
+ * entry points of the operator-apply and solve path; each cites the reference
+ * declaration it replaces. Part 3 is this library's own extension API
+ * (device residency, precision, multi-RHS, serving) and carries the
+ * qcdgpu_ prefix.
+ *
+ * Semantics shared by every Part-2 entry point:
+ *  - the whole lattice lives on one GPU; P must be {1,1,1,1} and numprocs 1;
+ *  - arguments and results are the caller's host arrays (v->D, u->D): an
+ *    entry point uploads what it reads and, before it returns, writes its
+ *    results back to host memory -- unless the object was made device
+ *    resident with qcdgpu_vector_make_resident / qcdgpu_gauge_upload, in
+ *    which case the device copy is authoritative (Part 3);
+ *  - errors return 1 (or NaN for scalar results) with a message on stderr,
+ *    as the reference does; CUDA failures are reported the same way; no
+ *    entry point aborts the process;
+ *  - Dv == v (in-place operator apply) is rejected with return value 1: the
+ *    reference leaves it undefined (qcd_wilson.c writes Dv while it still
+ *    reads neighbours of v).
+ *  - not re-entrant per geometry; call from one host thread at a time.
+ */
+#ifndef QCDGPU_H
+#define QCDGPU_H 1
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ============================ Part 1: data model ======================== */
+
+/* scalar types, include/qcd.h:18-28 */
+typedef float qcd_real_4;
+typedef double qcd_real_8;
+typedef char qcd_int_1;
+typedef short qcd_int_2;
+typedef int qcd_int_4;
+typedef long qcd_int_8;
+typedef unsigned char qcd_uint_1;
+typedef unsigned short qcd_uint_2;
+typedef unsigned int qcd_uint_4;
+typedef unsigned long qcd_uint_8;
+
+/* qcd_geometry embeds MPI handle arrays. The library never calls MPI; it only
+ * needs their size. Handles are int-sized (the MPICH convention). A build
+ * that includes a real <mpi.h> first must use an MPI with int handles. */
+#ifndef MPI_VERSION
+typedef int MPI_Request;
+typedef int MPI_Datatype;
+#endif
+
+/* include/qcd.h:31-41 */
+typedef struct {
+  qcd_real_8 re;
+  qcd_real_8 im;
+} qcd_complex_16;
+
+typedef struct {
+  qcd_real_4 re;
+  qcd_real_4 im;
+} qcd_complex_8;
+
+/* include/qcd.h:44-87 */
+typedef struct {
+  qcd_uint_8 V;                /* 4d volume */
+  qcd_uint_8 V3;               /* spatial volume */
+  qcd_uint_2 L[4];             /* lattice extents t,x,y,z */
+  qcd_uint_8 lV;               /* local volume (== V here) */
+  qcd_uint_8 lV3;
+  qcd_uint_2 lL[4];
+  qcd_uint_2 Pos[4];
+  qcd_real_8 theta[4];         /* psi(x + L_mu) = exp(i theta_mu) psi(x) */
+  qcd_uint_4 myid;
+  qcd_uint_4 nproc;
+  qcd_uint_4 Pplus[4];
+  qcd_uint_4 Pminus[4];
+  qcd_uint_8 (*plus)[4];       /* neighbour tables, periodic in the lattice */
+  qcd_uint_8 (*minus)[4];
+  qcd_uint_8 (*plus3d)[4];
+  qcd_uint_8 (*minus3d)[4];
+  qcd_uint_8 (*eo)[2];
+  qcd_uint_8 startBminus[4];
+  qcd_uint_8 startBplus[4];
+  qcd_uint_8 startBminus3d[4];
+  qcd_uint_8 startBplus3d[4];
+  qcd_uint_8 boundarySize;
+  qcd_uint_8 boundarySize3d;
+  qcd_uint_8 *edge;
+  qcd_uint_8 edgePoints;
+  qcd_uint_8 *edge0;
+  qcd_uint_8 edge0Points;
+  MPI_Request requests[32];
+  int numOfRequests;
+  MPI_Datatype stypeV[4];
+  MPI_Datatype rtypeV[4];
+  MPI_Datatype stypeU[4];
+  MPI_Datatype rtypeU[4];
+  MPI_Datatype stypeT[4];
+  MPI_Datatype rtypeT[4];
+  MPI_Datatype stypeP[4];
+  MPI_Datatype rtypeP[4];
+  qcd_uint_2 initialized;
+} qcd_geometry;
+
+/* include/qcd.h:90-97: spinor D[site][spin][colour] */
+typedef struct {
+  qcd_complex_16 (*D)[4][3];
+  qcd_complex_16 (*Bplus[4])[4][3];
+  qcd_complex_16 (*Bminus[4])[4][3];
+  qcd_geometry *geo;
+  qcd_uint_2 initialized;
+} qcd_vector;
+
+/* include/qcd.h:119-126: links D[site][mu][row][col] */
+typedef struct {
+  qcd_complex_16 (*D)[4][3][3];
+  qcd_complex_16 (*Bplus[4])[4][3][3];
+  qcd_complex_16 (*Bminus[4])[4][3][3];
+  qcd_geometry *geo;
+  qcd_uint_2 initialized;
+} qcd_gaugeField;
+
+/* ===================== Part 2: qcd_lib entry points ===================== */
+
+/* include/qcd.h:187-195 (lib/src/qcd_init.c:25,:394,:418,:614) */
+int qcd_initGeometry(qcd_geometry *geo, const qcd_uint_2 L[], const qcd_uint_2 P[],
+                     const qcd_real_8 theta[], const int myid, const int numprocs);
+void qcd_destroyGeometry(const qcd_geometry *geo);
+int qcd_initVector(qcd_vector *vec, qcd_geometry *geo);
+void qcd_destroyVector(qcd_vector *vec);
+int qcd_initGaugeField(qcd_gaugeField *u, qcd_geometry *geo);
+void qcd_destroyGaugeField(qcd_gaugeField *u);
+
+/* include/qcd_wilson.h:634-637 (lib/src/qcd_wilson.c:114,:351,:570,:795).
+ * D = (m+4) + i tm gamma_5 - 1/2 sum_mu [(1-gamma_mu) U_mu(x) e^{i th/L} v(x+mu)
+ *                                    + (1+gamma_mu) U_mu(x-mu)^+ e^{-i th/L} v(x-mu)]
+ * in the chiral basis of qcd_gamma.c; Q = i gamma_5 D. The three D entry
+ * points are the same operator (the reference's three implementations agree
+ * to rounding). */
+int qcd_applyWilsonTMOp(qcd_vector *Dv, qcd_vector *v, qcd_gaugeField *u, qcd_real_8 m, qcd_real_8 tm);
+int qcd_applyWilsonTMOpNoScripts(qcd_vector *Dv, qcd_vector *v, qcd_gaugeField *u, qcd_real_8 m, qcd_real_8 tm);
+int qcd_applyWilsonTMOpNoOptim(qcd_vector *Dv, qcd_vector *v, qcd_gaugeField *u, qcd_real_8 m, qcd_real_8 tm);
+int qcd_applyQTMOp(qcd_vector *Dv, qcd_vector *v, qcd_gaugeField *u, qcd_real_8 m, qcd_real_8 tm);
+
+/* include/qcd_blas.h:245-267 (lib/src/qcd_blas.c:137-492); all on the GPU */
+void qcd_zeroVector(qcd_vector *vec);
+void qcd_setVector(qcd_vector *vec, qcd_complex_16 c);
+void qcd_copyVector(qcd_vector *dest, qcd_vector *src);
+void qcd_mulVectorC(qcd_vector *vec, qcd_complex_16 c);
+void qcd_scaleVector(qcd_vector *vec, qcd_real_8 r);
+void qcd_subVector(qcd_vector *difference, qcd_vector *minuend, qcd_vector *subtrahend);
+void qcd_addVector(qcd_vector *sum, qcd_vector *summand1, qcd_vector *summand2);
+void qcd_axpyVector(qcd_vector *axpy, qcd_complex_16 a, qcd_vector *x, qcd_vector *y);
+qcd_complex_16 qcd_mulAdjointVectorVector(qcd_vector *factor1, qcd_vector *factor2);
+qcd_real_8 qcd_normVector(qcd_vector *vec);
+/* include/qcd_gamma.h (lib/src/qcd_gamma.c:521) */
+void qcd_gamma5Vector(qcd_vector *v);
+
+/* include/qcd_communication.h:12,21 (lib/src/qcd_communication.c:20,:343).
+ * One GPU holds the whole lattice: no halo exists, both are no-ops that keep
+ * the reference's "communication already in flight" check. */
+int qcd_communicateVectorPMGaugeP(qcd_vector *v, qcd_gaugeField *u);
+void qcd_waitall(qcd_geometry *geo);
+
+/* invert.c:20. n-step GCR with modified Gram-Schmidt on Q = i gamma_5 D,
+ * m = 1/(2 kappa) - 4. The solution update includes the first basis term
+ * (the algorithm of gcr.m); the shipped invert.c omits it (:52-53), which
+ * qcdgpu_set_gcr_compat(1) restores. Returns 0, or EXIT_FAILURE when the
+ * Krylov space degenerates (NaN norm). */
+qcd_int_4 gcr(qcd_vector *sol, qcd_vector *src, qcd_gaugeField *u, qcd_real_8 kappa,
+              qcd_real_8 muTM, qcd_uint_4 n, qcd_geometry *geo);
+
+/* No reference counterpart (qcd_lib ships only GCR): BiCGstab (van der Vorst
+ * 1992) on D x = b in FP64, x0 = 0, shadow residual a fixed seeded Z4 vector,
+ * run until the true relative residual |b - Dx|/|b| <= tol or maxiter.
+ * Same argument order as gcr(). Returns iterations (>= 0), or -1 on
+ * breakdown / non-convergence / error. */
+qcd_int_4 bicgstab(qcd_vector *sol, qcd_vector *src, qcd_gaugeField *u, qcd_real_8 kappa,
+                   qcd_real_8 muTM, qcd_real_8 tol, qcd_uint_4 maxiter, qcd_geometry *geo);
+
+/* No reference counterpart: CG on D^+ D x = D^+ b (FP64), stopping on the
+ * true relative residual |b - Dx|/|b| <= tol. Returns iterations or -1. */
+qcd_int_4 cgnr(qcd_vector *sol, qcd_vector *src, qcd_gaugeField *u, qcd_real_8 kappa,
+               qcd_real_8 muTM, qcd_real_8 tol, qcd_uint_4 maxiter, qcd_geometry *geo);
+
+/* ====================== Part 3: extension API ========================== */
+
+/* Storage precision of a device field. */
+enum {
+  QCDGPU_F64 = 0,  /* 8-byte reals */
+  QCDGPU_F32 = 1,  /* 4-byte reals */
+  QCDGPU_F16 = 2   /* 2-byte reals; spinors carry one float norm per site */
+};
+/* Operator selector. */
+enum {
+  QCDGPU_OP_D = 0,       /* D */
+  QCDGPU_OP_Q = 1,       /* i gamma_5 D */
+  QCDGPU_OP_DDAG = 2,    /* D^+ */
+  QCDGPU_OP_DDAGD = 3    /* D^+ D */
+};
+/* FP64 operator arithmetic. */
+enum {
+  QCDGPU_ARITH_F64 = 0,  /* native double precision */
+  QCDGPU_ARITH_DF64 = 1  /* float-float (two FP32 words per real) */
+};
+
+typedef struct qcdgpu_field_s *qcdgpu_field; /* device spinor field */
+typedef struct qcdgpu_gauge_s *qcdgpu_gauge; /* device gauge field */
+
+/* last error message of this thread ("" if none) */
+const char *qcdgpu_last_error(void);
+/* select the CUDA stream (cudaStream_t) later calls launch on; NULL = default */
+int qcdgpu_set_stream(void *stream);
+/* synchronise the current stream */
+int qcdgpu_sync(void);
+/* restore invert.c's shipped GCR update (1) or the algorithm's (0, default) */
+void qcdgpu_set_gcr_compat(int shipped);
+/* arithmetic of the FP64 operator used by the Part-2 entry points */
+int qcdgpu_set_f64_arith(int arith);
+/* number of kernels this library launched since the process started */
+uint64_t qcdgpu_kernel_launches(void);
+
+/* Residency of the Part-2 host structs. make_resident uploads v->D once and
+ * from then on the device copy is authoritative: entry points neither
+ * upload nor download it. to_host / to_device copy explicitly. release
+ * returns the object to per-call transfers (after copying back to host). */
+int qcdgpu_vector_make_resident(qcd_vector *v);
+int qcdgpu_vector_to_host(qcd_vector *v);
+int qcdgpu_vector_to_device(qcd_vector *v);
+int qcdgpu_vector_release(qcd_vector *v);
+/* upload u->D and keep it resident (call again after changing u->D) */
+int qcdgpu_gauge_upload(qcd_gaugeField *u);
+int qcdgpu_gauge_release(qcd_gaugeField *u);
+
+/* Device fields. L = {Lt, Lx, Ly, Lz}. Gauge fields store 12 reals per link
+ * (third row rebuilt as the conjugate cross product of the first two) when
+ * every link is in SU(3) to 1e-12, else all 18. */
+int qcdgpu_gauge_create(qcdgpu_gauge *g, const int L[4], const double theta[4], int prec);
+int qcdgpu_gauge_destroy(qcdgpu_gauge g);
+/* host array in the qcd_gaugeField layout, float64[V][4][3][3][2] */
+int qcdgpu_gauge_load(qcdgpu_gauge g, const double *host);
+/* make a lower-precision copy of an existing gauge field */
+int qcdgpu_gauge_convert(qcdgpu_gauge dst, qcdgpu_gauge src);
+/* synthetic links exp(i eps H), H Gaussian traceless Hermitian, seeded */
+int qcdgpu_gauge_synthetic(qcdgpu_gauge g, uint64_t seed, double eps);
+/* copy out to the qcd_gaugeField layout */
+int qcdgpu_gauge_store(qcdgpu_gauge g, double *host);
+int qcdgpu_gauge_recon(qcdgpu_gauge g); /* 12 or 18 */
+double qcdgpu_plaquette(qcdgpu_gauge g);
+
+int qcdgpu_field_create(qcdgpu_field *f, const int L[4], int prec);
+int qcdgpu_field_destroy(qcdgpu_field f);
+/* host array in the qcd_vector layout, float64[V][4][3][2] */
+int qcdgpu_field_load(qcdgpu_field f, const double *host);
+int qcdgpu_field_store(qcdgpu_field f, double *host);
+/* device-to-device copy with precision conversion */
+int qcdgpu_field_copy(qcdgpu_field dst, qcdgpu_field src);
+int qcdgpu_field_gaussian(qcdgpu_field f, uint64_t seed);
+int qcdgpu_field_point(qcdgpu_field f, const int x[4], int spin, int colour);
+/* bytes of device memory the field occupies */
+size_t qcdgpu_field_bytes(qcdgpu_field f);
+size_t qcdgpu_gauge_bytes(qcdgpu_gauge g);
+/* raw device pointer of the field's storage (for timing harnesses) */
+void *qcdgpu_field_data(qcdgpu_field f);
+
+/* out = op(in), m = 1/(2 kappa) - 4; out and in must differ; out, in and g
+ * must have the same precision (FP64 fields use the FP64 arithmetic set by
+ * qcdgpu_set_f64_arith unless arith >= 0 is given). */
+int qcdgpu_dslash(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double kappa, double mu,
+                  int op, int arith);
+
+/* BLAS-1 on device fields of equal shape (FP64 fields; reductions return
+ * through host pointers after synchronising). */
+int qcdgpu_axpy(qcdgpu_field out, double are, double aim, qcdgpu_field x, qcdgpu_field y);
+int qcdgpu_norm2(qcdgpu_field x, double *result);
+int qcdgpu_dot(qcdgpu_field a, qcdgpu_field b, double result[2]);
+
+/* Solver parameters for qcdgpu_solve. */
+typedef struct {
+  int solver;        /* QCDGPU_SOLVER_* */
+  int op;            /* QCDGPU_OP_D or QCDGPU_OP_Q (system matrix) */
+  int inner_prec;    /* QCDGPU_F64 / F32 / F16: storage of the inner iteration */
+  double tol;        /* target true relative residual |b - A x|/|b| */
+  int maxiter;       /* cap on operator applications of the inner solver */
+  int restart;       /* GCR basis size */
+  double delta;      /* reliable-update threshold (mixed precision), e.g. 0.1 */
+  /* outputs */
+  int iters;         /* inner iterations performed */
+  int reliable_updates;
+  double true_residual;
+  int status;        /* 0 converged, 1 not converged, 2 breakdown, 3 error */
+} qcdgpu_solve_params;
+enum {
+  QCDGPU_SOLVER_GCR = 0,
+  QCDGPU_SOLVER_BICGSTAB = 1,
+  QCDGPU_SOLVER_CGNR = 2
+};
+/* solve A x = b with A = op(g; kappa, mu); x, b FP64 device fields */
+int qcdgpu_solve(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double kappa, double mu,
+                 qcdgpu_solve_params *p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,376 @@
+"""qcd_gb300 -- Python access to the GB300 Wilson-twisted-mass library.
+
+The library itself is ``_build/libqcdgpu.so`` (C ABI declared in
+``include/qcdgpu.h``), built by :func:`qcd_gb300.build.build`. This module
+mirrors its two interfaces:
+
+* the qcd_lib drop-in (``qcd_initGeometry``, ``qcd_applyWilsonTMOp``,
+  ``gcr`` ...) on ctypes copies of the ``qcd.h`` structs
+  (:class:`Geometry`, :class:`Vector`, :class:`GaugeField`), whose data arrays
+  are exposed as numpy views in the reference layout;
+* the device API (``qcdgpu_*``): :class:`Field`, :class:`Gauge`,
+  :func:`dslash`, :func:`solve`.
+
+Importing never falls back to CPU arithmetic: if the shared library is
+missing, :func:`lib` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libqcdgpu.so")
+
+F64, F32, F16 = 0, 1, 2
+OP_D, OP_Q, OP_DDAG, OP_DDAGD = 0, 1, 2, 3
+ARITH_F64, ARITH_DF64 = 0, 1
+SOLVER_GCR, SOLVER_BICGSTAB, SOLVER_CGNR = 0, 1, 2
+
+_u8p = C.POINTER(C.c_uint64)
+
+
+class QcdGeometry(C.Structure):
+    """include/qcd.h:44-87 (MPI handles int-sized)."""
+    _fields_ = [
+        ("V", C.c_uint64), ("V3", C.c_uint64), ("L", C.c_uint16 * 4),
+        ("lV", C.c_uint64), ("lV3", C.c_uint64), ("lL", C.c_uint16 * 4), ("Pos", C.c_uint16 * 4),
+        ("theta", C.c_double * 4), ("myid", C.c_uint32), ("nproc", C.c_uint32),
+        ("Pplus", C.c_uint32 * 4), ("Pminus", C.c_uint32 * 4),
+        ("plus", _u8p), ("minus", _u8p), ("plus3d", _u8p), ("minus3d", _u8p), ("eo", _u8p),
+        ("startBminus", C.c_uint64 * 4), ("startBplus", C.c_uint64 * 4),
+        ("startBminus3d", C.c_uint64 * 4), ("startBplus3d", C.c_uint64 * 4),
+        ("boundarySize", C.c_uint64), ("boundarySize3d", C.c_uint64),
+        ("edge", _u8p), ("edgePoints", C.c_uint64), ("edge0", _u8p), ("edge0Points", C.c_uint64),
+        ("requests", C.c_int * 32), ("numOfRequests", C.c_int),
+        ("stypeV", C.c_int * 4), ("rtypeV", C.c_int * 4), ("stypeU", C.c_int * 4),
+        ("rtypeU", C.c_int * 4), ("stypeT", C.c_int * 4), ("rtypeT", C.c_int * 4),
+        ("stypeP", C.c_int * 4), ("rtypeP", C.c_int * 4),
+        ("initialized", C.c_uint16),
+    ]
+
+
+class QcdVector(C.Structure):
+    """include/qcd.h:90-97."""
+    _fields_ = [("D", C.c_void_p), ("Bplus", C.c_void_p * 4), ("Bminus", C.c_void_p * 4),
+                ("geo", C.POINTER(QcdGeometry)), ("initialized", C.c_uint16)]
+
+
+class QcdGaugeField(C.Structure):
+    """include/qcd.h:119-126."""
+    _fields_ = [("D", C.c_void_p), ("Bplus", C.c_void_p * 4), ("Bminus", C.c_void_p * 4),
+                ("geo", C.POINTER(QcdGeometry)), ("initialized", C.c_uint16)]
+
+
+class QcdComplex16(C.Structure):
+    _fields_ = [("re", C.c_double), ("im", C.c_double)]
+
+
+class SolveParams(C.Structure):
+    """qcdgpu_solve_params (include/qcdgpu.h)."""
+    _fields_ = [("solver", C.c_int), ("op", C.c_int), ("inner_prec", C.c_int), ("tol", C.c_double),
+                ("maxiter", C.c_int), ("restart", C.c_int), ("delta", C.c_double),
+                ("iters", C.c_int), ("reliable_updates", C.c_int), ("true_residual", C.c_double),
+                ("status", C.c_int)]
+
+
+# every symbol include/qcdgpu.h declares (checked against the .so by the tests)
+DROPIN_SYMBOLS = [
+    "qcd_initGeometry", "qcd_destroyGeometry", "qcd_initVector", "qcd_destroyVector",
+    "qcd_initGaugeField", "qcd_destroyGaugeField", "qcd_applyWilsonTMOp",
+    "qcd_applyWilsonTMOpNoScripts", "qcd_applyWilsonTMOpNoOptim", "qcd_applyQTMOp",
+    "qcd_zeroVector", "qcd_setVector", "qcd_copyVector", "qcd_mulVectorC", "qcd_scaleVector",
+    "qcd_subVector", "qcd_addVector", "qcd_axpyVector", "qcd_mulAdjointVectorVector",
+    "qcd_normVector", "qcd_gamma5Vector", "qcd_communicateVectorPMGaugeP", "qcd_waitall",
+    "gcr", "bicgstab", "cgnr",
+]
+
+_lib = None
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+def lib() -> C.CDLL:
+    """The loaded library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is not built; run qcd_gb300.build.build()")
+    L = C.CDLL(LIB_PATH)
+    gp, vp, up = C.POINTER(QcdGeometry), C.POINTER(QcdVector), C.POINTER(QcdGaugeField)
+    L.qcd_initGeometry.argtypes = [gp, C.POINTER(C.c_uint16), C.POINTER(C.c_uint16), C.POINTER(C.c_double), C.c_int, C.c_int]
+    L.qcd_destroyGeometry.argtypes = [gp]
+    L.qcd_initVector.argtypes = [vp, gp]
+    L.qcd_destroyVector.argtypes = [vp]
+    L.qcd_initGaugeField.argtypes = [up, gp]
+    L.qcd_destroyGaugeField.argtypes = [up]
+    for n in ("qcd_applyWilsonTMOp", "qcd_applyWilsonTMOpNoScripts", "qcd_applyWilsonTMOpNoOptim", "qcd_applyQTMOp"):
+        getattr(L, n).argtypes = [vp, vp, up, C.c_double, C.c_double]
+    L.qcd_zeroVector.argtypes = [vp]
+    L.qcd_setVector.argtypes = [vp, QcdComplex16]
+    L.qcd_copyVector.argtypes = [vp, vp]
+    L.qcd_mulVectorC.argtypes = [vp, QcdComplex16]
+    L.qcd_scaleVector.argtypes = [vp, C.c_double]
+    L.qcd_subVector.argtypes = [vp, vp, vp]
+    L.qcd_addVector.argtypes = [vp, vp, vp]
+    L.qcd_axpyVector.argtypes = [vp, QcdComplex16, vp, vp]
+    L.qcd_mulAdjointVectorVector.argtypes = [vp, vp]
+    L.qcd_mulAdjointVectorVector.restype = QcdComplex16
+    L.qcd_normVector.argtypes = [vp]
+    L.qcd_normVector.restype = C.c_double
+    L.qcd_gamma5Vector.argtypes = [vp]
+    L.qcd_communicateVectorPMGaugeP.argtypes = [vp, up]
+    L.qcd_waitall.argtypes = [gp]
+    L.gcr.argtypes = [vp, vp, up, C.c_double, C.c_double, C.c_uint32, gp]
+    L.bicgstab.argtypes = [vp, vp, up, C.c_double, C.c_double, C.c_double, C.c_uint32, gp]
+    L.cgnr.argtypes = [vp, vp, up, C.c_double, C.c_double, C.c_double, C.c_uint32, gp]
+    L.qcdgpu_last_error.restype = C.c_char_p
+    L.qcdgpu_set_stream.argtypes = [C.c_void_p]
+    L.qcdgpu_set_gcr_compat.argtypes = [C.c_int]
+    L.qcdgpu_set_gcr_compat.restype = None
+    L.qcdgpu_set_f64_arith.argtypes = [C.c_int]
+    L.qcdgpu_kernel_launches.restype = C.c_uint64
+    for n in ("qcdgpu_vector_make_resident", "qcdgpu_vector_to_host", "qcdgpu_vector_to_device", "qcdgpu_vector_release"):
+        getattr(L, n).argtypes = [vp]
+    L.qcdgpu_gauge_upload.argtypes = [up]
+    L.qcdgpu_gauge_release.argtypes = [up]
+    vpp = C.POINTER(C.c_void_p)
+    L.qcdgpu_gauge_create.argtypes = [vpp, _ip, _dp, C.c_int]
+    L.qcdgpu_gauge_destroy.argtypes = [C.c_void_p]
+    L.qcdgpu_gauge_load.argtypes = [C.c_void_p, _dp]
+    L.qcdgpu_gauge_store.argtypes = [C.c_void_p, _dp]
+    L.qcdgpu_gauge_convert.argtypes = [C.c_void_p, C.c_void_p]
+    L.qcdgpu_gauge_synthetic.argtypes = [C.c_void_p, C.c_uint64, C.c_double]
+    L.qcdgpu_gauge_recon.argtypes = [C.c_void_p]
+    L.qcdgpu_gauge_bytes.argtypes = [C.c_void_p]
+    L.qcdgpu_gauge_bytes.restype = C.c_size_t
+    L.qcdgpu_plaquette.argtypes = [C.c_void_p]
+    L.qcdgpu_plaquette.restype = C.c_double
+    L.qcdgpu_field_create.argtypes = [vpp, _ip, C.c_int]
+    L.qcdgpu_field_destroy.argtypes = [C.c_void_p]
+    L.qcdgpu_field_load.argtypes = [C.c_void_p, _dp]
+    L.qcdgpu_field_store.argtypes = [C.c_void_p, _dp]
+    L.qcdgpu_field_copy.argtypes = [C.c_void_p, C.c_void_p]
+    L.qcdgpu_field_gaussian.argtypes = [C.c_void_p, C.c_uint64]
+    L.qcdgpu_field_point.argtypes = [C.c_void_p, _ip, C.c_int, C.c_int]
+    L.qcdgpu_field_bytes.argtypes = [C.c_void_p]
+    L.qcdgpu_field_bytes.restype = C.c_size_t
+    L.qcdgpu_field_data.argtypes = [C.c_void_p]
+    L.qcdgpu_field_data.restype = C.c_void_p
+    L.qcdgpu_dslash.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_int]
+    L.qcdgpu_axpy.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_void_p]
+    L.qcdgpu_norm2.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+    L.qcdgpu_dot.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]
+    L.qcdgpu_solve.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.POINTER(SolveParams)]
+    _lib = L
+    return L
+
+
+class QcdGpuError(RuntimeError):
+    pass
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != 0:
+        raise QcdGpuError(f"{what} failed: {lib().qcdgpu_last_error().decode()}")
+
+
+def volume(L) -> int:
+    return int(L[0]) * int(L[1]) * int(L[2]) * int(L[3])
+
+
+# --------------------------------------------------------------- drop-in
+class Geometry:
+    """A qcd_geometry built by the library's qcd_initGeometry (one rank)."""
+
+    def __init__(self, L, theta=(np.pi, 0.0, 0.0, 0.0), P=(1, 1, 1, 1), myid=0, nproc=1):
+        self.s = QcdGeometry()
+        self.L = tuple(int(x) for x in L)
+        Ls = (C.c_uint16 * 4)(*self.L)
+        Ps = (C.c_uint16 * 4)(*P)
+        th = (C.c_double * 4)(*theta)
+        self.rc = lib().qcd_initGeometry(C.byref(self.s), Ls, Ps, th, myid, nproc)
+        self.ok = self.rc == 0
+
+    @property
+    def V(self) -> int:
+        return volume(self.L)
+
+    def close(self):
+        if self.ok:
+            lib().qcd_destroyGeometry(C.byref(self.s))
+            self.ok = False
+
+
+class Vector:
+    """qcd_vector allocated by qcd_initVector; ``a`` is a numpy view of D."""
+
+    def __init__(self, geo: Geometry):
+        self.geo = geo
+        self.s = QcdVector()
+        _check(lib().qcd_initVector(C.byref(self.s), C.byref(geo.s)), "qcd_initVector")
+        buf = (C.c_double * (geo.V * 24)).from_address(self.s.D)
+        self.a = np.ctypeslib.as_array(buf).reshape(geo.V, 4, 3, 2)
+
+    @property
+    def ref(self):
+        return C.byref(self.s)
+
+    def close(self):
+        if self.s.initialized:
+            lib().qcd_destroyVector(C.byref(self.s))
+            self.s.initialized = 0
+
+
+class GaugeField:
+    """qcd_gaugeField allocated by qcd_initGaugeField; ``a`` is a numpy view of D."""
+
+    def __init__(self, geo: Geometry):
+        self.geo = geo
+        self.s = QcdGaugeField()
+        _check(lib().qcd_initGaugeField(C.byref(self.s), C.byref(geo.s)), "qcd_initGaugeField")
+        buf = (C.c_double * (geo.V * 72)).from_address(self.s.D)
+        self.a = np.ctypeslib.as_array(buf).reshape(geo.V, 4, 3, 3, 2)
+
+    @property
+    def ref(self):
+        return C.byref(self.s)
+
+    def close(self):
+        if self.s.initialized:
+            lib().qcd_destroyGaugeField(C.byref(self.s))
+            self.s.initialized = 0
+
+
+# ----------------------------------------------------------- device API
+class Field:
+    """Device spinor field (qcdgpu_field)."""
+
+    def __init__(self, L, prec=F64):
+        self.L = np.ascontiguousarray(L, dtype=np.int32)
+        self.prec = prec
+        h = C.c_void_p()
+        _check(lib().qcdgpu_field_create(C.byref(h), self.L, prec), "qcdgpu_field_create")
+        self.h = h
+
+    @property
+    def V(self) -> int:
+        return volume(self.L)
+
+    def load(self, arr: np.ndarray) -> "Field":
+        _check(lib().qcdgpu_field_load(self.h, np.ascontiguousarray(arr, dtype=np.float64)), "field_load")
+        return self
+
+    def store(self) -> np.ndarray:
+        out = np.empty((self.V, 4, 3, 2))
+        _check(lib().qcdgpu_field_store(self.h, out), "field_store")
+        return out
+
+    def gaussian(self, seed: int) -> "Field":
+        _check(lib().qcdgpu_field_gaussian(self.h, seed), "field_gaussian")
+        return self
+
+    def point(self, x, spin, colour) -> "Field":
+        _check(lib().qcdgpu_field_point(self.h, np.ascontiguousarray(x, dtype=np.int32), spin, colour), "field_point")
+        return self
+
+    def copy_from(self, other: "Field") -> "Field":
+        _check(lib().qcdgpu_field_copy(self.h, other.h), "field_copy")
+        return self
+
+    def norm2(self) -> float:
+        r = C.c_double()
+        _check(lib().qcdgpu_norm2(self.h, C.byref(r)), "norm2")
+        return r.value
+
+    def dot(self, other: "Field") -> complex:
+        r = (C.c_double * 2)()
+        _check(lib().qcdgpu_dot(self.h, other.h, r), "dot")
+        return complex(r[0], r[1])
+
+    @property
+    def nbytes(self) -> int:
+        return lib().qcdgpu_field_bytes(self.h)
+
+    def close(self):
+        if self.h:
+            lib().qcdgpu_field_destroy(self.h)
+            self.h = None
+
+
+class Gauge:
+    """Device gauge field (qcdgpu_gauge)."""
+
+    def __init__(self, L, theta=(np.pi, 0.0, 0.0, 0.0), prec=F64):
+        self.L = np.ascontiguousarray(L, dtype=np.int32)
+        self.theta = np.ascontiguousarray(theta, dtype=np.float64)
+        self.prec = prec
+        h = C.c_void_p()
+        _check(lib().qcdgpu_gauge_create(C.byref(h), self.L, self.theta, prec), "qcdgpu_gauge_create")
+        self.h = h
+
+    def load(self, arr: np.ndarray) -> "Gauge":
+        _check(lib().qcdgpu_gauge_load(self.h, np.ascontiguousarray(arr, dtype=np.float64)), "gauge_load")
+        return self
+
+    def store(self) -> np.ndarray:
+        out = np.empty((volume(self.L), 4, 3, 3, 2))
+        _check(lib().qcdgpu_gauge_store(self.h, out), "gauge_store")
+        return out
+
+    def synthetic(self, seed: int, eps: float) -> "Gauge":
+        _check(lib().qcdgpu_gauge_synthetic(self.h, seed, eps), "gauge_synthetic")
+        return self
+
+    def convert_from(self, other: "Gauge") -> "Gauge":
+        _check(lib().qcdgpu_gauge_convert(self.h, other.h), "gauge_convert")
+        return self
+
+    @property
+    def recon(self) -> int:
+        return lib().qcdgpu_gauge_recon(self.h)
+
+    @property
+    def nbytes(self) -> int:
+        return lib().qcdgpu_gauge_bytes(self.h)
+
+    def plaquette(self) -> float:
+        return lib().qcdgpu_plaquette(self.h)
+
+    def close(self):
+        if self.h:
+            lib().qcdgpu_gauge_destroy(self.h)
+            self.h = None
+
+
+def dslash(out: Field, inp: Field, g: Gauge, kappa: float, mu: float = 0.0, op: int = OP_D, arith: int = -1):
+    _check(lib().qcdgpu_dslash(out.h, inp.h, g.h, kappa, mu, op, arith), "qcdgpu_dslash")
+
+
+def axpy(out: Field, a: complex, x: Field, y: Field):
+    _check(lib().qcdgpu_axpy(out.h, a.real, a.imag, x.h, y.h), "qcdgpu_axpy")
+
+
+def solve(x: Field, b: Field, g: Gauge, kappa: float, mu: float = 0.0, solver=SOLVER_CGNR, op=OP_D,
+          inner_prec=F64, tol=1e-10, maxiter=100000, restart=32, delta=0.1) -> SolveParams:
+    p = SolveParams(solver=solver, op=op, inner_prec=inner_prec, tol=tol, maxiter=maxiter,
+                    restart=restart, delta=delta)
+    rc = lib().qcdgpu_solve(x.h, b.h, g.h, kappa, mu, C.byref(p))
+    if rc == 3:
+        raise QcdGpuError(f"qcdgpu_solve failed: {lib().qcdgpu_last_error().decode()}")
+    return p
+
+
+def set_stream(stream_ptr: int | None):
+    _check(lib().qcdgpu_set_stream(C.c_void_p(stream_ptr or 0)), "set_stream")
+
+
+def sync():
+    _check(lib().qcdgpu_sync(), "sync")
+
+
+def kernel_launches() -> int:
+    return lib().qcdgpu_kernel_launches()

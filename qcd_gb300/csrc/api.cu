@@ -1,0 +1,590 @@
+// api.cu -- qcd_lib entry points on the caller's host structs.
+//
+// Every qcd_vector / qcd_gaugeField seen by an entry point gets a device
+// mirror, found by its data pointer D. Unless the object was made device
+// resident, an entry point uploads each input it reads and writes each
+// output back to host memory before returning, so the caller observes the
+// reference's synchronous semantics. qcd_initVector / qcd_initGaugeField
+// allocate page-locked host memory so these copies run at full link speed.
+#include <stdlib.h>
+#include <string.h>
+
+#include <mutex>
+#include <unordered_map>
+#include <unordered_set>
+
+#include "internal.h"
+
+namespace qg {
+
+qcdgpu_gauge gauge_at(qcdgpu_gauge g, int prec);
+void gauge_forget(qcdgpu_gauge g);
+
+struct VecMirror {
+  qcdgpu_field f = nullptr;
+  bool resident = false;
+};
+struct GaugeMirror {
+  qcdgpu_gauge g = nullptr;
+  bool resident = false;
+};
+
+static std::mutex g_mu;
+static std::unordered_map<const void *, VecMirror> g_vec;
+static std::unordered_map<const void *, GaugeMirror> g_gauge;
+static std::unordered_set<const void *> g_pinned;  // host blocks from cudaMallocHost
+
+static void *host_alloc(size_t bytes)
+{
+  void *p = nullptr;
+  if (cudaMallocHost(&p, bytes) == cudaSuccess) {
+    g_pinned.insert(p);
+    return p;
+  }
+  cudaGetLastError();  // no usable GPU here: plain host memory still works
+  return malloc(bytes);
+}
+
+static void host_free(void *p)
+{
+  if (!p) return;
+  auto it = g_pinned.find(p);
+  if (it != g_pinned.end()) {
+    g_pinned.erase(it);
+    cudaFreeHost(p);
+  } else {
+    free(p);
+  }
+}
+
+static void geo_L(const qcd_geometry *geo, int L[4])
+{
+  for (int i = 0; i < 4; i++) L[i] = geo->L[i];
+}
+
+static bool same_L(const int a[4], const int b[4])
+{
+  return a[0] == b[0] && a[1] == b[1] && a[2] == b[2] && a[3] == b[3];
+}
+
+static VecMirror *vec_mirror(qcd_vector *v)
+{
+  if (!v || !v->initialized || !v->D || !v->geo || v->geo->initialized != 1) {
+    set_error("vector not properly initialized");
+    return nullptr;
+  }
+  int L[4];
+  geo_L(v->geo, L);
+  VecMirror &m = g_vec[(const void *)v->D];
+  if (m.f && !same_L(m.f->L, L)) {
+    field_free(m.f);
+    m.f = nullptr;
+    m.resident = false;
+  }
+  if (!m.f) m.f = field_new(L, QCDGPU_F64);
+  return m.f ? &m : nullptr;
+}
+
+// device field holding v's current value
+static qcdgpu_field vec_in(qcd_vector *v)
+{
+  VecMirror *m = vec_mirror(v);
+  if (!m) return nullptr;
+  if (!m->resident && !upload_spinor_aos(m->f, (const double *)v->D)) return nullptr;
+  return m->f;
+}
+
+// device field that will receive v's new value
+static qcdgpu_field vec_out(qcd_vector *v)
+{
+  VecMirror *m = vec_mirror(v);
+  return m ? m->f : nullptr;
+}
+
+// publish the device result to the host unless v is resident
+static bool vec_done(qcd_vector *v)
+{
+  auto it = g_vec.find((const void *)v->D);
+  if (it == g_vec.end() || !it->second.f) return false;
+  if (it->second.resident) return true;
+  return download_spinor_aos(it->second.f, (double *)v->D);
+}
+
+static qcdgpu_gauge gauge_in(qcd_gaugeField *u)
+{
+  if (!u || !u->initialized || !u->D || !u->geo || u->geo->initialized != 1) {
+    set_error("gauge field not properly initialized");
+    return nullptr;
+  }
+  int L[4];
+  geo_L(u->geo, L);
+  GaugeMirror &m = g_gauge[(const void *)u->D];
+  if (m.g && (!same_L(m.g->L, L) || memcmp(m.g->theta, u->geo->theta, sizeof(m.g->theta)) != 0)) {
+    gauge_forget(m.g);
+    gauge_free(m.g);
+    m.g = nullptr;
+    m.resident = false;
+  }
+  if (m.resident && m.g) return m.g;
+  if (!m.g) m.g = gauge_new(L, u->geo->theta, QCDGPU_F64, 18);
+  if (!m.g) return nullptr;
+  gauge_forget(m.g);  // host data may have changed: drop derived copies
+  if (!upload_gauge_aos(m.g, (const double *)u->D)) return nullptr;
+  return m.g;
+}
+
+// the reference's argument checks (qcd_wilson.c:139-166)
+static bool check_op_args(qcd_vector *Dv, qcd_vector *v, qcd_gaugeField *u)
+{
+  if (!v || !v->initialized) {
+    set_error("Error in qcd_ApplyWilsonTMOp! Vector must be properly initialized");
+    return false;
+  }
+  if (!u || !u->initialized) {
+    set_error("Error in qcd_ApplyWilsonTMOp! Gauge field must be properly initialized");
+    return false;
+  }
+  const qcd_geometry *a = v->geo, *b = u->geo;
+  if (!a || !b || a->initialized != 1 || b->initialized != 1 || memcmp(a->L, b->L, sizeof(a->L)) != 0 ||
+      memcmp(a->lL, b->lL, sizeof(a->lL)) != 0 || memcmp(a->Pos, b->Pos, sizeof(a->Pos)) != 0) {
+    set_error("Error in qcd_ApplyWilsonTMOp! Geometry not initialized or missmatched");
+    return false;
+  }
+  if (!Dv || !Dv->initialized || !Dv->D) {
+    set_error("Error in qcd_ApplyWilsonTMOp! Output vector must be properly initialized");
+    return false;
+  }
+  if (Dv->D == v->D) {
+    set_error("Error in qcd_ApplyWilsonTMOp! Output and input vectors must differ");
+    return false;
+  }
+  return true;
+}
+
+static int apply_op(qcd_vector *Dv, qcd_vector *v, qcd_gaugeField *u, double m, double tm, int op)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!check_op_args(Dv, v, u)) return 1;
+  if (v->geo->numOfRequests != 0) {
+    set_error("process %u: Error in qcd_communicateVectorPMGaugeP! Previous communication not finished",
+              v->geo->myid);
+    return 1;
+  }
+  qcdgpu_gauge g = gauge_in(u);
+  if (!g) return 1;
+  qcdgpu_field in = vec_in(v);
+  qcdgpu_field out = vec_out(Dv);
+  if (!in || !out) return 1;
+  if (!dslash(out, in, g, 4.0 + m, tm, op, -1)) return 1;
+  return vec_done(Dv) ? 0 : 1;
+}
+
+}  // namespace qg
+
+using namespace qg;
+
+extern "C" {
+
+// ------------------------------------------------------------- geometry
+int qcd_initGeometry(qcd_geometry *geo, const qcd_uint_2 L[], const qcd_uint_2 P[], const qcd_real_8 theta[],
+                     const int myid, const int numprocs)
+{
+  // checks of qcd_init.c:31-52, plus the single-GPU restriction
+  if (L[0] % P[0] || L[1] % P[1] || L[2] % P[2] || L[3] % P[3]) {
+    set_error("process %i: Error in qcd_initGeometry! %i x %i x %i x %i cannot be subdivided in %i x %i x %i x %i",
+              myid, L[0], L[1], L[2], L[3], P[0], P[1], P[2], P[3]);
+    return 1;
+  }
+  if (P[0] != 1 || P[1] != 1 || P[2] != 1 || P[3] != 1 || numprocs != 1 || myid != 0) {
+    set_error("process %i: Error in qcd_initGeometry! one GPU holds the whole lattice: P must be 1 1 1 1 "
+              "with one process", myid);
+    return 1;
+  }
+  if (L[0] < 2 || L[1] < 2 || L[2] < 2 || L[3] < 2) {
+    set_error("process %i: Error in qcd_initGeometry! Local lattices must be at least 2x2x2x2", myid);
+    return 1;
+  }
+  if (((uint64_t)L[0] * L[1] * L[2] * L[3]) % 2) {
+    set_error("process %i: Error in qcd_initGeometry! Local volume must be multiple of 2.", myid);
+    return 1;
+  }
+  memset(geo, 0, sizeof(*geo));
+  for (int i = 0; i < 4; i++) {
+    geo->L[i] = L[i];
+    geo->lL[i] = L[i];
+    geo->theta[i] = theta[i];
+  }
+  const uint64_t Lt = L[0], Lx = L[1], Ly = L[2], Lz = L[3];
+  geo->V = geo->lV = Lt * Lx * Ly * Lz;
+  geo->V3 = geo->lV3 = Lx * Ly * Lz;
+  geo->myid = 0;
+  geo->nproc = 1;
+  geo->plus = (qcd_uint_8(*)[4])malloc(sizeof(qcd_uint_8) * 4 * geo->lV);
+  geo->minus = (qcd_uint_8(*)[4])malloc(sizeof(qcd_uint_8) * 4 * geo->lV);
+  geo->plus3d = (qcd_uint_8(*)[4])malloc(sizeof(qcd_uint_8) * 4 * geo->lV3);
+  geo->minus3d = (qcd_uint_8(*)[4])malloc(sizeof(qcd_uint_8) * 4 * geo->lV3);
+  geo->eo = (qcd_uint_8(*)[2])malloc(sizeof(qcd_uint_8) * geo->lV);
+  geo->edgePoints = geo->lV - (Lt - 2) * (Lx - 2) * (Ly - 2) * (Lz - 2);
+  geo->edge0Points = geo->lV3 - (Lx - 2) * (Ly - 2) * (Lz - 2);
+  geo->edge = (qcd_uint_8 *)malloc(sizeof(qcd_uint_8) * (geo->edgePoints ? geo->edgePoints : 1));
+  geo->edge0 = (qcd_uint_8 *)malloc(sizeof(qcd_uint_8) * (geo->edge0Points ? geo->edge0Points : 1));
+  if (!geo->plus || !geo->minus || !geo->plus3d || !geo->minus3d || !geo->eo || !geo->edge || !geo->edge0) {
+    set_error("process %i: Error in qcd_initGeometry! Out of memory", myid);
+    return 1;
+  }
+  // periodic neighbour tables (qcd_init.c:110-124 at one rank), t fastest
+  auto lex = [&](uint64_t t, uint64_t x, uint64_t y, uint64_t z) { return t + Lt * (x + Lx * (y + Ly * z)); };
+  uint64_t j = 0, ne = 0, no = 0;
+  for (uint64_t z = 0; z < Lz; z++)
+    for (uint64_t y = 0; y < Ly; y++)
+      for (uint64_t x = 0; x < Lx; x++)
+        for (uint64_t t = 0; t < Lt; t++) {
+          uint64_t i = lex(t, x, y, z);
+          geo->plus[i][0] = lex((t + 1) % Lt, x, y, z);
+          geo->plus[i][1] = lex(t, (x + 1) % Lx, y, z);
+          geo->plus[i][2] = lex(t, x, (y + 1) % Ly, z);
+          geo->plus[i][3] = lex(t, x, y, (z + 1) % Lz);
+          geo->minus[i][0] = lex((t + Lt - 1) % Lt, x, y, z);
+          geo->minus[i][1] = lex(t, (x + Lx - 1) % Lx, y, z);
+          geo->minus[i][2] = lex(t, x, (y + Ly - 1) % Ly, z);
+          geo->minus[i][3] = lex(t, x, y, (z + Lz - 1) % Lz);
+          if (z == 0 || z == Lz - 1 || y == 0 || y == Ly - 1 || x == 0 || x == Lx - 1 || t == 0 || t == Lt - 1)
+            geo->edge[j++] = i;
+          // even/odd split (qcd_init.c:315-335): (0,0,0,0) is even at one rank
+          // when sum_mu P_mu lL_mu = sum_mu L_mu is even
+          uint64_t b = (Lt + Lx + Ly + Lz) % 2;
+          if ((t + x + y + z + b) % 2) geo->eo[no++][1] = i;
+          else geo->eo[ne++][0] = i;
+        }
+  j = 0;
+  for (uint64_t z = 0; z < Lz; z++)
+    for (uint64_t y = 0; y < Ly; y++)
+      for (uint64_t x = 0; x < Lx; x++) {
+        uint64_t i = x + Lx * (y + Ly * z);
+        geo->plus3d[i][1] = ((x + 1) % Lx) + Lx * (y + Ly * z);
+        geo->plus3d[i][2] = x + Lx * (((y + 1) % Ly) + Ly * z);
+        geo->plus3d[i][3] = x + Lx * (y + Ly * ((z + 1) % Lz));
+        geo->minus3d[i][1] = ((x + Lx - 1) % Lx) + Lx * (y + Ly * z);
+        geo->minus3d[i][2] = x + Lx * (((y + Ly - 1) % Ly) + Ly * z);
+        geo->minus3d[i][3] = x + Lx * (y + Ly * ((z + Lz - 1) % Lz));
+        if (z == 0 || z == Lz - 1 || y == 0 || y == Ly - 1 || x == 0 || x == Lx - 1) geo->edge0[j++] = i;
+      }
+  geo->numOfRequests = 0;
+  geo->initialized = 1;
+  return 0;
+}
+
+void qcd_destroyGeometry(const qcd_geometry *geo)
+{
+  free(geo->plus);
+  free(geo->minus);
+  free(geo->plus3d);
+  free(geo->minus3d);
+  free(geo->edge);
+  free(geo->edge0);
+  free(geo->eo);
+}
+
+// --------------------------------------------------------------- fields
+int qcd_initVector(qcd_vector *vec, qcd_geometry *geo)
+{
+  if (!geo->initialized) {
+    set_error("error in qcd_initVector! Geometry must be properly initialized.");
+    return 1;
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  memset(vec, 0, sizeof(*vec));
+  vec->D = (qcd_complex_16(*)[4][3])host_alloc(sizeof(qcd_complex_16) * 12 * geo->lV);
+  if (!vec->D) {
+    set_error("process %i: Error in qcd_initVector! Out of memory", geo->myid);
+    return 1;
+  }
+  vec->geo = geo;
+  vec->initialized = 1;
+  return 0;
+}
+
+void qcd_destroyVector(qcd_vector *vec)
+{
+  if (!vec->initialized) {
+    fprintf(stderr, "Error in qcd_destroyVector! Vector not initialized\n");
+    return;
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_vec.find((const void *)vec->D);
+  if (it != g_vec.end()) {
+    field_free(it->second.f);
+    g_vec.erase(it);
+  }
+  host_free(vec->D);
+}
+
+int qcd_initGaugeField(qcd_gaugeField *u, qcd_geometry *geo)
+{
+  if (!geo->initialized) {
+    set_error("error in qcd_initGaugeField! Geometry must be properly initialized.");
+    return 1;
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  memset(u, 0, sizeof(*u));
+  u->D = (qcd_complex_16(*)[4][3][3])host_alloc(sizeof(qcd_complex_16) * 36 * geo->lV);
+  if (!u->D) {
+    set_error("process %i: Error in qcd_initGaugeField! Out of memory", geo->myid);
+    return 1;
+  }
+  u->geo = geo;
+  u->initialized = 1;
+  return 0;
+}
+
+void qcd_destroyGaugeField(qcd_gaugeField *u)
+{
+  if (!u->initialized) {
+    fprintf(stderr, "Error in qcd_destroyGaugeField! Gauge field not initialized\n");
+    return;
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_gauge.find((const void *)u->D);
+  if (it != g_gauge.end()) {
+    gauge_forget(it->second.g);
+    gauge_free(it->second.g);
+    g_gauge.erase(it);
+  }
+  host_free(u->D);
+}
+
+// ------------------------------------------------------------ operators
+int qcd_applyWilsonTMOp(qcd_vector *Dv, qcd_vector *v, qcd_gaugeField *u, qcd_real_8 m, qcd_real_8 tm)
+{
+  return apply_op(Dv, v, u, m, tm, QCDGPU_OP_D);
+}
+int qcd_applyWilsonTMOpNoScripts(qcd_vector *Dv, qcd_vector *v, qcd_gaugeField *u, qcd_real_8 m, qcd_real_8 tm)
+{
+  return apply_op(Dv, v, u, m, tm, QCDGPU_OP_D);
+}
+int qcd_applyWilsonTMOpNoOptim(qcd_vector *Dv, qcd_vector *v, qcd_gaugeField *u, qcd_real_8 m, qcd_real_8 tm)
+{
+  return apply_op(Dv, v, u, m, tm, QCDGPU_OP_D);
+}
+int qcd_applyQTMOp(qcd_vector *Dv, qcd_vector *v, qcd_gaugeField *u, qcd_real_8 m, qcd_real_8 tm)
+{
+  return apply_op(Dv, v, u, m, tm, QCDGPU_OP_Q);
+}
+
+// ----------------------------------------------------------------- BLAS
+#define QG_BLAS_GUARD std::lock_guard<std::mutex> lk(g_mu)
+
+void qcd_zeroVector(qcd_vector *vec)
+{
+  QG_BLAS_GUARD;
+  qcdgpu_field f = vec_out(vec);
+  if (f && blas_zero(f)) vec_done(vec);
+}
+
+void qcd_setVector(qcd_vector *vec, qcd_complex_16 c)
+{
+  QG_BLAS_GUARD;
+  qcdgpu_field f = vec_out(vec);
+  if (f && blas_set(f, c.re, c.im)) vec_done(vec);
+}
+
+void qcd_copyVector(qcd_vector *dest, qcd_vector *src)
+{
+  QG_BLAS_GUARD;
+  qcdgpu_field s = vec_in(src);
+  qcdgpu_field d = s ? vec_out(dest) : nullptr;
+  if (d && blas_copy(d, s)) vec_done(dest);
+}
+
+void qcd_mulVectorC(qcd_vector *vec, qcd_complex_16 c)
+{
+  QG_BLAS_GUARD;
+  qcdgpu_field f = vec_in(vec);
+  if (f && blas_axpby(f, c.re, c.im, f, 0.0, 0.0, f)) vec_done(vec);
+}
+
+void qcd_scaleVector(qcd_vector *vec, qcd_real_8 r)
+{
+  QG_BLAS_GUARD;
+  qcdgpu_field f = vec_in(vec);
+  if (f && blas_axpby(f, r, 0.0, f, 0.0, 0.0, f)) vec_done(vec);
+}
+
+static void lincomb(qcd_vector *out, double ar, double ai, qcd_vector *x, double br, double bi, qcd_vector *y)
+{
+  qcdgpu_field fx = vec_in(x);
+  qcdgpu_field fy = fx ? (y->D == x->D ? fx : vec_in(y)) : nullptr;
+  qcdgpu_field fo = fy ? vec_out(out) : nullptr;
+  if (fo && blas_axpby(fo, ar, ai, fx, br, bi, fy)) vec_done(out);
+}
+
+void qcd_subVector(qcd_vector *difference, qcd_vector *minuend, qcd_vector *subtrahend)
+{
+  QG_BLAS_GUARD;
+  lincomb(difference, 1.0, 0.0, minuend, -1.0, 0.0, subtrahend);
+}
+
+void qcd_addVector(qcd_vector *sum, qcd_vector *summand1, qcd_vector *summand2)
+{
+  QG_BLAS_GUARD;
+  lincomb(sum, 1.0, 0.0, summand1, 1.0, 0.0, summand2);
+}
+
+void qcd_axpyVector(qcd_vector *axpy, qcd_complex_16 a, qcd_vector *x, qcd_vector *y)
+{
+  QG_BLAS_GUARD;
+  lincomb(axpy, a.re, a.im, x, 1.0, 0.0, y);
+}
+
+qcd_complex_16 qcd_mulAdjointVectorVector(qcd_vector *factor1, qcd_vector *factor2)
+{
+  QG_BLAS_GUARD;
+  qcd_complex_16 r = {NAN, NAN};
+  qcdgpu_field a = vec_in(factor1);
+  qcdgpu_field b = a ? (factor2->D == factor1->D ? a : vec_in(factor2)) : nullptr;
+  double d[2];
+  if (b && blas_dot(a, b, d)) {
+    r.re = d[0];
+    r.im = d[1];
+  }
+  return r;
+}
+
+qcd_real_8 qcd_normVector(qcd_vector *vec)
+{
+  QG_BLAS_GUARD;
+  qcdgpu_field f = vec_in(vec);
+  double n2;
+  if (f && blas_norm2(f, &n2)) return sqrt(n2);
+  return NAN;
+}
+
+void qcd_gamma5Vector(qcd_vector *v)
+{
+  QG_BLAS_GUARD;
+  qcdgpu_field f = vec_in(v);
+  if (f && blas_gamma5(f, f)) vec_done(v);
+}
+
+// -------------------------------------------------------- communication
+int qcd_communicateVectorPMGaugeP(qcd_vector *v, qcd_gaugeField *u)
+{
+  (void)u;
+  if (v->geo->numOfRequests != 0) {
+    set_error("process %u: Error in qcd_communicateVectorPMGaugeP! Previous communication not finished",
+              v->geo->myid);
+    return 1;
+  }
+  return 0;  // one GPU holds the whole lattice: there is no halo to send
+}
+
+void qcd_waitall(qcd_geometry *geo) { geo->numOfRequests = 0; }
+
+// --------------------------------------------------------------- solvers
+qcd_int_4 gcr(qcd_vector *sol, qcd_vector *src, qcd_gaugeField *u, qcd_real_8 kappa, qcd_real_8 muTM,
+              qcd_uint_4 n, qcd_geometry *geo)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  (void)geo;
+  if (!check_op_args(sol, src, u)) return EXIT_FAILURE;
+  qcdgpu_gauge g = gauge_in(u);
+  qcdgpu_field b = g ? vec_in(src) : nullptr;
+  qcdgpu_field x = b ? vec_out(sol) : nullptr;
+  if (!x) return EXIT_FAILURE;
+  // m = 1/(2 kappa) - 4 as the callers pass it (invert.c:46), diagonal m + 4
+  double mp4 = (1.0 / (2.0 * kappa) - 4.0) + 4.0;
+  if (gcr_dropin(x, b, g, mp4, muTM, (int)n, g_gcr_shipped)) return EXIT_FAILURE;
+  return vec_done(sol) ? 0 : EXIT_FAILURE;
+}
+
+static qcd_int_4 solve_dropin(int solver, qcd_vector *sol, qcd_vector *src, qcd_gaugeField *u, double kappa,
+                              double mu, double tol, unsigned maxiter)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!check_op_args(sol, src, u)) return -1;
+  qcdgpu_gauge g = gauge_in(u);
+  qcdgpu_field b = g ? vec_in(src) : nullptr;
+  qcdgpu_field x = b ? vec_out(sol) : nullptr;
+  if (!x) return -1;
+  qcdgpu_solve_params p;
+  memset(&p, 0, sizeof(p));
+  p.solver = solver;
+  p.op = QCDGPU_OP_D;
+  p.inner_prec = QCDGPU_F64;
+  p.tol = tol;
+  p.maxiter = (int)maxiter;
+  double mp4 = (1.0 / (2.0 * kappa) - 4.0) + 4.0;
+  int st = solve(x, b, g, mp4, mu, &p);
+  if (!vec_done(sol)) return -1;
+  return st == 0 ? p.iters : -1;
+}
+
+qcd_int_4 bicgstab(qcd_vector *sol, qcd_vector *src, qcd_gaugeField *u, qcd_real_8 kappa, qcd_real_8 muTM,
+                   qcd_real_8 tol, qcd_uint_4 maxiter, qcd_geometry *geo)
+{
+  (void)geo;
+  return solve_dropin(QCDGPU_SOLVER_BICGSTAB, sol, src, u, kappa, muTM, tol, maxiter);
+}
+
+qcd_int_4 cgnr(qcd_vector *sol, qcd_vector *src, qcd_gaugeField *u, qcd_real_8 kappa, qcd_real_8 muTM,
+               qcd_real_8 tol, qcd_uint_4 maxiter, qcd_geometry *geo)
+{
+  (void)geo;
+  return solve_dropin(QCDGPU_SOLVER_CGNR, sol, src, u, kappa, muTM, tol, maxiter);
+}
+
+// ------------------------------------------------------------ residency
+int qcdgpu_vector_make_resident(qcd_vector *v)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  VecMirror *m = vec_mirror(v);
+  if (!m) return 1;
+  if (!m->resident && !upload_spinor_aos(m->f, (const double *)v->D)) return 1;
+  m->resident = true;
+  return 0;
+}
+
+int qcdgpu_vector_to_host(qcd_vector *v)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  VecMirror *m = vec_mirror(v);
+  return m && download_spinor_aos(m->f, (double *)v->D) ? 0 : 1;
+}
+
+int qcdgpu_vector_to_device(qcd_vector *v)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  VecMirror *m = vec_mirror(v);
+  return m && upload_spinor_aos(m->f, (const double *)v->D) ? 0 : 1;
+}
+
+int qcdgpu_vector_release(qcd_vector *v)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  VecMirror *m = vec_mirror(v);
+  if (!m) return 1;
+  if (m->resident && !download_spinor_aos(m->f, (double *)v->D)) return 1;
+  m->resident = false;
+  return 0;
+}
+
+int qcdgpu_gauge_upload(qcd_gaugeField *u)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_gauge.find((const void *)u->D);
+  if (it != g_gauge.end()) it->second.resident = false;  // force a fresh upload
+  qcdgpu_gauge g = gauge_in(u);
+  if (!g) return 1;
+  g_gauge[(const void *)u->D].resident = true;
+  return 0;
+}
+
+int qcdgpu_gauge_release(qcd_gaugeField *u)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_gauge.find((const void *)u->D);
+  if (it != g_gauge.end()) it->second.resident = false;
+  return 0;
+}
+
+}  // extern "C"

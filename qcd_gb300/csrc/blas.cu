@@ -1,0 +1,329 @@
+// blas.cu -- BLAS-1 and reductions on device spinor fields
+// (qcd_blas.c:137-492: zero, set, copy, scale, mulC, add, sub, axpy, the
+// complex dot <a,b> = sum conj(a) b and the 2-norm).
+//
+// Kernels work one site per thread through the precision accessors, so the
+// same code serves FP64, FP32 and FP16(+norm) storage. Reductions accumulate
+// in double: each block reduces with warp shuffles into one partial, and a
+// single block sums the partials in a fixed order, so results do not depend
+// on scheduling (the reference's MPI_Allreduce becomes this second pass).
+#include <string.h>
+
+#include "internal.h"
+
+namespace qg {
+
+using namespace qgd;
+
+static inline unsigned grid_sites(int64_t V) { return (unsigned)((V + 127) / 128); }
+
+// -------------------------------------------------------------- elementwise
+template <int P, typename R>
+__global__ void k_axpby(void *out, float *onorm, R ar, R ai, const void *x, const float *xn, R br,
+                        R bi, const void *y, const float *yn, int64_t stride, int64_t V)
+{
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= V) return;
+  C<R> a{ar, ai}, b{br, bi}, vx[12], vy[12];
+  Spinor<P, R>::load(x, xn, stride, s, vx);
+  Spinor<P, R>::load(y, yn, stride, s, vy);
+#pragma unroll
+  for (int k = 0; k < 12; k++) vx[k] = a * vx[k] + b * vy[k];
+  Spinor<P, R>::store(out, onorm, stride, s, vx);
+}
+
+// y = a x + y with real a: one fused multiply-add per real
+template <int P, typename R>
+__global__ void k_axpy_real(void *y, float *yn, R a, const void *x, const float *xn, int64_t stride,
+                            int64_t V)
+{
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= V) return;
+  C<R> vx[12], vy[12];
+  Spinor<P, R>::load(x, xn, stride, s, vx);
+  Spinor<P, R>::load(y, yn, stride, s, vy);
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    vy[k].re = qfma(a, vx[k].re, vy[k].re);
+    vy[k].im = qfma(a, vx[k].im, vy[k].im);
+  }
+  Spinor<P, R>::store(y, yn, stride, s, vy);
+}
+
+template <int P, typename R>
+__global__ void k_set(void *out, float *onorm, R cr, R ci, int64_t stride, int64_t V)
+{
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= V) return;
+  C<R> v[12];
+#pragma unroll
+  for (int k = 0; k < 12; k++) v[k] = C<R>{cr, ci};
+  Spinor<P, R>::store(out, onorm, stride, s, v);
+}
+
+// mode 0: g5 in ; mode 1: i g5 in
+template <int P, typename R>
+__global__ void k_g5(void *out, float *onorm, const void *in, const float *inorm, int mode,
+                     int64_t stride, int64_t V)
+{
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= V) return;
+  C<R> v[12];
+  Spinor<P, R>::load(in, inorm, stride, s, v);
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    C<R> w = mode ? mul_i(v[k]) : v[k];
+    v[k] = k < 6 ? w : -w;
+  }
+  Spinor<P, R>::store(out, onorm, stride, s, v);
+}
+
+// --------------------------------------------------------------- reductions
+__device__ __forceinline__ double warp_sum(double v)
+{
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// block-level sum of (v0, v1) into partials[2*blockIdx.x + {0,1}]
+__device__ __forceinline__ void block_sum2(double v0, double v1, double *partials)
+{
+  __shared__ double sh[2][32];
+  v0 = warp_sum(v0);
+  v1 = warp_sum(v1);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sh[0][w] = v0;
+    sh[1][w] = v1;
+  }
+  __syncthreads();
+  if (w == 0) {
+    int nw = blockDim.x >> 5;
+    v0 = l < nw ? sh[0][l] : 0.0;
+    v1 = l < nw ? sh[1][l] : 0.0;
+    v0 = warp_sum(v0);
+    v1 = warp_sum(v1);
+    if (l == 0) {
+      partials[2 * blockIdx.x] = v0;
+      partials[2 * blockIdx.x + 1] = v1;
+    }
+  }
+}
+
+// kind 0: |a|^2 ; kind 1: <a,b> ; kind 2: b = b + (ar,ai) a, then |b|^2
+template <int P, typename R, int KIND>
+__global__ void __launch_bounds__(256) k_reduce(const void *a, const float *an, void *b, float *bn,
+                                                R ar, R ai, int64_t stride, int64_t V, double *partials)
+{
+  double s0 = 0, s1 = 0;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < V;
+       s += (int64_t)gridDim.x * blockDim.x) {
+    C<R> va[12];
+    Spinor<P, R>::load(a, an, stride, s, va);
+    if (KIND == 0) {
+#pragma unroll
+      for (int k = 0; k < 12; k++) s0 += (double)va[k].re * va[k].re + (double)va[k].im * va[k].im;
+    } else if (KIND == 1) {
+      C<R> vb[12];
+      Spinor<P, R>::load(b, bn, stride, s, vb);
+#pragma unroll
+      for (int k = 0; k < 12; k++) {
+        s0 += (double)va[k].re * vb[k].re + (double)va[k].im * vb[k].im;
+        s1 += (double)va[k].re * vb[k].im - (double)va[k].im * vb[k].re;
+      }
+    } else {
+      C<R> vb[12], c{ar, ai};
+      Spinor<P, R>::load(b, bn, stride, s, vb);
+#pragma unroll
+      for (int k = 0; k < 12; k++) {
+        vb[k] = vb[k] + c * va[k];
+        s0 += (double)vb[k].re * vb[k].re + (double)vb[k].im * vb[k].im;
+      }
+      Spinor<P, R>::store(b, bn, stride, s, vb);
+    }
+  }
+  block_sum2(s0, s1, partials);
+}
+
+// one block: res[0..1] = sum of n partial pairs, in index order per lane
+__global__ void k_finalize(const double *partials, int n, double *res)
+{
+  double v0 = 0, v1 = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    v0 += partials[2 * i];
+    v1 += partials[2 * i + 1];
+  }
+  __shared__ double sh[2][32];
+  v0 = warp_sum(v0);
+  v1 = warp_sum(v1);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sh[0][w] = v0;
+    sh[1][w] = v1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0, b = 0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+      a += sh[0][i];
+      b += sh[1][i];
+    }
+    res[0] = a;
+    res[1] = b;
+  }
+}
+
+static int reduce_blocks(int64_t V)
+{
+  int64_t n = (V + 255) / 256;
+  return (int)(n < kMaxPartials ? n : kMaxPartials);
+}
+
+// --------------------------------------------------------------- dispatch
+#define QG_DISPATCH(prec, F64CALL, F32CALL, F16CALL) \
+  do {                                               \
+    if ((prec) == QCDGPU_F64) { F64CALL; }           \
+    else if ((prec) == QCDGPU_F32) { F32CALL; }      \
+    else { F16CALL; }                                \
+  } while (0)
+
+bool blas_zero(qcdgpu_field x) { return QG_CUDA(cudaMemsetAsync(x->data, 0, x->bytes, stream())); }
+
+bool blas_copy(qcdgpu_field d, qcdgpu_field s)
+{
+  if (!same_shape(d, s) || d->prec != s->prec) {
+    set_error("copy: fields differ in shape or precision");
+    return false;
+  }
+  if (d == s) return true;
+  return QG_CUDA(cudaMemcpyAsync(d->data, s->data, d->bytes, cudaMemcpyDeviceToDevice, stream()));
+}
+
+bool blas_axpby(qcdgpu_field out, double ar, double ai, qcdgpu_field x, double br, double bi, qcdgpu_field y)
+{
+  if (!same_shape(out, x) || !same_shape(out, y) || out->prec != x->prec || out->prec != y->prec) {
+    set_error("axpby: fields differ in shape or precision");
+    return false;
+  }
+  unsigned g = grid_sites(out->V);
+  cudaStream_t st = stream();
+  if (ai == 0.0 && br == 1.0 && bi == 0.0 && out == y) {
+    QG_DISPATCH(out->prec,
+                (k_axpy_real<QCDGPU_F64, double><<<g, 128, 0, st>>>(y->data, y->norm, ar, x->data, x->norm, out->stride, out->V)),
+                (k_axpy_real<QCDGPU_F32, float><<<g, 128, 0, st>>>(y->data, y->norm, (float)ar, x->data, x->norm, out->stride, out->V)),
+                (k_axpy_real<QCDGPU_F16, float><<<g, 128, 0, st>>>(y->data, y->norm, (float)ar, x->data, x->norm, out->stride, out->V)));
+    return QG_LAUNCHED("axpy_real");
+  }
+  QG_DISPATCH(out->prec,
+              (k_axpby<QCDGPU_F64, double><<<g, 128, 0, st>>>(out->data, out->norm, ar, ai, x->data, x->norm, br, bi, y->data, y->norm, out->stride, out->V)),
+              (k_axpby<QCDGPU_F32, float><<<g, 128, 0, st>>>(out->data, out->norm, (float)ar, (float)ai, x->data, x->norm, (float)br, (float)bi, y->data, y->norm, out->stride, out->V)),
+              (k_axpby<QCDGPU_F16, float><<<g, 128, 0, st>>>(out->data, out->norm, (float)ar, (float)ai, x->data, x->norm, (float)br, (float)bi, y->data, y->norm, out->stride, out->V)));
+  return QG_LAUNCHED("axpby");
+}
+
+bool blas_set(qcdgpu_field x, double cr, double ci)
+{
+  unsigned g = grid_sites(x->V);
+  cudaStream_t st = stream();
+  QG_DISPATCH(x->prec,
+              (k_set<QCDGPU_F64, double><<<g, 128, 0, st>>>(x->data, x->norm, cr, ci, x->stride, x->V)),
+              (k_set<QCDGPU_F32, float><<<g, 128, 0, st>>>(x->data, x->norm, (float)cr, (float)ci, x->stride, x->V)),
+              (k_set<QCDGPU_F16, float><<<g, 128, 0, st>>>(x->data, x->norm, (float)cr, (float)ci, x->stride, x->V)));
+  return QG_LAUNCHED("set");
+}
+
+static bool g5_common(qcdgpu_field out, qcdgpu_field in, int mode)
+{
+  if (!same_shape(out, in) || out->prec != in->prec) {
+    set_error("gamma5: fields differ in shape or precision");
+    return false;
+  }
+  unsigned g = grid_sites(out->V);
+  cudaStream_t st = stream();
+  QG_DISPATCH(out->prec,
+              (k_g5<QCDGPU_F64, double><<<g, 128, 0, st>>>(out->data, out->norm, in->data, in->norm, mode, out->stride, out->V)),
+              (k_g5<QCDGPU_F32, float><<<g, 128, 0, st>>>(out->data, out->norm, in->data, in->norm, mode, out->stride, out->V)),
+              (k_g5<QCDGPU_F16, float><<<g, 128, 0, st>>>(out->data, out->norm, in->data, in->norm, mode, out->stride, out->V)));
+  return QG_LAUNCHED("gamma5");
+}
+bool blas_gamma5(qcdgpu_field out, qcdgpu_field in) { return g5_common(out, in, 0); }
+bool blas_ig5(qcdgpu_field out, qcdgpu_field in) { return g5_common(out, in, 1); }
+
+template <int KIND>
+static bool reduce_common(qcdgpu_field a, qcdgpu_field b, double ar, double ai, double *res)
+{
+  double *part = reduce_scratch();
+  if (!part) return false;
+  int nb = reduce_blocks(a->V);
+  cudaStream_t st = stream();
+  const void *bd = b ? b->data : nullptr;
+  float *bn = b ? b->norm : nullptr;
+  QG_DISPATCH(a->prec,
+              (k_reduce<QCDGPU_F64, double, KIND><<<nb, 256, 0, st>>>(a->data, a->norm, (void *)bd, bn, ar, ai, a->stride, a->V, part)),
+              (k_reduce<QCDGPU_F32, float, KIND><<<nb, 256, 0, st>>>(a->data, a->norm, (void *)bd, bn, (float)ar, (float)ai, a->stride, a->V, part)),
+              (k_reduce<QCDGPU_F16, float, KIND><<<nb, 256, 0, st>>>(a->data, a->norm, (void *)bd, bn, (float)ar, (float)ai, a->stride, a->V, part)));
+  if (!QG_LAUNCHED("reduce")) return false;
+  k_finalize<<<1, 256, 0, st>>>(part, nb, res);
+  return QG_LAUNCHED("reduce_finalize");
+}
+
+bool blas_norm2_dev(qcdgpu_field x, double *res) { return reduce_common<0>(x, nullptr, 0, 0, res); }
+
+bool blas_dot_dev(qcdgpu_field a, qcdgpu_field b, double *res)
+{
+  if (!same_shape(a, b) || a->prec != b->prec) {
+    set_error("dot: fields differ in shape or precision");
+    return false;
+  }
+  return reduce_common<1>(a, b, 0, 0, res);
+}
+
+bool blas_axpy_norm2_dev(qcdgpu_field y, double ar, double ai, qcdgpu_field x, double *res)
+{
+  if (!same_shape(x, y) || x->prec != y->prec) {
+    set_error("axpy_norm: fields differ in shape or precision");
+    return false;
+  }
+  return reduce_common<2>(x, y, ar, ai, res);
+}
+
+static bool fetch(double *dev_res, double *out, int n)
+{
+  double *h = host_result();
+  if (!h) return false;
+  if (!QG_CUDA(cudaMemcpyAsync(h, dev_res, sizeof(double) * n, cudaMemcpyDeviceToHost, stream()))) return false;
+  if (!QG_CUDA(cudaStreamSynchronize(stream()))) return false;
+  memcpy(out, h, sizeof(double) * n);
+  return true;
+}
+
+bool blas_norm2(qcdgpu_field x, double *out)
+{
+  double *r = reduce_scratch();
+  if (!r) return false;
+  r += 2 * kMaxPartials;
+  return blas_norm2_dev(x, r) && fetch(r, out, 1);
+}
+
+bool blas_dot(qcdgpu_field a, qcdgpu_field b, double out[2])
+{
+  double *r = reduce_scratch();
+  if (!r) return false;
+  r += 2 * kMaxPartials;
+  return blas_dot_dev(a, b, r) && fetch(r, out, 2);
+}
+
+}  // namespace qg
+
+extern "C" {
+
+int qcdgpu_axpy(qcdgpu_field out, double are, double aim, qcdgpu_field x, qcdgpu_field y)
+{
+  return qg::blas_axpby(out, are, aim, x, 1.0, 0.0, y) ? 0 : 1;
+}
+
+int qcdgpu_norm2(qcdgpu_field x, double *result) { return qg::blas_norm2(x, result) ? 0 : 1; }
+
+int qcdgpu_dot(qcdgpu_field a, qcdgpu_field b, double result[2]) { return qg::blas_dot(a, b, result) ? 0 : 1; }
+
+}  // extern "C"

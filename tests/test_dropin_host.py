@@ -1,0 +1,131 @@
+"""Host-side behaviour of the drop-in C ABI (no GPU needed): the library
+loads, exports every declared symbol, keeps the qcd.h struct layout, builds
+the reference's geometry tables and returns the reference's error codes."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import qcd_gb300 as q
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "qcdgpu.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    # function declarations, not the pointer-to-array members "(*D)[4][3]"
+    names = set(re.findall(r"\b((?:qcd|qcdgpu)_\w+|gcr|bicgstab|cgnr)\s*\((?!\s*\*)", src))
+    return sorted(n for n in names if not n.endswith("_s"))
+
+
+def test_library_exports_every_declared_symbol(qlib):
+    names = declared_functions()
+    assert len(names) > 40
+    missing = [n for n in names if not hasattr(qlib, n)]
+    assert not missing, missing
+    for n in q.DROPIN_SYMBOLS:
+        assert n in names
+
+
+def test_struct_layout_matches_reference(ref):
+    assert C.sizeof(q.QcdGeometry) == ref.lib.ref_sizeof_geometry()
+    assert C.sizeof(q.QcdVector) == ref.lib.ref_sizeof_vector()
+    assert C.sizeof(q.QcdGaugeField) == ref.lib.ref_sizeof_gauge()
+
+
+def test_struct_layout_offsets():
+    # LP64 layout of include/qcd.h with int-sized MPI handles
+    assert C.sizeof(q.QcdVector) == 88
+    assert q.QcdGeometry.initialized.offset > q.QcdGeometry.requests.offset
+    assert q.QcdGeometry.plus.offset % 8 == 0
+
+
+@pytest.mark.parametrize("L", [(4, 4, 4, 4), (6, 4, 2, 8), (2, 2, 2, 2)])
+def test_geometry_tables_match_reference(qlib, ref, L):
+    th = (np.pi, 0.0, 0.0, 0.0)
+    geo = q.Geometry(L, th)
+    assert geo.ok
+    s = geo.s
+    V, V3 = geo.V, geo.V // L[0]
+    t = ref.geometry(L, th)
+
+    def arr(ptr, n):
+        return np.ctypeslib.as_array(ptr, shape=(n,)).copy()
+
+    assert np.array_equal(arr(s.plus, 4 * V), t["plus"].ravel())
+    assert np.array_equal(arr(s.minus, 4 * V), t["minus"].ravel())
+    p3 = arr(s.plus3d, 4 * V3).reshape(V3, 4)[:, 1:]
+    m3 = arr(s.minus3d, 4 * V3).reshape(V3, 4)[:, 1:]
+    assert np.array_equal(p3, t["plus3d"][:, 1:])
+    assert np.array_equal(m3, t["minus3d"][:, 1:])
+    assert np.array_equal(arr(s.eo, V), t["eo"].ravel())
+    assert s.edgePoints == len(t["edge"]) and np.array_equal(arr(s.edge, s.edgePoints), t["edge"])
+    assert s.edge0Points == len(t["edge0"]) and np.array_equal(arr(s.edge0, s.edge0Points), t["edge0"])
+    assert (s.V, s.V3, s.lV, s.lV3, s.nproc, s.initialized) == (V, V3, V, V3, 1, 1)
+    assert list(s.theta) == list(th)
+    geo.close()
+
+
+def test_geometry_rejects_what_the_reference_rejects(qlib):
+    assert q.Geometry((5, 4, 4, 4), P=(2, 1, 1, 1), nproc=2).rc == 1  # not divisible
+    assert q.Geometry((3, 3, 3, 3)).rc == 1  # odd volume
+    assert q.Geometry((1, 4, 4, 4)).rc == 1  # extent < 2
+    # more than one process: one GPU holds the whole lattice
+    assert q.Geometry((4, 4, 4, 4), P=(2, 1, 1, 1), nproc=2).rc == 1
+
+
+def test_vectors_allocate_and_checks_run_without_gpu(qlib):
+    geo = q.Geometry((4, 4, 4, 4))
+    v, w = q.Vector(geo), q.Vector(geo)
+    u = q.GaugeField(geo)
+    v.a[:] = 1.0
+    assert v.a.shape == (256, 4, 3, 2) and v.a.sum() == 256 * 24
+    # uninitialised input vector: error 1 before any device work (qcd_wilson.c:139-143)
+    bad = q.QcdVector()
+    assert qlib.qcd_applyWilsonTMOp(w.ref, C.byref(bad), u.ref, -0.5, 0.0) == 1
+    # uninitialised gauge field (:144-148)
+    badu = q.QcdGaugeField()
+    assert qlib.qcd_applyWilsonTMOp(w.ref, v.ref, C.byref(badu), -0.5, 0.0) == 1
+    # in-place apply is rejected
+    assert qlib.qcd_applyWilsonTMOp(v.ref, v.ref, u.ref, -0.5, 0.0) == 1
+    # geometry mismatch (:149-166)
+    geo2 = q.Geometry((4, 4, 4, 8))
+    x = q.Vector(geo2)
+    assert qlib.qcd_applyWilsonTMOp(w.ref, x.ref, u.ref, -0.5, 0.0) == 1
+    # a halo "in flight" is refused as qcd_communication.c:25-29 does
+    geo.s.numOfRequests = 2
+    assert qlib.qcd_communicateVectorPMGaugeP(v.ref, u.ref) == 1
+    qlib.qcd_waitall(C.byref(geo.s))
+    assert geo.s.numOfRequests == 0
+    assert qlib.qcd_communicateVectorPMGaugeP(v.ref, u.ref) == 0
+    for o in (v, w, x, u):
+        o.close()
+    geo.close()
+    geo2.close()
+
+
+def test_c_program_links_against_the_library(qlib, tmp_path):
+    """A qcd_lib-style C driver compiles against include/qcdgpu.h and links."""
+    import subprocess
+
+    src = tmp_path / "driver.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <math.h>\n#include "qcdgpu.h"\n'
+        "int main(void){ qcd_geometry geo; qcd_uint_2 L[4]={4,4,4,4}, P[4]={1,1,1,1};\n"
+        " qcd_real_8 th[4]={M_PI,0,0,0}; qcd_vector v, Dv; qcd_gaugeField u;\n"
+        " if(qcd_initGeometry(&geo,L,P,th,0,1)) return 2;\n"
+        " if(qcd_initVector(&v,&geo)||qcd_initVector(&Dv,&geo)||qcd_initGaugeField(&u,&geo)) return 3;\n"
+        " printf(\"%lu %lu\\n\", (unsigned long)geo.V, (unsigned long)sizeof(qcd_geometry));\n"
+        " if(0) { qcd_applyWilsonTMOp(&Dv,&v,&u,-0.5,0.0); gcr(&Dv,&v,&u,0.15,0.0,32,&geo); }\n"
+        " qcd_destroyVector(&v); qcd_destroyVector(&Dv); qcd_destroyGaugeField(&u); qcd_destroyGeometry(&geo); return 0; }\n")
+    root = os.path.dirname(HEADER)
+    exe = tmp_path / "driver"
+    subprocess.run(["gcc", "-std=gnu99", "-I", root, str(src), "-o", str(exe), q.LIB_PATH, "-lm",
+                    f"-Wl,-rpath,{os.path.dirname(q.LIB_PATH)}"], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.split()[0] == "256"
+    assert int(out.stdout.split()[1]) == C.sizeof(q.QcdGeometry)

@@ -1,0 +1,132 @@
+"""GPU solver parity. GCR against the reference's own gcr() (golden) and the
+oracle; every other solve is judged the b_minus_Dx.c way (:152-169): the
+true residual |b - D x|/|b| recomputed by the CPU oracle in FP64, plus the
+error against an oracle solve."""
+import numpy as np
+import pytest
+
+import qcd_gb300 as q
+from tests.conftest import EPS_PLAQ_060
+
+pytestmark = pytest.mark.gpu
+TH = (np.pi, 0.0, 0.0, 0.0)
+
+
+def dropin(L, u, theta=TH):
+    geo = q.Geometry(L, theta)
+    gf = q.GaugeField(geo)
+    gf.a[:] = u
+    return geo, gf
+
+
+@pytest.mark.parametrize("case", ["wilson_L6442", "wilson_L4444_theta"])
+def test_gcr_shipped_matches_reference_golden(gpu, golden, case):
+    g = golden[case]
+    geo, u = dropin(g["L"], g["u"], g["theta"])
+    src, sol = q.Vector(geo), q.Vector(geo)
+    src.a[:] = 0
+    src.a[0, 0, 0, 0] = 1.0
+    lib = q.lib()
+    lib.qcdgpu_set_gcr_compat(1)
+    try:
+        rc = lib.gcr(sol.ref, src.ref, u.ref, float(g["kappa"]), float(g["tm"]), 6, geo.s)
+    finally:
+        lib.qcdgpu_set_gcr_compat(0)
+    assert rc == 0
+    assert np.max(np.abs(sol.a - g["gcr6_shipped"])) <= 1e-12 * np.max(np.abs(g["gcr6_shipped"]))
+    for o in (src, sol, u):
+        o.close()
+    geo.close()
+
+
+def test_gcr_fixed_matches_oracle(gpu, orc):
+    L = (8, 4, 4, 4)
+    u = orc.gauge_synthetic(L, 2, EPS_PLAQ_060)
+    b = orc.gaussian_spinor(L, 3)
+    geo, gf = dropin(L, u)
+    src, sol = q.Vector(geo), q.Vector(geo)
+    src.a[:] = b
+    assert q.lib().gcr(sol.ref, src.ref, gf.ref, 0.15, 0.01, 12, geo.s) == 0
+    ref, rc = orc.gcr(b, u, L, TH, 0.15, 0.01, 12, fixed=True)
+    assert np.max(np.abs(sol.a - ref)) <= 1e-11 * np.max(np.abs(ref))
+    for o in (src, sol, gf):
+        o.close()
+    geo.close()
+
+
+@pytest.mark.parametrize("col", [0, 5, 11])
+def test_cgnr_dropin_point_source_columns(gpu, orc, col):
+    """config 1: 8^3 x 16, kappa 0.150, point source at the origin."""
+    L = (16, 8, 8, 8)
+    u = orc.gauge_synthetic(L, 0, EPS_PLAQ_060)
+    geo, gf = dropin(L, u)
+    src, sol = q.Vector(geo), q.Vector(geo)
+    src.a[:] = 0
+    src.a[0, col // 3, col % 3, 0] = 1.0
+    it = q.lib().cgnr(sol.ref, src.ref, gf.ref, 0.15, 0.0, 1e-10, 20000, geo.s)
+    assert it > 0
+    res = orc.true_residual(sol.a, src.a, u, L, TH, 0.15)
+    assert res <= 1e-10
+    x, _, _ = orc.cgnr(np.array(src.a), u, L, TH, 0.15, tol=1e-12)
+    err = np.linalg.norm(sol.a - x) / np.linalg.norm(x)
+    assert err <= 1e-8
+    for o in (src, sol, gf):
+        o.close()
+    geo.close()
+
+
+def test_bicgstab_dropin_converges_where_bicgstab_does(gpu, orc):
+    L = (16, 8, 8, 8)
+    u = orc.gauge_synthetic(L, 0, EPS_PLAQ_060)
+    geo, gf = dropin(L, u)
+    src, sol = q.Vector(geo), q.Vector(geo)
+    src.a[:] = orc.gaussian_spinor(L, 9)
+    kappa = 0.12
+    it = q.lib().bicgstab(sol.ref, src.ref, gf.ref, kappa, 0.0, 1e-10, 5000, geo.s)
+    assert it > 0
+    assert orc.true_residual(sol.a, src.a, u, L, TH, kappa) <= 1e-10
+    for o in (src, sol, gf):
+        o.close()
+    geo.close()
+
+
+@pytest.mark.parametrize("solver,prec", [(q.SOLVER_CGNR, q.F64), (q.SOLVER_CGNR, q.F32), (q.SOLVER_CGNR, q.F16),
+                                         (q.SOLVER_BICGSTAB, q.F32), (q.SOLVER_GCR, q.F64)])
+def test_device_solver_true_residual(gpu, orc, solver, prec):
+    L = (16, 8, 8, 8)
+    kappa = 0.15 if solver == q.SOLVER_CGNR else 0.12
+    u = orc.gauge_synthetic(L, 4, EPS_PLAQ_060)
+    b = orc.gaussian_spinor(L, 5)
+    g = q.Gauge(L, TH).load(u)
+    fb, fx = q.Field(L).load(b), q.Field(L)
+    op = q.OP_Q if solver == q.SOLVER_GCR else q.OP_D
+    p = q.solve(fx, fb, g, kappa, 0.0, solver=solver, op=op, inner_prec=prec, tol=1e-10, maxiter=20000,
+                restart=16, delta=0.1)
+    x = fx.store()
+    assert p.status == 0, (p.status, p.true_residual, p.iters)
+    opname = "Q" if op == q.OP_Q else "D"
+    assert orc.true_residual(x, b, u, L, TH, kappa, op=opname) <= 1e-10
+    assert p.true_residual <= 1e-10
+    if prec != q.F64:
+        assert p.reliable_updates >= 2
+    for f in (g, fb, fx):
+        f.close()
+
+
+def test_mixed_precision_cgnr_matches_fp64_solution(gpu, orc):
+    L = (16, 8, 8, 8)
+    u = orc.gauge_synthetic(L, 6, EPS_PLAQ_060)
+    b = orc.gaussian_spinor(L, 7)
+    g = q.Gauge(L, TH).load(u)
+    fb = q.Field(L).load(b)
+    xs = {}
+    for prec in (q.F64, q.F32, q.F16):
+        fx = q.Field(L)
+        p = q.solve(fx, fb, g, 0.15, 0.0, solver=q.SOLVER_CGNR, inner_prec=prec, tol=1e-11)
+        assert p.status == 0
+        xs[prec] = fx.store()
+        fx.close()
+    for prec in (q.F32, q.F16):
+        assert np.linalg.norm(xs[prec] - xs[q.F64]) / np.linalg.norm(xs[q.F64]) <= 1e-9
+    g.close()
+    fb.close()
