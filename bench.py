@@ -161,7 +161,7 @@ def cpu_baseline(budget_s: float, procs: int, L=L_BENCH) -> dict:
         with ctx.Pool(procs) as pool:
             res = pool.map(_cpu_worker, [(budget_s, L)] * procs)
     rate = sum(n / t for n, t in res)  # applies per second, all processes
-    gbs = rate * V * bytes_per_site(0, 12) / 1e9
+    gbs = rate * V * bytes_per_site(0, 18) / 1e9
     applies = sum(n for n, _ in res)
     return {"value": gbs, "unit": "GB/s", "cores": procs, "kind": "port",
             "sample": f"{applies} FP64 D applies of {L[3]}^3x{L[0]} ({budget_s:.0f} s per process, "
@@ -218,7 +218,7 @@ def solve_bench(q, orc_check, g, L, n_rhs):
     b, x = q.Field(L), q.Field(L)
     for name, solver, prec in (("fp64_cgnr", q.SOLVER_CGNR, q.F64), ("mixed_cgnr_f16", q.SOLVER_CGNR, q.F16),
                                ("mixed_cgnr_f32", q.SOLVER_CGNR, q.F32)):
-        lat, iters, res = [], [], []
+        lat, iters, res, status = [], [], [], []
         for col in range(n_rhs):
             b.point((0, 0, 0, 0), col // 3, col % 3)
             q.sync()
@@ -228,13 +228,16 @@ def solve_bench(q, orc_check, g, L, n_rhs):
             lat.append(time.perf_counter() - t0)
             iters.append(p.iters)
             res.append(p.true_residual)
-            if p.status != 0:
-                raise RuntimeError(f"{name} did not converge: {p.status} {p.true_residual}")
+            status.append(p.status)
         lat.sort()
-        out[name] = {"rhs_solves_per_s": n_rhs / sum(lat), "p50_ms": 1e3 * lat[len(lat) // 2],
+        ok = all(s == 0 for s in status)
+        out[name] = {"rhs_solves_per_s": n_rhs / sum(lat) if ok else None, "p50_ms": 1e3 * lat[len(lat) // 2],
                      "p99_ms": 1e3 * lat[min(len(lat) - 1, int(0.99 * len(lat)))], "iters": iters,
-                     "max_true_residual": max(res)}
-    out["speedup_mixed_vs_fp64"] = out["mixed_cgnr_f16"]["rhs_solves_per_s"] / out["fp64_cgnr"]["rhs_solves_per_s"]
+                     "max_true_residual": max(res), "status": status}
+    if out["fp64_cgnr"]["rhs_solves_per_s"]:
+        for k in ("mixed_cgnr_f16", "mixed_cgnr_f32"):
+            if out[k]["rhs_solves_per_s"]:
+                out["speedup_" + k + "_vs_fp64"] = out[k]["rhs_solves_per_s"] / out["fp64_cgnr"]["rhs_solves_per_s"]
     b.close()
     x.close()
     return out
@@ -254,7 +257,7 @@ def run_ours(args, rank, world, local_rank):
     plaq = g.plaquette()
     fin, fout = q.Field(L_BENCH).gaussian(2000 + rank), q.Field(L_BENCH)
     recon = g.recon
-    bps = bytes_per_site(0, recon)
+    bps = bytes_per_site(0, 18)  # FP64 kernels read complete links (arithmetic-bound, no rebuild)
     sampler = ClockSampler(local_rank)
     sampler.start()
     if world > 1:
@@ -296,7 +299,7 @@ def run_ours(args, rank, world, local_rank):
         "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if arith == "f64" else "f64 storage, df64 arithmetic",
         "data": "synthetic (seeded SU(3) links exp(i eps H), plaquette %.4f; Gaussian spinor)" % plaq,
-        "config": {"workload": "FP64 Wilson-Dirac apply D psi, 24^3x48, kappa 0.150, theta_t = pi, 12-real links",
+        "config": {"workload": "FP64 Wilson-Dirac apply D psi, 24^3x48, kappa 0.150, theta_t = pi, 18-real links",
                    "lattice_txyz": list(L_BENCH), "sites": V, "bytes_per_site": bps, "flops_per_site": FLOPS_PER_SITE,
                    "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (working set %d MB vs 129 MB)" % (V * bps // 2**20)},
         "gflops": V * FLOPS_PER_SITE / (ms_max * 1e-3) / 1e9 * world,
@@ -327,7 +330,7 @@ def run_reference(args, rank, world):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "FP64 Wilson-Dirac apply D psi, 24^3x48, kappa 0.150, theta_t = pi",
-                       "lattice_txyz": list(L_BENCH), "sites": V, "bytes_per_site": bytes_per_site(0, 12),
+                       "lattice_txyz": list(L_BENCH), "sites": V, "bytes_per_site": bytes_per_site(0, 18),
                        "parallelism": f"{ncores} CPU processes, one apply stream each"},
             "impl": "reference", "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": cb["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

@@ -25,7 +25,7 @@ def sources() -> list[str]:
 
 def _compile(src: str, extra: list[str]) -> str:
     obj = os.path.join(OUT, os.path.basename(src)[:-3] + ".o")
-    deps = [src] + [os.path.join(SRC, h) for h in os.listdir(SRC) if h.endswith(".h")]
+    deps = [src] + [os.path.join(SRC, h) for h in os.listdir(SRC) if h.endswith((".h", ".cuh"))]
     deps.append(os.path.join(HERE, "..", "include", "qcdgpu.h"))
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj

@@ -106,7 +106,9 @@ static bool vec_done(qcd_vector *v)
 {
   auto it = g_vec.find((const void *)v->D);
   if (it == g_vec.end() || !it->second.f) return false;
-  if (it->second.resident) return true;
+  // uploads from page-locked memory are asynchronous: finish them before the
+  // caller may touch its host buffers again
+  if (it->second.resident) return QG_CUDA(cudaStreamSynchronize(stream()));
   return download_spinor_aos(it->second.f, (double *)v->D);
 }
 
@@ -540,6 +542,7 @@ int qcdgpu_vector_make_resident(qcd_vector *v)
   VecMirror *m = vec_mirror(v);
   if (!m) return 1;
   if (!m->resident && !upload_spinor_aos(m->f, (const double *)v->D)) return 1;
+  if (!QG_CUDA(cudaStreamSynchronize(stream()))) return 1;
   m->resident = true;
   return 0;
 }
@@ -555,7 +558,7 @@ int qcdgpu_vector_to_device(qcd_vector *v)
 {
   std::lock_guard<std::mutex> lk(g_mu);
   VecMirror *m = vec_mirror(v);
-  return m && upload_spinor_aos(m->f, (const double *)v->D) ? 0 : 1;
+  return m && upload_spinor_aos(m->f, (const double *)v->D) && QG_CUDA(cudaStreamSynchronize(stream())) ? 0 : 1;
 }
 
 int qcdgpu_vector_release(qcd_vector *v)

@@ -8,7 +8,10 @@
 //   spinor F32 :  6 blocks of float4   -- block j = complex components 2j,2j+1
 //   spinor F16 :  3 blocks of uint4    -- 8 halves = complex 4j..4j+3, values
 //                 divided by a per-site float norm (max |real| of the site)
-//   gauge  F64 : recon 18 -> 4 mu x 9 double2 ; recon 12 -> 4 mu x 6 double2
+//   gauge  F64 : 4 mu x 9 double2, always complete; when every link is in
+//                SU(3) (recon 12) kernels may read rows 0,1 only and rebuild
+//                row 2 -- memory-bound kernels do, FP64-compute-bound ones
+//                read all 9 and skip the rebuild
 //   gauge  F32 : recon 12 -> 4 mu x 3 float4  ; recon 18 -> 4 mu x 9 float2
 //   gauge  F16 : recon 12 -> 4 mu x 3 uint2 (4 halves each)
 //
@@ -131,6 +134,11 @@ int solve(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, double tm,
 int gcr_dropin(qcdgpu_field sol, qcdgpu_field src, qcdgpu_gauge g, double mp4, double tm, int n,
                int shipped);
 
+// low-precision copies of a gauge field made for mixed-precision solves;
+// gauge_forget drops them (the field was reloaded or destroyed)
+qcdgpu_gauge gauge_at(qcdgpu_gauge g, int prec);
+void gauge_forget(qcdgpu_gauge g);
+
 extern int g_gcr_shipped;
 extern int g_f64_arith;
 
@@ -248,6 +256,9 @@ struct Spinor<QCDGPU_F16, R> {
     float m = 0.f;
 #pragma unroll
     for (int k = 0; k < 12; k++) m = fmaxf(m, fmaxf(fabsf((float)s[k].re), fabsf((float)s[k].im)));
+    // a site whose largest component is below the smallest normal float
+    // (1.2e-38) is stored as zero: 1/m would overflow and 0 * inf is NaN
+    if (!(m >= 1.17549435e-38f)) m = 0.f;
     float inv = m > 0.f ? 1.0f / m : 0.f;
     uint4 *p = (uint4 *)base + x;
 #pragma unroll
@@ -295,7 +306,8 @@ struct Link<QCDGPU_F64, 12, R> {
   __device__ __forceinline__ static void load(const void *base, int64_t stride, int64_t x, int mu,
                                               C<R> U[9])
   {
-    const double2 *p = (const double2 *)base + (int64_t)mu * 6 * stride + x;
+    // FP64 links always hold all 9 entries; this reader takes rows 0 and 1
+    const double2 *p = (const double2 *)base + (int64_t)mu * 9 * stride + x;
 #pragma unroll
     for (int k = 0; k < 6; k++) {
       double2 v = __ldg(p + k * stride);
@@ -351,28 +363,34 @@ struct Link<QCDGPU_F16, 12, R> {
 };
 
 // site coordinates (t fastest) and neighbour offsets with periodic wrap
+// Lattice geometry for kernels. Site indices fit in 32 bits (the library
+// rejects volumes of 2^31 sites or more), so coordinates are recovered with
+// 32-bit unsigned divisions.
 struct Geom {
   int L[4];
-  int64_t st[4];  // 1, Lt, Lt*Lx, Lt*Lx*Ly
+  int st[4];  // 1, Lt, Lt*Lx, Lt*Lx*Ly
 };
 
-__device__ __forceinline__ void coords(const Geom &g, int64_t x, int c[4])
+__device__ __forceinline__ void coords(const Geom &g, int x, int c[4])
 {
-  int64_t r = x;
-  c[0] = (int)(r % g.L[0]);
-  r /= g.L[0];
-  c[1] = (int)(r % g.L[1]);
-  r /= g.L[1];
-  c[2] = (int)(r % g.L[2]);
-  c[3] = (int)(r / g.L[2]);
+  unsigned r = (unsigned)x;
+  unsigned q = r / (unsigned)g.L[0];
+  c[0] = (int)(r - q * (unsigned)g.L[0]);
+  r = q;
+  q = r / (unsigned)g.L[1];
+  c[1] = (int)(r - q * (unsigned)g.L[1]);
+  r = q;
+  q = r / (unsigned)g.L[2];
+  c[2] = (int)(r - q * (unsigned)g.L[2]);
+  c[3] = (int)q;
 }
-__device__ __forceinline__ int64_t fwd(const Geom &g, int64_t x, const int c[4], int mu)
+__device__ __forceinline__ int fwd(const Geom &g, int x, const int c[4], int mu)
 {
-  return c[mu] == g.L[mu] - 1 ? x - (int64_t)(g.L[mu] - 1) * g.st[mu] : x + g.st[mu];
+  return c[mu] == g.L[mu] - 1 ? x - (g.L[mu] - 1) * g.st[mu] : x + g.st[mu];
 }
-__device__ __forceinline__ int64_t bwd(const Geom &g, int64_t x, const int c[4], int mu)
+__device__ __forceinline__ int bwd(const Geom &g, int x, const int c[4], int mu)
 {
-  return c[mu] == 0 ? x + (int64_t)(g.L[mu] - 1) * g.st[mu] : x - g.st[mu];
+  return c[mu] == 0 ? x + (g.L[mu] - 1) * g.st[mu] : x - g.st[mu];
 }
 
 }  // namespace qgd

@@ -181,8 +181,9 @@ __device__ __forceinline__ void put_link(void *dst, int64_t stride, int64_t x, i
                                          const C<double> U[9])
 {
   if (P == QCDGPU_F64) {
-    double2 *d = (double2 *)dst + (int64_t)mu * recon / 2 * stride + x;
-    for (int k = 0; k < recon / 2; k++) d[k * stride] = make_double2(U[k].re, U[k].im);
+    // FP64 links are stored complete whatever recon says (see internal.h)
+    double2 *d = (double2 *)dst + (int64_t)mu * 9 * stride + x;
+    for (int k = 0; k < 9; k++) d[k * stride] = make_double2(U[k].re, U[k].im);
   } else if (P == QCDGPU_F32) {
     if (recon == 12) {
       float4 *d = (float4 *)dst + (int64_t)mu * 3 * stride + x;
@@ -299,8 +300,7 @@ bool download_gauge_aos(qcdgpu_gauge g, double *host)
   if (!st) return false;
   unsigned gr = grid_for(g->V * 4, 128);
   double2 *d = (double2 *)st;
-  if (g->prec == QCDGPU_F64 && g->recon == 12) k_gauge_soa_to_aos<QCDGPU_F64, 12><<<gr, 128, 0, stream()>>>(d, g->data, g->stride, g->V);
-  else if (g->prec == QCDGPU_F64) k_gauge_soa_to_aos<QCDGPU_F64, 18><<<gr, 128, 0, stream()>>>(d, g->data, g->stride, g->V);
+  if (g->prec == QCDGPU_F64) k_gauge_soa_to_aos<QCDGPU_F64, 18><<<gr, 128, 0, stream()>>>(d, g->data, g->stride, g->V);
   else if (g->prec == QCDGPU_F32 && g->recon == 12) k_gauge_soa_to_aos<QCDGPU_F32, 12><<<gr, 128, 0, stream()>>>(d, g->data, g->stride, g->V);
   else if (g->prec == QCDGPU_F32) k_gauge_soa_to_aos<QCDGPU_F32, 18><<<gr, 128, 0, stream()>>>(d, g->data, g->stride, g->V);
   else k_gauge_soa_to_aos<QCDGPU_F16, 12><<<gr, 128, 0, stream()>>>(d, g->data, g->stride, g->V);
@@ -344,8 +344,16 @@ extern "C" {
 int qcdgpu_field_load(qcdgpu_field f, const double *host) { return qg::upload_spinor_aos(f, host) ? 0 : 1; }
 int qcdgpu_field_store(qcdgpu_field f, double *host) { return qg::download_spinor_aos(f, host) ? 0 : 1; }
 int qcdgpu_field_copy(qcdgpu_field d, qcdgpu_field s) { return qg::convert_field(d, s) ? 0 : 1; }
-int qcdgpu_gauge_load(qcdgpu_gauge g, const double *host) { return qg::upload_gauge_aos(g, host) ? 0 : 1; }
+int qcdgpu_gauge_load(qcdgpu_gauge g, const double *host)
+{
+  qg::gauge_forget(g);  // derived low-precision copies are stale now
+  return qg::upload_gauge_aos(g, host) ? 0 : 1;
+}
 int qcdgpu_gauge_store(qcdgpu_gauge g, double *host) { return qg::download_gauge_aos(g, host) ? 0 : 1; }
-int qcdgpu_gauge_convert(qcdgpu_gauge d, qcdgpu_gauge s) { return qg::convert_gauge(d, s) ? 0 : 1; }
+int qcdgpu_gauge_convert(qcdgpu_gauge d, qcdgpu_gauge s)
+{
+  qg::gauge_forget(d);
+  return qg::convert_gauge(d, s) ? 0 : 1;
+}
 
 }  // extern "C"

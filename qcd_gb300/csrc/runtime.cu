@@ -63,6 +63,11 @@ qcdgpu_field field_new(const int L[4], int prec)
   auto *f = new qcdgpu_field_s();
   memcpy(f->L, L, sizeof(f->L));
   f->V = (int64_t)L[0] * L[1] * L[2] * L[3];
+  if (f->V >= (1ll << 31) - 128) {
+    set_error("lattice of %lld sites: kernels index sites with 32-bit integers", (long long)f->V);
+    delete f;
+    return nullptr;
+  }
   f->stride = pad_stride(f->V);
   f->prec = prec;
   f->bytes = spinor_bytes(prec, f->stride);
@@ -97,6 +102,11 @@ qcdgpu_gauge gauge_new(const int L[4], const double theta[4], int prec, int reco
   memcpy(g->L, L, sizeof(g->L));
   for (int i = 0; i < 4; i++) g->theta[i] = theta ? theta[i] : 0.0;
   g->V = (int64_t)L[0] * L[1] * L[2] * L[3];
+  if (g->V >= (1ll << 31) - 128) {
+    set_error("lattice of %lld sites: kernels index sites with 32-bit integers", (long long)g->V);
+    delete g;
+    return nullptr;
+  }
   g->stride = pad_stride(g->V);
   g->prec = prec;
   g->recon = recon;
@@ -217,6 +227,7 @@ int qcdgpu_gauge_create(qcdgpu_gauge *g, const int L[4], const double theta[4], 
 
 int qcdgpu_gauge_destroy(qcdgpu_gauge g)
 {
+  qg::gauge_forget(g);
   qg::gauge_free(g);
   return 0;
 }

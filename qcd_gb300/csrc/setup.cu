@@ -322,6 +322,7 @@ extern "C" {
 
 int qcdgpu_gauge_synthetic(qcdgpu_gauge g, uint64_t seed, double eps)
 {
+  qg::gauge_forget(g);
   return qg::gauge_synthetic(g, seed, eps) ? 0 : 1;
 }
 double qcdgpu_plaquette(qcdgpu_gauge g) { return qg::plaquette(g); }

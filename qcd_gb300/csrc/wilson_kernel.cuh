@@ -1,0 +1,140 @@
+// wilson_kernel.cuh -- the operator kernel template, shared by the native
+// (double / float) and the float-float instantiations.
+//
+// One thread per site. Each of the eight neighbour spinors is projected to a
+// two-spin half spinor straight after its load, multiplied by the link,
+// phased when theta_mu != 0, and expanded back into the 4-spin accumulator
+// (projectors of the chiral basis, qcd_wilson.h:17-387). Links arrive as 12
+// reals (third row rebuilt) when the field is SU(3). R is the arithmetic
+// type: any type with +, -, * and unary - and conversions from/to double.
+#pragma once
+
+#include "dslash_args.h"
+
+namespace qg {
+
+using namespace qgd;
+
+// h = (1 + S g_mu) p restricted to spins 0,1 (the independent half)
+template <int MU, int S, typename R>
+__device__ __forceinline__ void project(const C<R> p[12], C<R> h[6])
+{
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    C<R> p0 = p[c], p1 = p[3 + c], p2 = p[6 + c], p3 = p[9 + c];
+    if (MU == 0) {
+      h[c] = S > 0 ? p0 - p2 : p0 + p2;
+      h[3 + c] = S > 0 ? p1 - p3 : p1 + p3;
+    } else if (MU == 1) {
+      h[c] = S > 0 ? p0 - mul_i(p3) : p0 + mul_i(p3);
+      h[3 + c] = S > 0 ? p1 - mul_i(p2) : p1 + mul_i(p2);
+    } else if (MU == 2) {
+      h[c] = S > 0 ? p0 - p3 : p0 + p3;
+      h[3 + c] = S > 0 ? p1 + p2 : p1 - p2;
+    } else {
+      h[c] = S > 0 ? p0 - mul_i(p2) : p0 + mul_i(p2);
+      h[3 + c] = S > 0 ? p1 + mul_i(p3) : p1 - mul_i(p3);
+    }
+  }
+}
+
+// acc += (1 + S g_mu) spinor rebuilt from its upper half h
+template <int MU, int S, typename R>
+__device__ __forceinline__ void accumulate(C<R> acc[12], const C<R> h[6])
+{
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    C<R> h0 = h[c], h1 = h[3 + c];
+    acc[c] = acc[c] + h0;
+    acc[3 + c] = acc[3 + c] + h1;
+    if (MU == 0) {
+      acc[6 + c] = S > 0 ? acc[6 + c] - h0 : acc[6 + c] + h0;
+      acc[9 + c] = S > 0 ? acc[9 + c] - h1 : acc[9 + c] + h1;
+    } else if (MU == 1) {
+      acc[6 + c] = S > 0 ? acc[6 + c] + mul_i(h1) : acc[6 + c] - mul_i(h1);
+      acc[9 + c] = S > 0 ? acc[9 + c] + mul_i(h0) : acc[9 + c] - mul_i(h0);
+    } else if (MU == 2) {
+      acc[6 + c] = S > 0 ? acc[6 + c] + h1 : acc[6 + c] - h1;
+      acc[9 + c] = S > 0 ? acc[9 + c] - h0 : acc[9 + c] + h0;
+    } else {
+      acc[6 + c] = S > 0 ? acc[6 + c] + mul_i(h0) : acc[6 + c] - mul_i(h0);
+      acc[9 + c] = S > 0 ? acc[9 + c] - mul_i(h1) : acc[9 + c] + mul_i(h1);
+    }
+  }
+}
+
+template <int MU, bool DAG, int SP, int GP, int RECON, typename R>
+__device__ __forceinline__ void hop_pair(const DArgs &a, int x, const int c[4], C<R> acc[12])
+{
+  constexpr int SF = DAG ? +1 : -1;  // projector sign of the forward hop
+  const bool twisted = (a.twist_mask >> MU) & 1;
+  {
+    int y = fwd(a.geo, x, c, MU);
+    C<R> s[12], h[6], uh[6], U[9];
+    Spinor<SP, R>::load(a.in, a.in_norm, a.stride, y, s);
+    project<MU, SF>(s, h);
+    Link<GP, RECON, R>::load(a.gauge, a.gstride, x, MU, U);
+#pragma unroll
+    for (int j = 0; j < 2; j++)
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+        uh[3 * j + i] = U[3 * i] * h[3 * j] + U[3 * i + 1] * h[3 * j + 1] + U[3 * i + 2] * h[3 * j + 2];
+    if (twisted) {
+      C<R> ph{Scalar<R>::get(a.phr[MU], a.phr_h[MU], a.phr_l[MU]), Scalar<R>::get(a.phi[MU], a.phi_h[MU], a.phi_l[MU])};
+#pragma unroll
+      for (int k = 0; k < 6; k++) uh[k] = uh[k] * ph;
+    }
+    accumulate<MU, SF>(acc, uh);
+  }
+  {
+    int y = bwd(a.geo, x, c, MU);
+    C<R> s[12], h[6], uh[6], U[9];
+    Spinor<SP, R>::load(a.in, a.in_norm, a.stride, y, s);
+    project<MU, -SF>(s, h);
+    Link<GP, RECON, R>::load(a.gauge, a.gstride, y, MU, U);
+#pragma unroll
+    for (int j = 0; j < 2; j++)
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+        uh[3 * j + i] = cdot(U[i], h[3 * j]) + cdot(U[3 + i], h[3 * j + 1]) + cdot(U[6 + i], h[3 * j + 2]);
+    if (twisted) {
+      C<R> ph{Scalar<R>::get(a.phr[MU], a.phr_h[MU], a.phr_l[MU]), -Scalar<R>::get(a.phi[MU], a.phi_h[MU], a.phi_l[MU])};
+#pragma unroll
+      for (int k = 0; k < 6; k++) uh[k] = uh[k] * ph;
+    }
+    accumulate<MU, -SF>(acc, uh);
+  }
+}
+
+template <bool DAG, int SP, int GP, int RECON, typename R>
+__global__ void __launch_bounds__(128) k_wilson(const DArgs a)
+{
+  int x = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (x >= a.V) return;
+  int c[4];
+  coords(a.geo, x, c);
+  C<R> acc[12];
+#pragma unroll
+  const R zero = Scalar<R>::get(0.0, 0.0f, 0.0f);
+  for (int k = 0; k < 12; k++) acc[k] = C<R>{zero, zero};
+  hop_pair<0, DAG, SP, GP, RECON, R>(a, x, c, acc);
+  hop_pair<1, DAG, SP, GP, RECON, R>(a, x, c, acc);
+  hop_pair<2, DAG, SP, GP, RECON, R>(a, x, c, acc);
+  hop_pair<3, DAG, SP, GP, RECON, R>(a, x, c, acc);
+  C<R> s[12];
+  Spinor<SP, R>::load(a.in, a.in_norm, a.stride, x, s);
+  const R mp4 = Scalar<R>::get(a.mp4, a.mp4_h, a.mp4_l), tm = Scalar<R>::get(a.tm, a.tm_h, a.tm_l);
+  const R half = Scalar<R>::get(0.5, 0.5f, 0.0f);
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    // (m+4) s + i tm g5 s - acc/2 ; g5 = +1 for spins 0,1, -1 for spins 2,3
+    R g5tm = k < 6 ? tm : -tm;
+    C<R> d{mp4 * s[k].re - g5tm * s[k].im, mp4 * s[k].im + g5tm * s[k].re};
+    d = d - half * acc[k];
+    if (a.op_q) d = k < 6 ? mul_i(d) : -mul_i(d);
+    acc[k] = d;
+  }
+  Spinor<SP, R>::store(a.out, a.out_norm, a.stride, x, acc);
+}
+
+}  // namespace qg

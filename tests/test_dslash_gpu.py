@@ -93,6 +93,9 @@ def test_low_precision_operator(gpu, orc, prec, tol):
         ref = orc.dslash(v, u, L, th, kappa=0.15, tm=0.05, op=o)
         out, _ = run_op(L, th, u, v, 0.15, 0.05, op, prec=prec)
         assert rel(out, ref) <= tol
+    dd = orc.dslash(orc.dslash(v, u, L, th, kappa=0.15, tm=0.05), u, L, th, kappa=0.15, tm=0.05, op="Ddag")
+    out, _ = run_op(L, th, u, v, 0.15, 0.05, q.OP_DDAGD, prec=prec)
+    assert rel(out, dd) <= 2 * tol
 
 
 def test_dropin_operator_entry_points(gpu, golden):
