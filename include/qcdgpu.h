@@ -306,6 +306,21 @@ enum {
 int qcdgpu_solve(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double kappa, double mu,
                  qcdgpu_solve_params *p);
 
+/* No counterpart in the reference. The complex dot product
+ * result[0] + i result[1] = sum_i conj(a_i) b_i, for callers that cannot
+ * allocate device memory (their device heap belongs to a framework's
+ * allocator or a pre-reserved serving budget, or they cannot afford the
+ * synchronisation an allocation may cause): it allocates nothing. a and b
+ * are device arrays of n complex doubles (re, im interleaved, 16-byte
+ * aligned), result a device array of 2 doubles; the work is queued on
+ * `stream` (a cudaStream_t, NULL = default stream) and the call returns
+ * without waiting. Its partial sums live in a fixed 32 KB device array that
+ * every call shares: n may not exceed 134,217,728 (larger n returns 1 with a
+ * message), and calls that overlap on the GPU race on that array. The first
+ * call on each device looks the array's address up; make it before any
+ * stream capture. Returns 0, or 1 on error (qcdgpu_last_error). */
+int qcdgpu_dot_noalloc(const double *a, const double *b, int64_t n, double *result, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -165,6 +165,7 @@ def lib() -> C.CDLL:
     L.qcdgpu_norm2.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
     L.qcdgpu_dot.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]
     L.qcdgpu_solve.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.POINTER(SolveParams)]
+    L.qcdgpu_dot_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
     _lib = L
     return L
 
