@@ -319,6 +319,28 @@ def run_ours(args, rank, world, local_rank):
     return line
 
 
+def run_only(args):
+    """one operator variant on the bench lattice, nothing else (profiling target)"""
+    import torch
+
+    import qcd_gb300 as q
+
+    prec = {"f64": q.F64, "df64": q.F64, "f32": q.F32, "f16": q.F16}[args.only]
+    arith = q.ARITH_DF64 if args.only == "df64" else q.ARITH_F64
+    g64 = q.Gauge(L_BENCH, THETA).synthetic(1000, EPS_PLAQ_060)
+    g = g64 if prec == q.F64 else q.Gauge(L_BENCH, THETA, prec).convert_from(g64)
+    f64 = q.Field(L_BENCH).gaussian(2000)
+    fin = f64 if prec == q.F64 else q.Field(L_BENCH, prec).copy_from(f64)
+    fout = q.Field(L_BENCH, prec)
+    stream = torch.cuda.current_stream()
+    q.set_stream(stream.cuda_stream)
+    ms, n = time_dslash(q, torch, fout, fin, g, args.steps, args.warmup, arith, stream)
+    V = L_BENCH[0] * L_BENCH[1] * L_BENCH[2] * L_BENCH[3]
+    bps = bytes_per_site(prec, 18 if prec == q.F64 else 12)
+    return {"only": args.only, "ms_per_apply": ms, "gbs": V * bps / (ms * 1e-3) / 1e9, "bytes_per_site": bps,
+            "launches": n}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return None
@@ -347,12 +369,17 @@ def main():
     ap.add_argument("--solve-rhs", type=int, default=4)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-seconds", type=float, default=20.0)
+    ap.add_argument("--only", choices=["f64", "df64", "f32", "f16"],
+                    help="profiling target: time only this operator variant (a few launches under ncu)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.only:
+        print(json.dumps(run_only(args)), flush=True)
+        return
     if args.impl == "reference":
         line = run_reference(args, rank, world)
     else:

@@ -321,6 +321,49 @@ int qcdgpu_solve(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double kappa, d
  * stream capture. Returns 0, or 1 on error (qcdgpu_last_error). */
 int qcdgpu_dot_noalloc(const double *a, const double *b, int64_t n, double *result, void *stream);
 
+/* ---------------------------------------------------------------------- */
+/* Multi-RHS (no reference counterpart: qcd_lib solves one column at a time,
+ * invert.c:255). A multi-RHS field holds up to 64 spinors in FP16 with one
+ * norm per (site, RHS); the operator reads the gauge field once per site
+ * for all of them and runs the link x RHS products on the tensor cores. */
+typedef struct qcdgpu_mfield_s *qcdgpu_mfield;
+int qcdgpu_mfield_create(qcdgpu_mfield *m, const int L[4], int nrhs);
+int qcdgpu_mfield_destroy(qcdgpu_mfield m);
+/* slot r <- f / f <- slot r (f in any storage precision) */
+int qcdgpu_mfield_set(qcdgpu_mfield m, int r, qcdgpu_field f);
+int qcdgpu_mfield_get(qcdgpu_field f, qcdgpu_mfield m, int r);
+/* out = op(in) for slots 0..nact-1, op QCDGPU_OP_D or QCDGPU_OP_DDAG; g is
+ * the FP64 gauge field */
+int qcdgpu_dslash_mrhs(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_gauge g, double kappa, double mu, int op,
+                       int nact);
+
+/* Batched solver with continuous admission (no reference counterpart). A
+ * batch of `capacity` slots (1..64) runs mixed-precision CG on the normal
+ * equations for every occupied slot at once on the multi-RHS operator, with
+ * FP64 reliable updates per slot. Each slot carries its own kappa, mu and
+ * tolerance; slots retire when their FP64 true residual |b - op x| / |b|
+ * reaches tol and new right-hand sides enter free slots between steps. */
+typedef struct qcdgpu_batch_s *qcdgpu_batch;
+int qcdgpu_batch_create(qcdgpu_batch *b, qcdgpu_gauge g, int capacity);
+int qcdgpu_batch_destroy(qcdgpu_batch b);
+/* Solve op x = rhs (op QCDGPU_OP_D or QCDGPU_OP_Q; x, rhs FP64 fields that
+ * stay owned by the caller and untouched by it until polled). maxiter <= 0:
+ * 100000; delta <= 0: 0.1. Returns the slot, -1 when the batch is full, -2 on
+ * error. A right-hand side already solved by x = 0 is reported by the next
+ * poll without taking a slot. */
+int qcdgpu_batch_add(qcdgpu_batch b, qcdgpu_field x, qcdgpu_field rhs, double kappa, double mu, int op,
+                     double tol, int maxiter, double delta, int tag);
+/* Run `iterations` (rounded up to a multiple of 16) iterations of every
+ * occupied slot, retiring finished ones. Returns 0 or 3 on a CUDA error. */
+int qcdgpu_batch_step(qcdgpu_batch b, int iterations);
+int qcdgpu_batch_active(qcdgpu_batch b);
+int qcdgpu_batch_free_slots(qcdgpu_batch b);
+/* Retired right-hand sides, oldest first: tag, status (0 converged, 1
+ * maxiter, 2 breakdown), iterations and true residual. Returns the count. */
+int qcdgpu_batch_poll(qcdgpu_batch b, int *tags, int *status, int *iters, double *true_residual, int max);
+/* device bytes held by the batch */
+size_t qcdgpu_batch_bytes(qcdgpu_batch b);
+
 #ifdef __cplusplus
 }
 #endif

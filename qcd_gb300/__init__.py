@@ -166,6 +166,21 @@ def lib() -> C.CDLL:
     L.qcdgpu_dot.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]
     L.qcdgpu_solve.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.POINTER(SolveParams)]
     L.qcdgpu_dot_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
+    L.qcdgpu_mfield_create.argtypes = [vpp, _ip, C.c_int]
+    L.qcdgpu_mfield_destroy.argtypes = [C.c_void_p]
+    L.qcdgpu_mfield_set.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    L.qcdgpu_mfield_get.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+    L.qcdgpu_dslash_mrhs.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_int]
+    L.qcdgpu_batch_create.argtypes = [vpp, C.c_void_p, C.c_int]
+    L.qcdgpu_batch_destroy.argtypes = [C.c_void_p]
+    L.qcdgpu_batch_add.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_double,
+                                   C.c_int, C.c_double, C.c_int]
+    L.qcdgpu_batch_step.argtypes = [C.c_void_p, C.c_int]
+    L.qcdgpu_batch_active.argtypes = [C.c_void_p]
+    L.qcdgpu_batch_free_slots.argtypes = [C.c_void_p]
+    L.qcdgpu_batch_poll.argtypes = [C.c_void_p, _ip, _ip, _ip, _dp, C.c_int]
+    L.qcdgpu_batch_bytes.argtypes = [C.c_void_p]
+    L.qcdgpu_batch_bytes.restype = C.c_size_t
     _lib = L
     return L
 
@@ -375,3 +390,84 @@ def sync():
 
 def kernel_launches() -> int:
     return lib().qcdgpu_kernel_launches()
+
+
+class MField:
+    """Multi-RHS device field (qcdgpu_mfield): up to 64 FP16 spinors."""
+
+    def __init__(self, L, nrhs):
+        self.L = np.ascontiguousarray(L, dtype=np.int32)
+        self.n = nrhs
+        h = C.c_void_p()
+        _check(lib().qcdgpu_mfield_create(C.byref(h), self.L, nrhs), "qcdgpu_mfield_create")
+        self.h = h
+
+    def set(self, r: int, f: Field) -> "MField":
+        _check(lib().qcdgpu_mfield_set(self.h, r, f.h), "mfield_set")
+        return self
+
+    def get(self, r: int, f: Field) -> Field:
+        _check(lib().qcdgpu_mfield_get(f.h, self.h, r), "mfield_get")
+        return f
+
+    def close(self):
+        if self.h:
+            lib().qcdgpu_mfield_destroy(self.h)
+            self.h = None
+
+
+def dslash_mrhs(out: MField, inp: MField, g: Gauge, kappa: float, mu: float = 0.0, op: int = OP_D, nact=None):
+    _check(lib().qcdgpu_dslash_mrhs(out.h, inp.h, g.h, kappa, mu, op, inp.n if nact is None else nact),
+           "qcdgpu_dslash_mrhs")
+
+
+class Batch:
+    """Batched multi-RHS solver with continuous admission (qcdgpu_batch)."""
+
+    def __init__(self, g: Gauge, capacity: int):
+        self.h = C.c_void_p()
+        self.capacity = capacity
+        _check(lib().qcdgpu_batch_create(C.byref(self.h), g.h, capacity), "qcdgpu_batch_create")
+
+    def add(self, x: Field, b: Field, kappa: float, mu: float = 0.0, op: int = OP_D, tol: float = 1e-10,
+            maxiter: int = 0, delta: float = 0.1, tag: int = 0) -> int:
+        """Returns the slot, or -1 when the batch is full."""
+        k = lib().qcdgpu_batch_add(self.h, x.h, b.h, kappa, mu, op, tol, maxiter, delta, tag)
+        if k == -2:
+            raise QcdGpuError(f"qcdgpu_batch_add failed: {lib().qcdgpu_last_error().decode()}")
+        return k
+
+    def step(self, iterations: int = 16) -> None:
+        if lib().qcdgpu_batch_step(self.h, iterations) != 0:
+            raise QcdGpuError(f"qcdgpu_batch_step failed: {lib().qcdgpu_last_error().decode()}")
+
+    @property
+    def active(self) -> int:
+        return lib().qcdgpu_batch_active(self.h)
+
+    @property
+    def free_slots(self) -> int:
+        return lib().qcdgpu_batch_free_slots(self.h)
+
+    def nbytes(self) -> int:
+        return lib().qcdgpu_batch_bytes(self.h)
+
+    def poll(self, max_n: int = 64):
+        """[(tag, status, iterations, true_residual)] of the retired right-hand sides."""
+        tags = np.zeros(max_n, np.int32)
+        st = np.zeros(max_n, np.int32)
+        it = np.zeros(max_n, np.int32)
+        tr = np.zeros(max_n, np.float64)
+        n = lib().qcdgpu_batch_poll(self.h, tags, st, it, tr, max_n)
+        return [(int(tags[i]), int(st[i]), int(it[i]), float(tr[i])) for i in range(n)]
+
+    def close(self):
+        if self.h:
+            lib().qcdgpu_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -19,7 +19,7 @@ using namespace qgd;
 
 
 // float-float kernel for FP64 storage (dslash_df64.cu)
-bool dslash_df64(const DArgs &a, bool dag, int recon);
+bool dslash_df64(const DArgs &a, bool dag);
 
 template <bool DAG>
 static bool launch_native(const DArgs &a, int prec, int recon)
@@ -36,9 +36,10 @@ static bool launch_native(const DArgs &a, int prec, int recon)
 }
 
 static bool dslash_once(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4, double tm,
-                        bool dag, bool q, int arith)
+                        bool dag, bool q, int arith, double *partials = nullptr)
 {
   DArgs a;
+  a.partials = partials;
   a.out = out->data;
   a.out_norm = out->norm;
   a.in = in->data;
@@ -72,7 +73,14 @@ static bool dslash_once(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, doubl
   }
   split_host(a.mp4, &a.mp4_h, &a.mp4_l);
   split_host(a.tm, &a.tm_h, &a.tm_l);
-  if (in->prec == QCDGPU_F64 && arith == QCDGPU_ARITH_DF64) return dslash_df64(a, dag, g->recon);
+  if (in->prec == QCDGPU_F64 && arith == QCDGPU_ARITH_DF64) {
+    // float-pair copy of the links (made once per field, phases folded in)
+    qcdgpu_gauge gf = gauge_at(g, kGaugeFF);
+    if (!gf) return false;
+    a.gauge = gf->data;
+    a.gstride = gf->stride;
+    return dslash_df64(a, dag);
+  }
   return dag ? launch_native<true>(a, in->prec, g->recon) : launch_native<false>(a, in->prec, g->recon);
 }
 
@@ -110,6 +118,16 @@ bool dslash(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4, doubl
   }
   default: set_error("dslash: unknown operator %d", op); return false;
   }
+}
+
+// out = D in (dag: D^+ in) on fields checked by the caller; when partials is
+// non-null, block b of the launch (128 sites each) also writes the sum of
+// |out|^2 over its sites to partials[b]
+bool dslash_partials(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4, double tm, bool dag,
+                     int arith, double *partials)
+{
+  if (arith < 0) arith = g_f64_arith;
+  return dslash_once(out, in, g, mp4, tm, dag, false, arith, partials);
 }
 
 int g_f64_arith = QCDGPU_ARITH_F64;

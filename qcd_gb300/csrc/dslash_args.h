@@ -20,8 +20,24 @@ struct DArgs {
   double phr[4], phi[4], mp4, tm;  // tm already negated for D^+
   float phr_h[4], phr_l[4], phi_h[4], phi_l[4], mp4_h, mp4_l, tm_h, tm_l;
   int twist_mask;
-  int op_q;  // multiply the result by i g5
+  int op_q;          // multiply the result by i g5
+  double *partials;  // non-null: block b writes sum over its sites of |out|^2 to partials[b]
 };
+
+// |v|^2 summed over the block into partials[blockIdx.x]; every thread of the
+// block must call it (blockDim.x a multiple of 32, at most 1024)
+__device__ __forceinline__ void block_partial(double v, double *partials)
+{
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __shared__ double sh[32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += sh[i];
+    partials[blockIdx.x] = s;
+  }
+}
 
 // a launch scalar in the kernel's arithmetic type R
 template <typename R>

@@ -1,135 +1,352 @@
-// dslash_df64.cu -- the operator on FP64 fields in float-float arithmetic.
+// dslash_df64.cu -- the Wilson-TM operator on FP64 fields in float-float
+// arithmetic.
 //
 // GB300 executes FP64 fused multiply-adds at about 1/60 of its FP32 rate
-// (measured: 0.60 T DFMA/s against 35 T FFMA/s), so an FP64 Wilson operator
-// computed natively is bound by the FP64 pipe, not by HBM. This
-// instantiation keeps FP64 storage (fields are read and written as doubles)
-// but computes with unevaluated pairs of floats (hi + lo, ~48 significant
-// bits) on the FP32 pipes:
-//   * sum: Knuth's TwoSum of the high words plus the low words, then
-//     renormalised (Fast2Sum);
-//   * product: Dekker's exact product of the high words via FMA, plus the two
-//     cross terms, renormalised.
-// (T. J. Dekker, Numer. Math. 18 (1971) 224; D. E. Knuth, TAOCP vol. 2.)
-// Every operation uses the explicitly rounded intrinsics so the compiler can
-// neither contract nor reorder them. Conversions between double and the
-// float pair are done with integer operations on the bit patterns (the
-// hardware conversions run on the FP64 pipe too). Values whose magnitude lies
-// outside [2^-74, 2^127) take a slower exact path; doubles below 2^-1022
-// (denormals) count as zero. The result differs from FP64 by a few 2^-47
-// relative, inside the 1e-13 per-site parity bar.
-#include "wilson_kernel.cuh"
+// (measured: 0.60 T DFMA/s against 35 T FFMA/s), so the FP64 operator
+// computed natively is bound by the FP64 pipe, not by HBM. This kernel keeps
+// FP64 storage for the spinors (read and written as doubles) and computes on
+// the FP32 pipes with unevaluated float pairs (hi + lo, ~48 significant bits):
+//   * products: Dekker's exact product of the high words via FMA plus the two
+//     cross terms (T. J. Dekker, Numer. Math. 18 (1971) 224);
+//   * sums: Knuth's TwoSum (TAOCP vol. 2) into lazy accumulators (s, e) whose
+//     error word collects the rounding errors in FP32; an accumulator is
+//     renormalised (Fast2Sum) only when its value is consumed.
+// Every operation uses the explicitly rounded intrinsics, so the compiler can
+// neither contract nor reorder them. Double <-> float-pair conversions of the
+// spinors use integer bit operations, because the hardware conversions run on
+// the FP64 pipe. The links come from a copy of the gauge field stored as
+// float pairs, made once per field, with the boundary phase e^{i th/L}
+// multiplied into the links of twisted directions (U' h for the forward hop,
+// U'^+ h = e^{-i th/L} U^+ h for the backward one, as qcd_wilson.c applies it).
+// The result differs from FP64 by a few 2^-47 relative, within the 1e-13
+// per-site parity bar. Spinor values must lie in [2^-74, 2^127) in magnitude
+// for the fast conversion; other values take an exact slower path, and
+// doubles below 2^-1022 (denormals) count as zero.
+#include "dslash_args.h"
 
 namespace qg {
 
-__device__ __forceinline__ float f_from_bits(unsigned b) { return __uint_as_float(b); }
+using namespace qgd;
 
-struct FF {
+struct F2 {  // h + l
   float h, l;
-  FF() = default;
-  __device__ __forceinline__ FF(float hi, float lo) : h(hi), l(lo) {}
-
-  // double -> (hi, lo): hi = the leading 24 significand bits (truncated),
-  // lo = the next 29 bits rounded to 24, both carrying the sign of d
-  __device__ __forceinline__ explicit FF(double d)
-  {
-    unsigned lo32 = (unsigned)__double2loint(d), hi32 = (unsigned)__double2hiint(d);
-    unsigned e = (hi32 >> 20) & 0x7ffu;
-    unsigned sign = hi32 & 0x80000000u;
-    if (e >= 949u && e <= 1150u) {
-      h = f_from_bits(sign | ((e - 896u) << 23) | ((hi32 & 0xfffffu) << 3) | (lo32 >> 29));
-      unsigned r = lo32 & 0x1fffffffu;  // value r * 2^(e - 1075)
-      // r as a float: two exact 23-bit pieces joined by one rounding FMA
-      float f1 = __fsub_rn(f_from_bits(0x4B000000u | (r >> 6)), 8388608.0f);
-      float f2 = __fsub_rn(f_from_bits(0x4B000000u | (r & 63u)), 8388608.0f);
-      float rf = __fmaf_rn(f1, 64.0f, f2);
-      float lo = __fmul_rn(rf, f_from_bits((e - 948u) << 23));
-      l = __uint_as_float(__float_as_uint(lo) ^ sign);
-    } else if (e == 0u) {
-      h = f_from_bits(sign);
-      l = 0.0f;
-    } else {
-      h = __double2float_rn(d);
-      l = __double2float_rn(__dsub_rn(d, (double)h));
-    }
-  }
-
-  // (hi, lo) -> double by integer arithmetic on the significands; lo's bits
-  // below the double's last place are truncated (|lo| <= ulp(hi) here)
-  __device__ __forceinline__ explicit operator double() const
-  {
-    unsigned hb = __float_as_uint(h), lb = __float_as_uint(l);
-    unsigned eh = (hb >> 23) & 0xffu;
-    if ((hb & 0x7fffffffu) == 0u) return (double)l;  // zero hi: lo is the value
-    if (eh == 0u || eh == 255u) return __dadd_rn((double)h, (double)l);
-    unsigned long long M = (unsigned long long)((hb & 0x7fffffu) | 0x800000u) << 29;
-    unsigned el = (lb >> 23) & 0xffu;
-    if (el != 0u && el != 255u) {
-      unsigned long long ml = (unsigned long long)((lb & 0x7fffffu) | 0x800000u);
-      int sh = 29 - ((int)eh - (int)el);
-      unsigned long long add = sh >= 0 ? (ml << sh) : (sh > -60 ? (ml >> (-sh)) : 0ull);
-      if ((hb ^ lb) & 0x80000000u) M -= add;
-      else M += add;
-    }
-    int e = (int)eh + 896;
-    if (M >= (1ull << 53)) {
-      M >>= 1;
-      e += 1;
-    } else if (M < (1ull << 52)) {
-      if (M == 0ull) return 0.0;
-      int z = __clzll((long long)M) - 11;
-      M <<= z;
-      e -= z;
-    }
-    return __longlong_as_double((long long)(((unsigned long long)(hb >> 31) << 63) |
-                                            ((unsigned long long)e << 52) | (M & ((1ull << 52) - 1))));
-  }
+};
+struct FA {  // accumulator: value s + e, not normalised
+  float s, e;
+};
+struct CF {
+  F2 re, im;
+};
+struct CA {
+  FA re, im;
 };
 
-__device__ __forceinline__ FF fast2sum(float a, float b)
+// out of line so the common path carries no FP64 instructions
+__device__ __noinline__ F2 split_slow(double d)
 {
-  float s = __fadd_rn(a, b);
-  return FF(s, __fsub_rn(b, __fsub_rn(s, a)));
+  F2 r;
+  r.h = __double2float_rn(d);
+  r.l = __double2float_rn(__dsub_rn(d, (double)r.h));
+  return r;
 }
 
-__device__ __forceinline__ FF operator+(FF a, FF b)
+__device__ __forceinline__ F2 split_d(double d)
 {
-  float s = __fadd_rn(a.h, b.h);
-  float bb = __fsub_rn(s, a.h);
-  float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
-  e = __fadd_rn(e, __fadd_rn(a.l, b.l));
-  return fast2sum(s, e);
+  unsigned lo32 = (unsigned)__double2loint(d), hi32 = (unsigned)__double2hiint(d);
+  unsigned e = (hi32 >> 20) & 0x7ffu;
+  unsigned sign = hi32 & 0x80000000u;
+  F2 r;
+  if (e >= 949u && e <= 1150u) {
+    // hi: the leading 24 significand bits (truncated); lo: the next 29 bits
+    // rounded to 24 -- built from two exact 23-bit pieces and one FMA
+    r.h = __uint_as_float(sign | ((e - 896u) << 23) | ((hi32 & 0xfffffu) << 3) | (lo32 >> 29));
+    unsigned rem = lo32 & 0x1fffffffu;  // value rem * 2^(e - 1075)
+    float f1 = __fsub_rn(__uint_as_float(0x4B000000u | (rem >> 6)), 8388608.0f);
+    float f2 = __fsub_rn(__uint_as_float(0x4B000000u | (rem & 63u)), 8388608.0f);
+    float lo = __fmul_rn(__fmaf_rn(f1, 64.0f, f2), __uint_as_float((e - 948u) << 23));
+    r.l = __uint_as_float(__float_as_uint(lo) ^ sign);
+  } else if (e == 0u) {
+    r.h = __uint_as_float(sign);
+    r.l = 0.0f;
+  } else {
+    r = split_slow(d);
+  }
+  return r;
 }
-__device__ __forceinline__ FF operator-(FF a) { return FF(-a.h, -a.l); }
-__device__ __forceinline__ FF operator-(FF a, FF b) { return a + (-b); }
-__device__ __forceinline__ FF operator*(FF a, FF b)
+
+// h + l -> double with integer arithmetic; lo bits beyond the double's last
+// place are truncated (|l| <= ulp(h) for renormalised pairs)
+__device__ __forceinline__ double join_d(F2 x)
+{
+  unsigned hb = __float_as_uint(x.h), lb = __float_as_uint(x.l);
+  unsigned eh = (hb >> 23) & 0xffu;
+  if ((hb & 0x7fffffffu) == 0u) return (double)x.l;
+  if (eh == 0u || eh == 255u) return __dadd_rn((double)x.h, (double)x.l);
+  unsigned long long M = (unsigned long long)((hb & 0x7fffffu) | 0x800000u) << 29;
+  unsigned el = (lb >> 23) & 0xffu;
+  if (el != 0u && el != 255u) {
+    unsigned long long ml = (unsigned long long)((lb & 0x7fffffu) | 0x800000u);
+    int sh = 29 - ((int)eh - (int)el);
+    unsigned long long add = sh >= 0 ? (ml << sh) : (sh > -60 ? (ml >> (-sh)) : 0ull);
+    if ((hb ^ lb) & 0x80000000u) M -= add;
+    else M += add;
+  }
+  int e = (int)eh + 896;
+  if (M >= (1ull << 53)) {
+    M >>= 1;
+    e += 1;
+  } else if (M < (1ull << 52)) {
+    if (M == 0ull) return 0.0;
+    int z = __clzll((long long)M) - 11;
+    M <<= z;
+    e -= z;
+  }
+  return __longlong_as_double((long long)(((unsigned long long)(hb >> 31) << 63) | ((unsigned long long)e << 52) |
+                                          (M & ((1ull << 52) - 1))));
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &q)
+{
+  s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  q = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ F2 neg(F2 a) { return F2{-a.h, -a.l}; }
+// a + b, unnormalised
+__device__ __forceinline__ F2 add(F2 a, F2 b)
+{
+  F2 r;
+  float q;
+  two_sum(a.h, b.h, r.h, q);
+  r.l = __fadd_rn(q, __fadd_rn(a.l, b.l));
+  return r;
+}
+__device__ __forceinline__ F2 fin(FA a)
+{
+  float s = __fadd_rn(a.s, a.e);
+  return F2{s, __fsub_rn(a.e, __fsub_rn(s, a.s))};
+}
+// acc += a * b
+__device__ __forceinline__ void mac(FA &acc, F2 a, F2 b)
 {
   float p = __fmul_rn(a.h, b.h);
-  float e = __fmaf_rn(a.h, b.h, -p);
+  float t = __fmaf_rn(a.h, b.h, -p);
+  float s, q;
+  two_sum(acc.s, p, s, q);
+  float e = __fadd_rn(acc.e, __fadd_rn(t, q));
   e = __fmaf_rn(a.h, b.l, e);
-  e = __fmaf_rn(a.l, b.h, e);
-  return fast2sum(p, e);
+  acc.e = __fmaf_rn(a.l, b.h, e);
+  acc.s = s;
+}
+// acc += x
+__device__ __forceinline__ void acc_add(FA &acc, F2 x)
+{
+  float s, q;
+  two_sum(acc.s, x.h, s, q);
+  acc.e = __fadd_rn(acc.e, __fadd_rn(q, x.l));
+  acc.s = s;
 }
 
-template <>
-struct Scalar<FF> {
-  __device__ __forceinline__ static FF get(double, float h, float l) { return FF(h, l); }
-};
+__device__ __forceinline__ CF cadd(CF a, CF b) { return CF{add(a.re, b.re), add(a.im, b.im)}; }
+__device__ __forceinline__ CF cneg(CF a) { return CF{neg(a.re), neg(a.im)}; }
+__device__ __forceinline__ CF ci(CF a) { return CF{neg(a.im), a.re}; }  // i a
+__device__ __forceinline__ void cacc(CA &acc, CF x)
+{
+  acc_add(acc.re, x.re);
+  acc_add(acc.im, x.im);
+}
+
+__device__ __forceinline__ CF load_sp(const double2 *base, int64_t stride, int y, int k)
+{
+  double2 v = __ldg(base + (int64_t)k * stride + y);
+  return CF{split_d(v.x), split_d(v.y)};
+}
+__device__ __forceinline__ CF load_link(const float4 *base, int64_t stride, int y, int mu, int k)
+{
+  float4 v = __ldg(base + ((int64_t)mu * 9 + k) * stride + y);
+  return CF{F2{v.x, v.y}, F2{v.z, v.w}};
+}
+
+// z -> (i z if ifl) then negated if ng; ifl and ng are warp-uniform
+__device__ __forceinline__ CF coef(CF z, bool ifl, bool ng)
+{
+  CF r = ifl ? CF{neg(z.im), z.re} : z;
+  return ng ? cneg(r) : r;
+}
+
+// Thread layout: a block of 384 threads covers 128 sites as four groups of
+// three warps; warp w of a group owns colour row i = w for its 32 sites and
+// the four accumulators (spins 0..3) of that colour. Per hop each warp
+// projects the neighbour spinor of its colour, the three warps share the
+// half spinors through shared memory, and each warp multiplies its link row.
+// The hops run as a loop with one compiled body; with S the projector sign,
+// (1 + S g_mu) in the chiral basis is
+//   h0 = p0 + c0 p_b0, h1 = p1 + c1 p_b1            (upper half)
+//   b0 = 2 (mu 0,3) or 3 (mu 1,2), b1 = 5 - b0, c = +-1 (mu even) or +-i (odd)
+//   c0 = -S ; c1 = -S (mu 0,1) or +S (mu 2,3)
+// and the lower half rebuilt from v = U h:
+//   r2 = cA v_jA, r3 = cB v_jB ; jA = 1 for mu 1,2 else 0, jB = 1 - jA
+//   cA = -S (mu 0) else +S ; cB = +S (mu 1) else -S ; times i for odd mu
+// (qcd_wilson.h:17-387).
+constexpr int kFFSites = 128;
 
 template <bool DAG>
-static bool launch_ff(const DArgs &a)
+__global__ void __launch_bounds__(384) k_wilson_ff(const DArgs a)
 {
-  unsigned grid = (unsigned)((a.V + 127) / 128);
-  // all 9 link entries are read: rebuilding row 2 costs more float-float
-  // arithmetic than the extra 192 bytes per site cost in bandwidth
-  k_wilson<DAG, QCDGPU_F64, QCDGPU_F64, 18, FF><<<grid, 128, 0, stream()>>>(a);
-  return QG_LAUNCHED("wilson_df64");
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int grp = w / 3, col = w - 3 * grp;
+  const int x = blockIdx.x * kFFSites + grp * 32 + lane;
+  const bool act = x < a.V;
+  __shared__ CF hs[4][2][3][32];
+  const double2 *sp = (const double2 *)a.in;
+  const float4 *gf = (const float4 *)a.gauge;
+  constexpr int SF = DAG ? +1 : -1;
+  int c[4] = {0, 0, 0, 0};
+  if (act) coords(a.geo, x, c);
+  CA acc[4];
+#pragma unroll
+  for (int s = 0; s < 4; s++) acc[s] = CA{{0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll 1
+  for (int d = 0; d < 8; d++) {
+    const int mu = d >> 1;
+    const bool back = d & 1;
+    const int S = back ? -SF : SF;
+    const int cm = mu == 0 ? c[0] : mu == 1 ? c[1] : mu == 2 ? c[2] : c[3];
+    const int Lm = a.geo.L[mu], st = a.geo.st[mu];
+    int y = x;
+    if (act) {
+      if (back) y = cm == 0 ? x + (Lm - 1) * st : x - st;
+      else y = cm == Lm - 1 ? x - (Lm - 1) * st : x + st;
+    }
+    const int ly = back ? y : x;
+    const bool odd = mu & 1;
+    const int b0 = (mu == 0 || mu == 3) ? 2 : 3, b1 = 5 - b0;
+    const bool neg0 = S > 0, neg1 = mu < 2 ? S > 0 : S < 0;
+    CF h0 = {{0.f, 0.f}, {0.f, 0.f}}, h1 = h0;
+    if (act) {
+      CF p0 = load_sp(sp, a.stride, y, col), p1 = load_sp(sp, a.stride, y, 3 + col);
+      CF q0 = load_sp(sp, a.stride, y, 3 * b0 + col), q1 = load_sp(sp, a.stride, y, 3 * b1 + col);
+      h0 = cadd(p0, coef(q0, odd, neg0));
+      h1 = cadd(p1, coef(q1, odd, neg1));
+    }
+    hs[grp][0][col][lane] = h0;
+    hs[grp][1][col][lane] = h1;
+    __syncthreads();
+    CA u0 = {{0.f, 0.f}, {0.f, 0.f}}, u1 = u0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      CF g0 = hs[grp][0][k][lane], g1 = hs[grp][1][k][lane];
+      // forward: U[col][k]; backward: conj(U[k][col])
+      CF wl = act ? load_link(gf, a.gstride, ly, mu, back ? 3 * k + col : 3 * col + k) : CF{{0.f, 0.f}, {0.f, 0.f}};
+      F2 wr = wl.re, wi = back ? neg(wl.im) : wl.im, mwi = neg(wi);
+      mac(u0.re, wr, g0.re);
+      mac(u0.re, mwi, g0.im);
+      mac(u0.im, wr, g0.im);
+      mac(u0.im, wi, g0.re);
+      mac(u1.re, wr, g1.re);
+      mac(u1.re, mwi, g1.im);
+      mac(u1.im, wr, g1.im);
+      mac(u1.im, wi, g1.re);
+    }
+    CF v0{fin(u0.re), fin(u0.im)}, v1{fin(u1.re), fin(u1.im)};
+    const bool jA = (mu == 1 || mu == 2);
+    const bool negA = mu == 0 ? S > 0 : S < 0, negB = mu == 1 ? S < 0 : S > 0;
+    cacc(acc[0], v0);
+    cacc(acc[1], v1);
+    cacc(acc[2], coef(jA ? v1 : v0, odd, negA));
+    cacc(acc[3], coef(jA ? v0 : v1, odd, negB));
+    __syncthreads();  // hs is rewritten by the next hop
+  }
+  double n2 = 0.0;
+  if (act) {
+    double2 *out = (double2 *)a.out;
+    const F2 mp4{a.mp4_h, a.mp4_l}, tm{a.tm_h, a.tm_l};
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+      // (m+4) psi + i tm g5 psi - acc/2 for component (spin s, colour col)
+      const int k = 3 * s + col;
+      CF sv = load_sp(sp, a.stride, x, k);
+      F2 g5tm = s < 2 ? tm : neg(tm), mg5tm = neg(g5tm);
+      F2 ar = fin(acc[s].re), ai = fin(acc[s].im);
+      FA re{__fmul_rn(ar.h, -0.5f), __fmul_rn(ar.l, -0.5f)};
+      FA im{__fmul_rn(ai.h, -0.5f), __fmul_rn(ai.l, -0.5f)};
+      mac(re, mp4, sv.re);
+      mac(re, mg5tm, sv.im);
+      mac(im, mp4, sv.im);
+      mac(im, g5tm, sv.re);
+      F2 dr = fin(re), di = fin(im);
+      if (a.op_q) {  // i g5: spins 0,1 times i, spins 2,3 times -i
+        F2 t = dr;
+        if (s < 2) {
+          dr = neg(di);
+          di = t;
+        } else {
+          dr = di;
+          di = neg(t);
+        }
+      }
+      double vr = join_d(dr), vi = join_d(di);
+      out[(int64_t)k * a.stride + x] = make_double2(vr, vi);
+      n2 += vr * vr + vi * vi;
+    }
+  }
+  if (a.partials) block_partial(n2, a.partials);
 }
 
-bool dslash_df64(const DArgs &a, bool dag, int recon)
+// ------------------------------------------------------ float-pair links
+__global__ void k_gauge_to_ff(float4 *dst, int64_t dstride, const double2 *src, int64_t sstride, int64_t V,
+                              DArgs phases)
 {
-  (void)recon;
-  return dag ? launch_ff<true>(a) : launch_ff<false>(a);
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= V * 4) return;
+  int64_t x = i >> 2;
+  int mu = (int)(i & 3);
+  bool tw = (phases.twist_mask >> mu) & 1;
+  double pr = phases.phr[mu], pi = phases.phi[mu];
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    double2 u = src[((int64_t)mu * 9 + k) * sstride + x];
+    double re = u.x, im = u.y;
+    if (tw) {
+      re = u.x * pr - u.y * pi;
+      im = u.x * pi + u.y * pr;
+    }
+    float rh = __double2float_rn(re), ih = __double2float_rn(im);
+    dst[((int64_t)mu * 9 + k) * dstride + x] =
+        make_float4(rh, __double2float_rn(re - (double)rh), ih, __double2float_rn(im - (double)ih));
+  }
+}
+
+bool gauge_to_ff(qcdgpu_gauge d, qcdgpu_gauge s)
+{
+  if (s->prec != QCDGPU_F64) {
+    set_error("float-pair links are made from an FP64 gauge field");
+    return false;
+  }
+  DArgs ph;
+  ph.twist_mask = 0;
+  for (int mu = 0; mu < 4; mu++) {
+    ph.phr[mu] = 1.0;
+    ph.phi[mu] = 0.0;
+    if (s->theta[mu] != 0.0) {
+      ph.twist_mask |= 1 << mu;
+      ph.phr[mu] = cos(s->theta[mu] / (double)s->L[mu]);
+      ph.phi[mu] = sin(s->theta[mu] / (double)s->L[mu]);
+    }
+  }
+  d->recon = 18;
+  for (int i = 0; i < 4; i++) d->theta[i] = s->theta[i];
+  unsigned gr = (unsigned)((s->V * 4 + 127) / 128);
+  k_gauge_to_ff<<<gr, 128, 0, stream()>>>((float4 *)d->data, d->stride, (const double2 *)s->data, s->stride, s->V, ph);
+  return QG_LAUNCHED("gauge_to_ff");
+}
+
+bool dslash_df64(const DArgs &a, bool dag)
+{
+  unsigned grid = (unsigned)((a.V + kFFSites - 1) / kFFSites);
+  if (dag) k_wilson_ff<true><<<grid, 384, 0, stream()>>>(a);
+  else k_wilson_ff<false><<<grid, 384, 0, stream()>>>(a);
+  return QG_LAUNCHED("wilson_df64");
 }
 
 }  // namespace qg

@@ -44,6 +44,15 @@ cudaStream_t stream();
 // ------------------------------------------------------------------ fields
 inline int64_t pad_stride(int64_t V) { return (V + 127) / 128 * 128; }
 
+// Internal gauge storage used by the float-float operator: every link entry
+// as a float pair (re_hi, re_lo, im_hi, im_lo) in one float4, 4 mu x 9 blocks,
+// with the boundary phase e^{i theta_mu / L_mu} already multiplied into the
+// links of every direction whose theta is non-zero.
+constexpr int kGaugeFF = 3;
+// Internal key of the FP32 copy with all 18 reals per link (4 mu x 9 float2),
+// read by the tensor-core multi-RHS operator (it needs every entry).
+constexpr int kGaugeF32Full = 4;
+
 }  // namespace qg
 
 struct qcdgpu_field_s {
@@ -83,7 +92,7 @@ void work_put(qcdgpu_field f);
 // scratch for reductions: 2 * kMaxPartials doubles + result slots
 constexpr int kMaxPartials = 2048;
 double *reduce_scratch();
-double *host_result();  // pinned host slots, 16 doubles
+double *host_result();  // pinned host slots, 64 doubles
 
 // layout.cu
 bool upload_spinor_aos(qcdgpu_field f, const double *host);
@@ -91,7 +100,8 @@ bool download_spinor_aos(qcdgpu_field f, double *host);
 bool upload_gauge_aos(qcdgpu_gauge g, const double *host);  // decides recon
 bool download_gauge_aos(qcdgpu_gauge g, double *host);
 bool convert_field(qcdgpu_field dst, qcdgpu_field src);
-bool convert_gauge(qcdgpu_gauge dst, qcdgpu_gauge src);
+// force_recon = 18 stores all 18 reals even for SU(3) links (FP32 targets)
+bool convert_gauge(qcdgpu_gauge dst, qcdgpu_gauge src, int force_recon = 0);
 // device staging buffer of at least `bytes` (single-threaded use) and the
 // SU(3)-check + packing of a gauge field held there in the host layout
 void *stage_buffer(size_t bytes);

@@ -309,8 +309,11 @@ bool download_gauge_aos(qcdgpu_gauge g, double *host)
   return QG_CUDA(cudaStreamSynchronize(stream()));
 }
 
-bool convert_gauge(qcdgpu_gauge d, qcdgpu_gauge s)
+bool gauge_to_ff(qcdgpu_gauge d, qcdgpu_gauge s);  // dslash_df64.cu
+
+bool convert_gauge(qcdgpu_gauge d, qcdgpu_gauge s, int force_recon)
 {
+  if (d->prec == kGaugeFF) return gauge_to_ff(d, s);
   if (d->V != s->V) {
     set_error("gauge convert: volumes differ");
     return false;
@@ -319,7 +322,7 @@ bool convert_gauge(qcdgpu_gauge d, qcdgpu_gauge s)
     set_error("half-precision gauge fields need SU(3) links");
     return false;
   }
-  d->recon = s->recon;
+  d->recon = force_recon ? force_recon : s->recon;
   memcpy(d->theta, s->theta, sizeof(d->theta));
   unsigned gr = grid_for(s->V * 4, 128);
 #define QG_CONV(SP, SR)                                                                          \

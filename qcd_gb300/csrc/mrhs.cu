@@ -1,0 +1,414 @@
+// mrhs.cu -- many right-hand sides sharing one gauge-field read.
+//
+// A multi-RHS field holds N spinors in FP16 with one float norm per
+// (site, RHS), laid out [component 0..11][site][rhs] as half2 (re, im), so
+// the RHS of one site and component are contiguous.
+//
+// Operator (tensor cores): one warp per site. For each of the eight hops the
+// warp builds, for 16 RHS at a time, the matrix A (16 RHS x 12 reals of the
+// projected half spinor, padded to 16) and multiplies it with
+//   B = realified ( R_mu (x) U_mu )   (12 x 24, padded to 16 x 24)
+// where U_mu is the link (or U^+ for backward hops, phase e^{+-i th/L}
+// folded in) and R_mu the 4 x 2 spin matrix that rebuilds the lower spinor
+// half from the upper one (qcd_wilson.h:17-387). The eight products
+// accumulate in the same FP32 MMA accumulators (mma.sync m16n8k8, TF32
+// operands), so the link is read once per site for all N RHS and the
+// per-RHS arithmetic runs on the tensor pipe; the diagonal term and the FP16
+// re-normalisation are the epilogue. TF32 keeps the FP32 exponent range, so
+// small residual vectors need no rescaling.
+#include <string.h>
+
+#include "dslash_args.h"
+
+struct qcdgpu_mfield_s {
+  int L[4];
+  int64_t V;
+  int N;     // RHS slots
+  void *data;
+  float *norm;
+  size_t bytes;
+};
+
+namespace qg {
+
+using namespace qgd;
+
+struct MArgs {
+  __half2 *out;
+  float *out_norm;
+  const __half2 *in;
+  const float *in_norm;
+  const float2 *gauge;  // FP32, 4 mu x 9 float2 blocks
+  Geom geo;
+  int V, N, nact;
+  int64_t gstride;
+  float phr[4], phi[4];
+  int twist_mask;
+  float mp4, tm;  // tm negated for D^+
+  // per-slot diagonal (m+4 and tm of each RHS) when non-null; the hopping
+  // term does not depend on kappa or mu, so one batch may mix both
+  const float *mp4s, *tms;
+};
+
+__device__ __forceinline__ float2 mload(const __half2 *d, const float *nrm, int V, int N, int k, int site, int r)
+{
+  float2 f = __half22float2(d[((int64_t)k * V + site) * N + r]);
+  float s = nrm[(int64_t)site * N + r];
+  return make_float2(f.x * s, f.y * s);
+}
+
+__device__ __forceinline__ unsigned to_tf32(float x)
+{
+  unsigned r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void mma_tf32(float c[4], const unsigned a[4], unsigned b0, unsigned b1)
+{
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// MT = number of 16-RHS tiles (N <= 16 MT)
+template <bool DAG, int MT>
+__global__ void __launch_bounds__(128) k_wilson_mrhs(const MArgs a)
+{
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int x = blockIdx.x * 4 + wp;
+  if (x >= a.V) return;  // the whole warp leaves together
+  const int g = lane >> 2, t = lane & 3;
+  int c[4];
+  coords(a.geo, x, c);
+  float acc[MT][3][4];
+#pragma unroll
+  for (int m = 0; m < MT; m++)
+#pragma unroll
+    for (int n = 0; n < 3; n++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) acc[m][n][q] = 0.f;
+  constexpr int SF = DAG ? +1 : -1;
+#pragma unroll 1
+  for (int d = 0; d < 8; d++) {
+    const int mu = d >> 1;
+    const bool back = d & 1;
+    const int S = back ? -SF : SF;
+    const int cm = mu == 0 ? c[0] : mu == 1 ? c[1] : mu == 2 ? c[2] : c[3];
+    const int Lm = a.geo.L[mu], st = a.geo.st[mu];
+    int y;
+    if (back) y = cm == 0 ? x + (Lm - 1) * st : x - st;
+    else y = cm == Lm - 1 ? x - (Lm - 1) * st : x + st;
+    const int ly = back ? y : x;
+    // spin structure of (1 + S g_mu): see wilson_kernel / dslash_df64 tables
+    const bool odd = mu & 1;
+    const int b0 = (mu == 0 || mu == 3) ? 2 : 3, b1 = 5 - b0;
+    const bool neg0 = S > 0, neg1 = mu < 2 ? S > 0 : S < 0;
+    const int jA = (mu == 1 || mu == 2) ? 1 : 0;
+    const bool negA = mu == 0 ? S > 0 : S < 0, negB = mu == 1 ? S < 0 : S > 0;
+    const bool tw = (a.twist_mask >> mu) & 1;
+    const float pr = a.phr[mu], pi = back ? -a.phi[mu] : a.phi[mu];
+    // B fragments: element (row kk, col n) of the realified R (x) U
+    unsigned bf[2][3][2];
+#pragma unroll
+    for (int ks = 0; ks < 2; ks++)
+#pragma unroll
+      for (int nt = 0; nt < 3; nt++)
+#pragma unroll
+        for (int hf = 0; hf < 2; hf++) {
+          const int kk = 8 * ks + t + 4 * hf, n = 8 * nt + g;
+          float v = 0.f;
+          if (kk < 12) {
+            const int j = kk / 6, cp = (kk % 6) >> 1, rip = kk & 1;
+            const int s = n / 6, cc = (n % 6) >> 1, ri = n & 1;
+            bool nz, rodd = false, rneg = false;
+            if (s < 2) {
+              nz = s == j;
+            } else if (s == 2) {
+              nz = j == jA;
+              rodd = odd;
+              rneg = negA;
+            } else {
+              nz = j == 1 - jA;
+              rodd = odd;
+              rneg = negB;
+            }
+            if (nz) {
+              float2 u = __ldg(a.gauge + ((int64_t)mu * 9 + (back ? 3 * cp + cc : 3 * cc + cp)) * a.gstride + ly);
+              float wr = u.x, wi = back ? -u.y : u.y;
+              if (tw) {
+                float tr = wr * pr - wi * pi;
+                wi = wr * pi + wi * pr;
+                wr = tr;
+              }
+              if (rodd) {
+                float tr = -wi;
+                wi = wr;
+                wr = tr;
+              }
+              if (rneg) {
+                wr = -wr;
+                wi = -wi;
+              }
+              v = rip == 0 ? (ri == 0 ? wr : wi) : (ri == 0 ? -wi : wr);
+            }
+          }
+          bf[ks][nt][hf] = to_tf32(v);
+        }
+#pragma unroll
+    for (int m = 0; m < MT; m++) {
+      float hv[2][3];
+#pragma unroll
+      for (int row = 0; row < 2; row++) {
+        const int r = 16 * m + g + 8 * row;
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+          const int kk = t + 4 * q, j = kk / 6, cc = (kk % 6) >> 1;
+          float val = 0.f;
+          if (r < a.nact) {
+            float2 p = mload(a.in, a.in_norm, a.V, a.N, 3 * j + cc, y, r);
+            float2 pb = mload(a.in, a.in_norm, a.V, a.N, 3 * (j == 0 ? b0 : b1) + cc, y, r);
+            if (odd) pb = make_float2(-pb.y, pb.x);
+            if (j == 0 ? neg0 : neg1) pb = make_float2(-pb.x, -pb.y);
+            val = (t & 1) ? p.y + pb.y : p.x + pb.x;
+          }
+          hv[row][q] = val;
+        }
+      }
+      const unsigned a0[4] = {to_tf32(hv[0][0]), to_tf32(hv[1][0]), to_tf32(hv[0][1]), to_tf32(hv[1][1])};
+      const unsigned a1[4] = {to_tf32(hv[0][2]), to_tf32(hv[1][2]), 0u, 0u};
+#pragma unroll
+      for (int nt = 0; nt < 3; nt++) {
+        mma_tf32(acc[m][nt], a0, bf[0][nt][0], bf[0][nt][1]);
+        mma_tf32(acc[m][nt], a1, bf[1][nt][0], bf[1][nt][1]);
+      }
+    }
+  }
+  // epilogue: out = (m+4) psi + i tm g5 psi - acc/2, stored as FP16 + norm
+#pragma unroll
+  for (int m = 0; m < MT; m++)
+#pragma unroll
+    for (int row = 0; row < 2; row++) {
+      const int r = 16 * m + g + 8 * row;
+      const bool live = r < a.nact;
+      const float mp4r = (a.mp4s && live) ? a.mp4s[r] : a.mp4;
+      const float tmr = (a.tms && live) ? (DAG ? -a.tms[r] : a.tms[r]) : a.tm;
+      float2 o[3];
+      float mx = 0.f;
+#pragma unroll
+      for (int nt = 0; nt < 3; nt++) {
+        const int q = 4 * nt + t, s = q / 3;
+        float2 cq = make_float2(acc[m][nt][2 * row], acc[m][nt][2 * row + 1]);
+        float2 ps = live ? mload(a.in, a.in_norm, a.V, a.N, q, x, r) : make_float2(0.f, 0.f);
+        const float g5tm = s < 2 ? tmr : -tmr;
+        o[nt] = make_float2(mp4r * ps.x - g5tm * ps.y - 0.5f * cq.x, mp4r * ps.y + g5tm * ps.x - 0.5f * cq.y);
+        mx = fmaxf(mx, fmaxf(fabsf(o[nt].x), fabsf(o[nt].y)));
+      }
+      // the 12 components of RHS r are spread over the 4 lanes of its quad
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 2));
+      if (!(mx >= 1.17549435e-38f)) mx = 0.f;
+      const float inv = mx > 0.f ? 1.0f / mx : 0.f;
+      if (live) {
+#pragma unroll
+        for (int nt = 0; nt < 3; nt++) {
+          const int q = 4 * nt + t;
+          a.out[((int64_t)q * a.V + x) * a.N + r] = __floats2half2_rn(o[nt].x * inv, o[nt].y * inv);
+        }
+        if (t == 0) a.out_norm[(int64_t)x * a.N + r] = mx;
+      }
+    }
+}
+
+// ------------------------------------------------------------ fields
+qcdgpu_mfield mfield_new(const int L[4], int N)
+{
+  if (N < 1 || N > 64) {
+    set_error("multi-RHS fields hold 1..64 right-hand sides (got %d)", N);
+    return nullptr;
+  }
+  qcdgpu_field probe = field_new(L, QCDGPU_F16);  // validates L and the volume
+  if (!probe) return nullptr;
+  field_free(probe);
+  auto *m = new qcdgpu_mfield_s();
+  memcpy(m->L, L, sizeof(m->L));
+  m->V = (int64_t)L[0] * L[1] * L[2] * L[3];
+  m->N = N;
+  size_t nd = (size_t)12 * m->V * N * sizeof(__half2), nn = (size_t)m->V * N * sizeof(float);
+  m->bytes = nd + nn;
+  if (!QG_CUDA(cudaMalloc(&m->data, m->bytes))) {
+    delete m;
+    return nullptr;
+  }
+  m->norm = (float *)((char *)m->data + nd);
+  if (!QG_CUDA(cudaMemsetAsync(m->data, 0, m->bytes, stream()))) {
+    cudaFree(m->data);
+    delete m;
+    return nullptr;
+  }
+  return m;
+}
+
+void mfield_free(qcdgpu_mfield m)
+{
+  if (!m) return;
+  cudaFree(m->data);
+  delete m;
+}
+
+// slot r of m <- f (f in any storage precision)
+template <int P>
+__global__ void k_pack(__half2 *d, float *dn, int V, int N, int r, const void *f, const float *fn, int64_t stride)
+{
+  int x = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (x >= V) return;
+  C<float> s[12];
+  Spinor<P, float>::load(f, fn, stride, x, s);
+  float mx = 0.f;
+#pragma unroll
+  for (int k = 0; k < 12; k++) mx = fmaxf(mx, fmaxf(fabsf(s[k].re), fabsf(s[k].im)));
+  if (!(mx >= 1.17549435e-38f)) mx = 0.f;
+  float inv = mx > 0.f ? 1.0f / mx : 0.f;
+#pragma unroll
+  for (int k = 0; k < 12; k++) d[((int64_t)k * V + x) * N + r] = __floats2half2_rn(s[k].re * inv, s[k].im * inv);
+  dn[(int64_t)x * N + r] = mx;
+}
+
+// f <- slot r of m
+template <int P>
+__global__ void k_unpack(void *f, float *fn, int64_t stride, const __half2 *d, const float *dn, int V, int N, int r)
+{
+  int x = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (x >= V) return;
+  C<double> s[12];
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    float2 v = mload(d, dn, V, N, k, x, r);
+    s[k] = C<double>{(double)v.x, (double)v.y};
+  }
+  Spinor<P, double>::store(f, fn, stride, x, s);
+}
+
+bool mfield_set(qcdgpu_mfield m, int r, qcdgpu_field f)
+{
+  if (!m || !f || r < 0 || r >= m->N || f->V != m->V) {
+    set_error("multi-RHS set: bad slot or shape");
+    return false;
+  }
+  unsigned g = (unsigned)((m->V + 127) / 128);
+  __half2 *d = (__half2 *)m->data;
+  if (f->prec == QCDGPU_F64) k_pack<QCDGPU_F64><<<g, 128, 0, stream()>>>(d, m->norm, (int)m->V, m->N, r, f->data, f->norm, f->stride);
+  else if (f->prec == QCDGPU_F32) k_pack<QCDGPU_F32><<<g, 128, 0, stream()>>>(d, m->norm, (int)m->V, m->N, r, f->data, f->norm, f->stride);
+  else k_pack<QCDGPU_F16><<<g, 128, 0, stream()>>>(d, m->norm, (int)m->V, m->N, r, f->data, f->norm, f->stride);
+  return QG_LAUNCHED("mrhs_pack");
+}
+
+bool mfield_get(qcdgpu_field f, qcdgpu_mfield m, int r)
+{
+  if (!m || !f || r < 0 || r >= m->N || f->V != m->V) {
+    set_error("multi-RHS get: bad slot or shape");
+    return false;
+  }
+  unsigned g = (unsigned)((m->V + 127) / 128);
+  const __half2 *d = (const __half2 *)m->data;
+  if (f->prec == QCDGPU_F64) k_unpack<QCDGPU_F64><<<g, 128, 0, stream()>>>(f->data, f->norm, f->stride, d, m->norm, (int)m->V, m->N, r);
+  else if (f->prec == QCDGPU_F32) k_unpack<QCDGPU_F32><<<g, 128, 0, stream()>>>(f->data, f->norm, f->stride, d, m->norm, (int)m->V, m->N, r);
+  else k_unpack<QCDGPU_F16><<<g, 128, 0, stream()>>>(f->data, f->norm, f->stride, d, m->norm, (int)m->V, m->N, r);
+  return QG_LAUNCHED("mrhs_unpack");
+}
+
+// out = D in (dag: D^+ in) for the first nact RHS of the two fields; with
+// mp4s / tms (device float arrays) each slot r uses its own diagonal
+bool dslash_mrhs(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_gauge g, double mp4, double tm, bool dag, int nact,
+                 const float *mp4s, const float *tms)
+{
+  if (!out || !in || !g || out == in || out->N != in->N || out->V != in->V || in->V != g->V ||
+      memcmp(out->L, in->L, sizeof(in->L)) != 0 || memcmp(in->L, g->L, sizeof(g->L)) != 0) {
+    set_error("multi-RHS operator: fields differ in shape or alias");
+    return false;
+  }
+  if (nact < 0 || nact > in->N) {
+    set_error("multi-RHS operator: %d active RHS of %d slots", nact, in->N);
+    return false;
+  }
+  if (g->prec != QCDGPU_F64) {
+    set_error("multi-RHS operator takes the FP64 gauge field (it keeps its own FP32 copy)");
+    return false;
+  }
+  qcdgpu_gauge g32 = gauge_at(g, kGaugeF32Full);
+  if (!g32) return false;
+  MArgs a;
+  a.out = (__half2 *)out->data;
+  a.out_norm = out->norm;
+  a.in = (const __half2 *)in->data;
+  a.in_norm = in->norm;
+  a.gauge = (const float2 *)g32->data;
+  for (int i = 0; i < 4; i++) a.geo.L[i] = in->L[i];
+  a.geo.st[0] = 1;
+  a.geo.st[1] = in->L[0];
+  a.geo.st[2] = in->L[0] * in->L[1];
+  a.geo.st[3] = in->L[0] * in->L[1] * in->L[2];
+  a.V = (int)in->V;
+  a.N = in->N;
+  a.nact = nact;
+  a.gstride = g32->stride;
+  a.twist_mask = 0;
+  for (int mu = 0; mu < 4; mu++) {
+    a.phr[mu] = 1.f;
+    a.phi[mu] = 0.f;
+    if (g->theta[mu] != 0.0) {
+      a.twist_mask |= 1 << mu;
+      a.phr[mu] = (float)cos(g->theta[mu] / (double)g->L[mu]);
+      a.phi[mu] = (float)sin(g->theta[mu] / (double)g->L[mu]);
+    }
+  }
+  a.mp4 = (float)mp4;
+  a.tm = (float)(dag ? -tm : tm);
+  a.mp4s = mp4s;
+  a.tms = tms;
+  if (nact == 0) return true;
+  unsigned grid = (unsigned)((a.V + 3) / 4);
+  cudaStream_t s = stream();
+  int mt = (nact + 15) / 16;
+#define QG_MRHS(MT)                                                      \
+  if (dag) k_wilson_mrhs<true, MT><<<grid, 128, 0, s>>>(a);              \
+  else k_wilson_mrhs<false, MT><<<grid, 128, 0, s>>>(a);
+  switch (mt) {
+  case 1: QG_MRHS(1) break;
+  case 2: QG_MRHS(2) break;
+  case 3: QG_MRHS(3) break;
+  default: QG_MRHS(4) break;
+  }
+#undef QG_MRHS
+  return QG_LAUNCHED("wilson_mrhs");
+}
+
+}  // namespace qg
+
+extern "C" {
+
+int qcdgpu_mfield_create(qcdgpu_mfield *m, const int L[4], int nrhs)
+{
+  *m = qg::mfield_new(L, nrhs);
+  return *m ? 0 : 1;
+}
+int qcdgpu_mfield_destroy(qcdgpu_mfield m)
+{
+  qg::mfield_free(m);
+  return 0;
+}
+int qcdgpu_mfield_set(qcdgpu_mfield m, int r, qcdgpu_field f) { return qg::mfield_set(m, r, f) ? 0 : 1; }
+int qcdgpu_mfield_get(qcdgpu_field f, qcdgpu_mfield m, int r) { return qg::mfield_get(f, m, r) ? 0 : 1; }
+int qcdgpu_dslash_mrhs(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_gauge g, double kappa, double mu, int op,
+                       int nact)
+{
+  if (!(kappa > 0.0) || (op != QCDGPU_OP_D && op != QCDGPU_OP_DDAG)) {
+    qg::set_error("multi-RHS operator: kappa > 0 and op D or DDAG");
+    return 1;
+  }
+  return qg::dslash_mrhs(out, in, g, 1.0 / (2.0 * kappa), mu, op == QCDGPU_OP_DDAG, nact, nullptr, nullptr) ? 0 : 1;
+}
+
+}  // extern "C"

@@ -1,0 +1,509 @@
+// mrhs_cg.cu -- batched CG on the normal equations for many right-hand sides,
+// with continuous admission and retirement (the engine behind the serving
+// loop).
+//
+// A batch owns multi-RHS work fields (FP16, tensor-core operator) with a
+// fixed number of slots and runs the mixed-precision reliable-update CG of
+// cg.cu for all occupied slots at once: every inner iteration is two
+// multi-RHS operator launches plus four per-(site, RHS) kernels, with
+// per-slot scalars kept on the device. The operator's hopping term does not
+// depend on kappa or mu, so each slot carries its own diagonal and a batch
+// mixes requests of different kappa and twisted mass on one gauge field.
+// Between chunks of iterations the host reads the per-slot residual
+// histories, performs reliable updates (FP64 true residual per slot),
+// retires converged slots by moving the last occupied slot into their place,
+// and admits new right-hand sides into free slots -- while the others keep
+// iterating. Every reduction sums in a fixed order per slot, independent of
+// which other slots are occupied, so a right-hand side converges to the same
+// result alone and in any mix.
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
+#include "internal.h"
+
+struct qcdgpu_mfield_s {
+  int L[4];
+  int64_t V;
+  int N;
+  void *data;
+  float *norm;
+  size_t bytes;
+};
+
+namespace qg {
+
+using namespace qgd;
+
+qcdgpu_mfield mfield_new(const int L[4], int N);
+void mfield_free(qcdgpu_mfield m);
+bool mfield_set(qcdgpu_mfield m, int r, qcdgpu_field f);
+bool mfield_get(qcdgpu_field f, qcdgpu_mfield m, int r);
+bool dslash_mrhs(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_gauge g, double mp4, double tm, bool dag, int nact,
+                 const float *mp4s, const float *tms);
+
+struct MV {
+  __half2 *d;
+  float *n;
+  int V, N;
+};
+static MV mv(qcdgpu_mfield m) { return MV{(__half2 *)m->data, m->norm, (int)m->V, m->N}; }
+
+__device__ __forceinline__ void mv_load(const MV &m, int x, int r, float2 v[12])
+{
+  const float s = m.n[(int64_t)x * m.N + r];
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    float2 f = __half22float2(m.d[((int64_t)k * m.V + x) * m.N + r]);
+    v[k] = make_float2(f.x * s, f.y * s);
+  }
+}
+__device__ __forceinline__ void mv_store(const MV &m, int x, int r, const float2 v[12])
+{
+  float mx = 0.f;
+#pragma unroll
+  for (int k = 0; k < 12; k++) mx = fmaxf(mx, fmaxf(fabsf(v[k].x), fabsf(v[k].y)));
+  if (!(mx >= 1.17549435e-38f)) mx = 0.f;
+  const float inv = mx > 0.f ? 1.0f / mx : 0.f;
+#pragma unroll
+  for (int k = 0; k < 12; k++) m.d[((int64_t)k * m.V + x) * m.N + r] = __floats2half2_rn(v[k].x * inv, v[k].y * inv);
+  m.n[(int64_t)x * m.N + r] = mx;
+}
+
+// Launch shape of the per-(site, slot) kernels: block (N, SB) -- x = slot,
+// y = site within the block -- so a warp reads the slots of one site
+// contiguously; partials[block * N + slot] receives the block's sum for each
+// slot in a fixed order.
+static dim3 mblock(int N) { return dim3((unsigned)N, (unsigned)(256 / N > 0 ? 256 / N : 1)); }
+static unsigned mgrid(int V, int N) { return (unsigned)((V + mblock(N).y - 1) / mblock(N).y); }
+
+__device__ __forceinline__ void slot_partial(double v, double *partials)
+{
+  extern __shared__ double sh[];
+  const int N = blockDim.x, r = threadIdx.x, y = threadIdx.y;
+  sh[y * N + r] = v;
+  __syncthreads();
+  if (y == 0) {
+    double s = 0.0;
+    for (int i = 0; i < (int)blockDim.y; i++) s += sh[i * N + r];
+    partials[(int64_t)blockIdx.x * N + r] = s;
+  }
+}
+
+// partials <- Re <a_r, b_r> per slot
+__global__ void k_mdot(MV a, MV b, int nact, double *partials)
+{
+  const int r = threadIdx.x, x = blockIdx.x * blockDim.y + threadIdx.y;
+  double d = 0.0;
+  if (r < nact && x < a.V) {
+    float2 va[12], vb[12];
+    mv_load(a, x, r, va);
+    mv_load(b, x, r, vb);
+#pragma unroll
+    for (int k = 0; k < 12; k++) d += (double)va[k].x * vb[k].x + (double)va[k].y * vb[k].y;
+  }
+  slot_partial(d, partials);
+}
+
+// xs += alpha p ; rs -= alpha Ap ; partials <- |rs|^2 per slot
+__global__ void k_mupdate(MV xs, MV ps, MV rs, MV aps, int nact, const double *alpha, double *partials)
+{
+  const int r = threadIdx.x, x = blockIdx.x * blockDim.y + threadIdx.y;
+  double n2 = 0.0;
+  if (r < nact && x < xs.V) {
+    const float al = (float)alpha[r];
+    float2 a[12], b[12];
+    mv_load(xs, x, r, a);
+    mv_load(ps, x, r, b);
+#pragma unroll
+    for (int k = 0; k < 12; k++) a[k] = make_float2(__fmaf_rn(al, b[k].x, a[k].x), __fmaf_rn(al, b[k].y, a[k].y));
+    mv_store(xs, x, r, a);
+    mv_load(rs, x, r, a);
+    mv_load(aps, x, r, b);
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      a[k] = make_float2(__fmaf_rn(-al, b[k].x, a[k].x), __fmaf_rn(-al, b[k].y, a[k].y));
+      n2 += (double)a[k].x * a[k].x + (double)a[k].y * a[k].y;
+    }
+    mv_store(rs, x, r, a);
+  }
+  slot_partial(n2, partials);
+}
+
+// ps = rs + beta ps
+__global__ void k_mp(MV ps, MV rs, int nact, const double *beta)
+{
+  const int r = threadIdx.x, x = blockIdx.x * blockDim.y + threadIdx.y;
+  if (r >= nact || x >= ps.V) return;
+  const float be = (float)beta[r];
+  float2 p[12], q[12];
+  mv_load(ps, x, r, p);
+  mv_load(rs, x, r, q);
+#pragma unroll
+  for (int k = 0; k < 12; k++) p[k] = make_float2(__fmaf_rn(be, p[k].x, q[k].x), __fmaf_rn(be, p[k].y, q[k].y));
+  mv_store(ps, x, r, p);
+}
+
+// slot `to` <- slot `from` (zero == 1: slot `to` <- 0)
+__global__ void k_mcopy(MV m, int from, int to, int zero)
+{
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= m.V) return;
+#pragma unroll
+  for (int k = 0; k < 12; k++)
+    m.d[((int64_t)k * m.V + x) * m.N + to] = zero ? __floats2half2_rn(0.f, 0.f) : m.d[((int64_t)k * m.V + x) * m.N + from];
+  m.n[(int64_t)x * m.N + to] = zero ? 0.f : m.n[(int64_t)x * m.N + from];
+}
+
+// scalar layout, per slot r of N: rr, pAp, alpha, beta, then history[j]
+enum { M_RR = 0, M_PAP = 1, M_ALPHA = 2, M_BETA = 3, M_HIST = 4 };
+constexpr int kMChunk = 16;
+
+// block r sums the partials of slot r over nb blocks in a fixed order
+__global__ void k_mscalars(const double *partials, int nb, int N, double *s, int mode, int hist)
+{
+  const int r = blockIdx.x;
+  double v = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) v += partials[(int64_t)b * N + r];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __shared__ double sh[32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) t += sh[i];
+    if (mode == 0) {
+      s[M_PAP * N + r] = t;
+      s[M_ALPHA * N + r] = t > 0.0 ? s[M_RR * N + r] / t : nan("");
+    } else {
+      s[M_BETA * N + r] = t / s[M_RR * N + r];
+      s[M_RR * N + r] = t;
+      s[(M_HIST + hist) * N + r] = t;
+    }
+  }
+}
+
+}  // namespace qg
+
+// ----------------------------------------------------------------- engine
+namespace qg {
+
+struct BSlot {
+  int tag;
+  qcdgpu_field x, b;  // caller's FP64 fields
+  int op;             // QCDGPU_OP_D or QCDGPU_OP_Q
+  double mp4, tm, bn, tol, delta, maxr, hint, true_res;
+  int iters, maxiter, updates, since;
+};
+
+struct BDone {
+  int tag, status, iters, updates;
+  double true_res;
+};
+
+}  // namespace qg
+
+struct qcdgpu_batch_s {
+  qcdgpu_gauge g;
+  int cap, nact;
+  qcdgpu_mfield rs, xs, ps, t, aps;
+  qcdgpu_field rt, r, up, bd;  // FP64 work shared by the slots' reliable updates
+  double *s;                   // device scalars, (M_HIST + kMChunk) * cap
+  float *mp4s, *tms;           // device per-slot diagonal
+  double *part;                // device partials
+  double *hs;                  // pinned host copy of the scalars
+  std::vector<qg::BSlot> slots;
+  std::vector<qg::BDone> done;
+  bool first;                  // no p update before the next iteration
+};
+
+namespace qg {
+
+static void batch_free(qcdgpu_batch b)
+{
+  if (!b) return;
+  for (auto m : {b->rs, b->xs, b->ps, b->t, b->aps}) mfield_free(m);
+  for (auto f : {b->rt, b->r, b->up, b->bd}) field_free(f);
+  cudaFree(b->s);
+  cudaFree(b->mp4s);
+  cudaFree(b->tms);
+  cudaFree(b->part);
+  cudaFreeHost(b->hs);
+  delete b;
+}
+
+static qcdgpu_batch batch_new(qcdgpu_gauge g, int cap)
+{
+  if (!g || g->prec != QCDGPU_F64 || cap < 1 || cap > 64) {
+    set_error("batch: FP64 gauge field and 1..64 slots required");
+    return nullptr;
+  }
+  auto *b = new qcdgpu_batch_s();
+  b->g = g;
+  b->cap = cap;
+  b->nact = 0;
+  b->first = true;
+  b->rs = mfield_new(g->L, cap);
+  b->xs = mfield_new(g->L, cap);
+  b->ps = mfield_new(g->L, cap);
+  b->t = mfield_new(g->L, cap);
+  b->aps = mfield_new(g->L, cap);
+  b->rt = field_new(g->L, QCDGPU_F64);
+  b->r = field_new(g->L, QCDGPU_F64);
+  b->up = field_new(g->L, QCDGPU_F64);
+  b->bd = field_new(g->L, QCDGPU_F64);
+  size_t ns = (size_t)(M_HIST + kMChunk) * cap;
+  unsigned nb = mgrid((int)g->V, cap);
+  bool ok = b->rs && b->xs && b->ps && b->t && b->aps && b->rt && b->r && b->up && b->bd &&
+            QG_CUDA(cudaMalloc(&b->s, ns * sizeof(double))) && QG_CUDA(cudaMalloc(&b->mp4s, cap * sizeof(float))) &&
+            QG_CUDA(cudaMalloc(&b->tms, cap * sizeof(float))) &&
+            QG_CUDA(cudaMalloc(&b->part, (size_t)nb * cap * sizeof(double))) &&
+            QG_CUDA(cudaMallocHost(&b->hs, ns * sizeof(double)));
+  if (!ok) {
+    batch_free(b);
+    return nullptr;
+  }
+  return b;
+}
+
+// bd = b as seen by D (Q x = b  <=>  D x = -i g5 b)
+static bool slot_bd(qcdgpu_batch B, const BSlot &sl)
+{
+  if (sl.op == QCDGPU_OP_Q) return blas_ig5(B->bd, sl.b) && blas_axpby(B->bd, -1.0, 0.0, B->bd, 0.0, 0.0, B->bd);
+  return blas_copy(B->bd, sl.b);
+}
+
+// rt = bd - D x (FP64), r = D^+ rt; slot k of rs <- r; returns |rt| / |b| and |r|^2
+static bool slot_residual(qcdgpu_batch B, int k, const BSlot &sl, double *rel, double *rr)
+{
+  if (!slot_bd(B, sl)) return false;
+  if (!dslash(B->rt, sl.x, B->g, sl.mp4, sl.tm, QCDGPU_OP_D, -1)) return false;
+  if (!blas_axpby(B->rt, 1.0, 0.0, B->bd, -1.0, 0.0, B->rt)) return false;
+  double n2;
+  if (!blas_norm2(B->rt, &n2)) return false;
+  *rel = sl.bn > 0 ? sqrt(n2) / sl.bn : 0.0;
+  if (!dslash(B->r, B->rt, B->g, sl.mp4, sl.tm, QCDGPU_OP_DDAG, -1)) return false;
+  if (!blas_norm2(B->r, rr)) return false;
+  return mfield_set(B->rs, k, B->r);
+}
+
+static bool set_scalar(qcdgpu_batch B, int slot_kind, int k, double v)
+{
+  B->hs[0] = v;
+  return QG_CUDA(cudaMemcpyAsync(B->s + slot_kind * B->cap + k, B->hs, sizeof(double), cudaMemcpyHostToDevice,
+                                 stream())) &&
+         QG_CUDA(cudaStreamSynchronize(stream()));
+}
+
+static bool copy_slot(qcdgpu_batch B, int from, int to)
+{
+  unsigned g = (unsigned)((B->g->V + 127) / 128);
+  for (auto m : {B->rs, B->xs, B->ps}) {
+    k_mcopy<<<g, 128, 0, stream()>>>(mv(m), from, to, 0);
+    if (!QG_LAUNCHED("mrhs_copy_slot")) return false;
+  }
+  return QG_CUDA(cudaMemcpyAsync(B->mp4s + to, B->mp4s + from, sizeof(float), cudaMemcpyDeviceToDevice, stream())) &&
+         QG_CUDA(cudaMemcpyAsync(B->tms + to, B->tms + from, sizeof(float), cudaMemcpyDeviceToDevice, stream()));
+}
+
+int batch_add(qcdgpu_batch B, qcdgpu_field x, qcdgpu_field b, double kappa, double mu, int op, double tol,
+              int maxiter, double delta, int tag)
+{
+  if (!x || !b || x->prec != QCDGPU_F64 || b->prec != QCDGPU_F64 || !same_shape(x, B->rt) ||
+      !same_shape(b, B->rt) || x == b || !(kappa > 0.0) || (op != QCDGPU_OP_D && op != QCDGPU_OP_Q)) {
+    set_error("batch add: FP64 x, b on the batch's lattice, kappa > 0, op D or Q");
+    return -2;
+  }
+  if (B->nact >= B->cap) return -1;
+  BSlot sl;
+  sl.tag = tag;
+  sl.x = x;
+  sl.b = b;
+  sl.op = op;
+  sl.mp4 = 1.0 / (2.0 * kappa);
+  sl.tm = mu;
+  sl.tol = tol;
+  sl.delta = delta > 0 ? delta : 0.1;
+  sl.iters = 0;
+  sl.updates = 0;
+  sl.since = 0;
+  sl.maxiter = maxiter > 0 ? maxiter : 100000;
+  double bn2;
+  if (!blas_norm2(b, &bn2) || !blas_zero(x)) return -2;
+  sl.bn = sqrt(bn2);
+  const int k = B->nact;
+  double rel, rr;
+  if (!slot_residual(B, k, sl, &rel, &rr)) return -2;
+  sl.true_res = rel;
+  sl.maxr = sqrt(rr);
+  sl.hint = tol * sl.maxr;
+  unsigned g = (unsigned)((B->g->V + 127) / 128);
+  k_mcopy<<<g, 128, 0, stream()>>>(mv(B->xs), 0, k, 1);
+  if (!QG_LAUNCHED("mrhs_zero_slot")) return -2;
+  if (!mfield_set(B->ps, k, B->r)) return -2;
+  float mp = (float)sl.mp4, tmf = (float)mu;
+  if (!QG_CUDA(cudaMemcpyAsync(B->mp4s + k, &mp, sizeof(float), cudaMemcpyHostToDevice, stream())) ||
+      !QG_CUDA(cudaMemcpyAsync(B->tms + k, &tmf, sizeof(float), cudaMemcpyHostToDevice, stream())))
+    return -2;
+  // a fresh slot starts with beta = 0, so the shared p update leaves p = r
+  if (!set_scalar(B, M_RR, k, rr) || !set_scalar(B, M_BETA, k, 0.0)) return -2;
+  if (bn2 == 0.0 || rel <= tol) {
+    B->done.push_back(BDone{tag, 0, 0, 0, rel});
+    return k;
+  }
+  B->slots.push_back(sl);
+  B->nact++;
+  return k;
+}
+
+// retire slot k: the last occupied slot moves into it
+static bool retire(qcdgpu_batch B, int k, int status)
+{
+  BSlot &sl = B->slots[(size_t)k];
+  B->done.push_back(BDone{sl.tag, status, sl.iters, sl.updates, sl.true_res});
+  const int last = B->nact - 1;
+  if (k != last) {
+    if (!copy_slot(B, last, k)) return false;
+    // scalars of the moved slot
+    if (!QG_CUDA(cudaMemcpyAsync(B->hs, B->s, sizeof(double) * (M_HIST + kMChunk) * B->cap, cudaMemcpyDeviceToHost,
+                                 stream())) ||
+        !QG_CUDA(cudaStreamSynchronize(stream())))
+      return false;
+    for (int q = 0; q < M_HIST + kMChunk; q++) B->hs[q * B->cap + k] = B->hs[q * B->cap + last];
+    if (!QG_CUDA(cudaMemcpyAsync(B->s, B->hs, sizeof(double) * (M_HIST + kMChunk) * B->cap, cudaMemcpyHostToDevice,
+                                 stream())))
+      return false;
+    B->slots[(size_t)k] = B->slots[(size_t)last];
+  }
+  B->slots.pop_back();
+  B->nact--;
+  return QG_CUDA(cudaStreamSynchronize(stream()));
+}
+
+// run up to `iters` iterations (a multiple of the chunk), with reliable
+// updates and retirement at chunk boundaries; returns 0 or 3 on error
+int batch_step(qcdgpu_batch B, int iters)
+{
+  const int cap = B->cap;
+  const int V = (int)B->g->V;
+  const dim3 blk = mblock(cap);
+  const unsigned nb = mgrid(V, cap);
+  const size_t shm = sizeof(double) * blk.x * blk.y;
+  cudaStream_t st = stream();
+  for (int done_it = 0; done_it < iters && B->nact > 0; done_it += kMChunk) {
+    const int n = B->nact;
+    for (int j = 0; j < kMChunk; j++) {
+      // p = r + beta p (beta = 0 keeps a fresh slot's p = r)
+      k_mp<<<nb, blk, 0, st>>>(mv(B->ps), mv(B->rs), n, B->s + M_BETA * cap);
+      if (!QG_LAUNCHED("mrhs_p")) return 3;
+      if (!dslash_mrhs(B->t, B->ps, B->g, 4.0, 0.0, false, n, B->mp4s, B->tms)) return 3;
+      if (!dslash_mrhs(B->aps, B->t, B->g, 4.0, 0.0, true, n, B->mp4s, B->tms)) return 3;
+      k_mdot<<<nb, blk, shm, st>>>(mv(B->ps), mv(B->aps), n, B->part);
+      if (!QG_LAUNCHED("mrhs_dot")) return 3;
+      k_mscalars<<<n, 256, 0, st>>>(B->part, (int)nb, cap, B->s, 0, j);
+      if (!QG_LAUNCHED("mrhs_scalars")) return 3;
+      k_mupdate<<<nb, blk, shm, st>>>(mv(B->xs), mv(B->ps), mv(B->rs), mv(B->aps), n, B->s + M_ALPHA * cap, B->part);
+      if (!QG_LAUNCHED("mrhs_update")) return 3;
+      k_mscalars<<<n, 256, 0, st>>>(B->part, (int)nb, cap, B->s, 1, j);
+      if (!QG_LAUNCHED("mrhs_scalars")) return 3;
+    }
+    if (!QG_CUDA(cudaMemcpyAsync(B->hs, B->s, sizeof(double) * (M_HIST + kMChunk) * cap, cudaMemcpyDeviceToHost, st)) ||
+        !QG_CUDA(cudaStreamSynchronize(st)))
+      return 3;
+    std::vector<double> rr_iter(n), beta_iter(n);
+    std::vector<int> need(n, 0), fail(n, 0);
+    for (int k = 0; k < n; k++) {
+      BSlot &sl = B->slots[(size_t)k];
+      rr_iter[k] = B->hs[M_RR * cap + k];
+      beta_iter[k] = B->hs[M_BETA * cap + k];
+      bool update = false, hinted = false;
+      for (int j = 0; j < kMChunk; j++) {
+        double rn = sqrt(B->hs[(M_HIST + j) * cap + k]);
+        if (!(rn == rn)) {
+          fail[k] = 1;
+          break;
+        }
+        sl.iters++;
+        sl.since++;
+        if (rn <= sl.hint) hinted = true;
+        if (rn < sl.delta * sl.maxr) update = true;
+        if (!update && rn > sl.maxr) sl.maxr = rn;
+      }
+      need[k] = fail[k] || update || hinted || sl.iters >= sl.maxiter;
+      if (hinted) sl.hint *= 0.3;
+    }
+    // reliable updates, then retirement from the highest slot down
+    std::vector<int> retire_status(n, -1);
+    for (int k = 0; k < n; k++) {
+      if (!need[k]) continue;
+      BSlot &sl = B->slots[(size_t)k];
+      if (!mfield_get(B->up, B->xs, k) || !blas_axpby(sl.x, 1.0, 0.0, B->up, 1.0, 0.0, sl.x)) return 3;
+      k_mcopy<<<(unsigned)((V + 127) / 128), 128, 0, st>>>(mv(B->xs), 0, k, 1);
+      if (!QG_LAUNCHED("mrhs_zero_slot")) return 3;
+      double rel, rr;
+      if (!slot_residual(B, k, sl, &rel, &rr)) return 3;
+      sl.true_res = rel;
+      sl.updates++;
+      sl.since = 0;
+      if (rel <= sl.tol) {
+        retire_status[k] = 0;
+      } else if (fail[k]) {
+        retire_status[k] = 2;
+      } else if (sl.iters >= sl.maxiter) {
+        retire_status[k] = 1;
+      } else {
+        double bnew = (beta_iter[k] > 0.0 && rr_iter[k] > 0.0) ? rr * beta_iter[k] / rr_iter[k] : 0.0;
+        if (!set_scalar(B, M_RR, k, rr) || !set_scalar(B, M_BETA, k, bnew)) return 3;
+        sl.maxr = sqrt(rr);
+      }
+    }
+    for (int k = n - 1; k >= 0; k--)
+      if (retire_status[k] >= 0 && !retire(B, k, retire_status[k])) return 3;
+  }
+  return 0;
+}
+
+}  // namespace qg
+
+extern "C" {
+
+int qcdgpu_batch_create(qcdgpu_batch *b, qcdgpu_gauge g, int capacity)
+{
+  *b = qg::batch_new(g, capacity);
+  return *b ? 0 : 1;
+}
+int qcdgpu_batch_destroy(qcdgpu_batch b)
+{
+  qg::batch_free(b);
+  return 0;
+}
+int qcdgpu_batch_add(qcdgpu_batch b, qcdgpu_field x, qcdgpu_field rhs, double kappa, double mu, int op, double tol,
+                     int maxiter, double delta, int tag)
+{
+  return qg::batch_add(b, x, rhs, kappa, mu, op, tol, maxiter, delta, tag);
+}
+int qcdgpu_batch_step(qcdgpu_batch b, int iterations) { return qg::batch_step(b, iterations); }
+int qcdgpu_batch_active(qcdgpu_batch b) { return b ? b->nact : 0; }
+int qcdgpu_batch_free_slots(qcdgpu_batch b) { return b ? b->cap - b->nact : 0; }
+int qcdgpu_batch_poll(qcdgpu_batch b, int *tags, int *status, int *iters, double *true_residual, int max)
+{
+  int n = 0;
+  while (n < max && !b->done.empty()) {
+    qg::BDone d = b->done.front();
+    b->done.erase(b->done.begin());
+    tags[n] = d.tag;
+    status[n] = d.status;
+    iters[n] = d.iters;
+    true_residual[n] = d.true_res;
+    n++;
+  }
+  return n;
+}
+size_t qcdgpu_batch_bytes(qcdgpu_batch b)
+{
+  if (!b) return 0;
+  return 5 * b->rs->bytes + 4 * b->rt->bytes;
+}
+
+}  // extern "C"

@@ -111,7 +111,7 @@ qcdgpu_gauge gauge_new(const int L[4], const double theta[4], int prec, int reco
   g->prec = prec;
   g->recon = recon;
   size_t reals = (size_t)4 * recon;
-  size_t esz = prec == QCDGPU_F64 ? 8 : prec == QCDGPU_F32 ? 4 : 2;
+  size_t esz = (prec == QCDGPU_F64 || prec == kGaugeFF) ? 8 : prec == QCDGPU_F32 ? 4 : 2;
   g->bytes = reals * esz * (size_t)g->stride;
   if (!QG_CUDA(cudaMalloc(&g->data, g->bytes))) {
     delete g;
@@ -177,10 +177,30 @@ double *reduce_scratch()
   return g_scratch;
 }
 
+// per-block partial sums of launches with one block per 128 sites; grows
+// (outside any timed loop: solvers call it before iterating)
+static double *g_big = nullptr;
+static int64_t g_big_n = 0;
+
+double *big_partials(int64_t n)
+{
+  if (n > g_big_n) {
+    if (g_big) {
+      cudaStreamSynchronize(g_stream);
+      cudaFree(g_big);
+    }
+    g_big = nullptr;
+    g_big_n = 0;
+    if (!QG_CUDA(cudaMalloc(&g_big, sizeof(double) * (size_t)n))) return nullptr;
+    g_big_n = n;
+  }
+  return g_big;
+}
+
 double *host_result()
 {
   if (!g_host_res) {
-    if (!QG_CUDA(cudaMallocHost(&g_host_res, sizeof(double) * 16))) return nullptr;
+    if (!QG_CUDA(cudaMallocHost(&g_host_res, sizeof(double) * 64))) return nullptr;
   }
   return g_host_res;
 }

@@ -82,9 +82,10 @@ qcdgpu_gauge gauge_at(qcdgpu_gauge g, int prec)
   if (g->prec == prec) return g;
   auto it = g_low.find({g, prec});
   if (it != g_low.end()) return it->second;
-  qcdgpu_gauge lo = gauge_new(g->L, g->theta, prec, 18);
+  const bool full32 = prec == kGaugeF32Full;
+  qcdgpu_gauge lo = gauge_new(g->L, g->theta, full32 ? QCDGPU_F32 : prec, 18);
   if (!lo) return nullptr;
-  if (!convert_gauge(lo, g)) {
+  if (!convert_gauge(lo, g, full32 ? 18 : 0)) {
     gauge_free(lo);
     return nullptr;
   }
@@ -291,105 +292,9 @@ static int solve_bicgstab(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double
   return 1;
 }
 
-// --------------------------------------------------------------- CGNR
-static int solve_cgnr(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, double tm,
-                      qcdgpu_solve_params *p)
-{
-  Work w;
-  const int prec = p->inner_prec;
-  qcdgpu_gauge gi = gauge_at(g, prec);
-  qcdgpu_field rt = w.get(b->L, QCDGPU_F64);  // true residual b - D x
-  qcdgpu_field r = w.get(b->L, QCDGPU_F64);   // normal residual D^+ rt
-  qcdgpu_field rs = prec == QCDGPU_F64 ? r : w.get(b->L, prec);
-  qcdgpu_field xs = w.get(b->L, prec), ps = w.get(b->L, prec), aps = w.get(b->L, prec);
-  qcdgpu_field up = prec == QCDGPU_F64 ? nullptr : w.get(b->L, QCDGPU_F64);
-  if (!gi || !rt || !r || !rs || !xs || !ps || !aps || (prec != QCDGPU_F64 && !up)) return 3;
-  // the system matrix is D (op D) or Q = i g5 D (op Q); Q^+ Q = D^+ D, and
-  // Q^+ b = D^+ (-i g5) b, so both use the D^+ D iteration with a rotated b.
-  double bn;
-  if (!norm(b, &bn)) return 3;
-  p->iters = 0;
-  p->reliable_updates = 0;
-  p->true_residual = 1.0;
-  if (!blas_zero(x)) return 3;
-  if (bn == 0.0) {
-    p->true_residual = 0.0;
-    return 0;
-  }
-  // rt = b (as seen by D): for Q, D x = -i g5 b
-  qcdgpu_field bd = b;
-  qcdgpu_field brot = nullptr;
-  if (p->op == QCDGPU_OP_Q) {
-    brot = w.get(b->L, QCDGPU_F64);
-    if (!brot) return 3;
-    // -i g5 b = - (i g5 b)
-    if (!blas_ig5(brot, b) || !scale(brot, -1.0)) return 3;
-    bd = brot;
-  }
-  if (!blas_copy(rt, bd)) return 3;
-  if (!dslash(r, rt, g, mp4, tm, QCDGPU_OP_DDAG, -1)) return 3;
-  double rr;
-  if (!blas_norm2(r, &rr)) return 3;
-  if (prec != QCDGPU_F64 && !convert_field(rs, r)) return 3;
-  if (!blas_copy(ps, rs) || !blas_zero(xs)) return 3;
-  double maxr = sqrt(rr);
-  double hint = p->tol * maxr;  // check convergence once |D^+ r| <= tol |D^+ b|
-  const double delta = p->delta > 0 ? p->delta : 0.1;
-  while (true) {
-    if (!dslash(aps, ps, gi, mp4, tm, QCDGPU_OP_DDAGD, -1)) return 3;
-    double pap[2];
-    if (!blas_dot(ps, aps, pap)) return 3;
-    if (!(pap[0] > 0)) return 2;
-    double alpha = rr / pap[0];
-    if (!blas_axpby(xs, alpha, 0.0, ps, 1.0, 0.0, xs)) return 3;
-    double *dres = reduce_scratch() + 2 * kMaxPartials + 8;
-    double rr_new;
-    if (!blas_axpy_norm2_dev(rs, -alpha, 0.0, aps, dres)) return 3;
-    {
-      double *h = host_result();
-      if (!QG_CUDA(cudaMemcpyAsync(h, dres, sizeof(double), cudaMemcpyDeviceToHost, stream())) ||
-          !QG_CUDA(cudaStreamSynchronize(stream())))
-        return 3;
-      rr_new = h[0];
-    }
-    p->iters++;
-    double rn = sqrt(rr_new);
-    bool last = p->iters >= p->maxiter;
-    // update when the iterated residual fell by delta (low precision), every
-    // 25 iterations (FP64), or when it suggests convergence
-    bool hinted = rn <= hint;
-    bool do_update = last || hinted ||
-                     (prec != QCDGPU_F64 ? rn < delta * maxr : p->iters % 25 == 0);
-    {
-      if (do_update) {
-        // accumulate the low-precision increment into x and recompute the
-        // residual with the FP64 operator
-        if (prec == QCDGPU_F64) {
-          if (!blas_axpby(x, 1.0, 0.0, xs, 1.0, 0.0, x) || !blas_zero(xs)) return 3;
-        } else {
-          if (!convert_field(up, xs) || !blas_axpby(x, 1.0, 0.0, up, 1.0, 0.0, x) || !blas_zero(xs)) return 3;
-        }
-        double rel;
-        if (!true_residual(rt, x, bd, g, mp4, tm, QCDGPU_OP_D, bn, &rel)) return 3;
-        p->true_residual = rel;
-        p->reliable_updates++;
-        if (rel <= p->tol) return 0;
-        if (last) return 1;
-        if (hinted) hint = rn * 0.3;
-        if (!dslash(r, rt, g, mp4, tm, QCDGPU_OP_DDAG, -1)) return 3;
-        if (!blas_norm2(r, &rr_new)) return 3;
-        if (prec != QCDGPU_F64 && !convert_field(rs, r)) return 3;
-        maxr = sqrt(rr_new);
-      } else if (rn > maxr) {
-        maxr = rn;
-      }
-    }
-    double beta = rr_new / rr;
-    rr = rr_new;
-    // ps = rs + beta ps
-    if (!blas_axpby(ps, 1.0, 0.0, rs, beta, 0.0, ps)) return 3;
-  }
-}
+// CGNR with device-resident scalars: cg.cu
+int solve_cgnr_engine(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, double tm,
+                      qcdgpu_solve_params *p);
 
 // -------------------------------------------------- GCR with refinement
 static int solve_gcr(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, double tm,
@@ -447,7 +352,7 @@ int solve(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, double tm,
   switch (p->solver) {
   case QCDGPU_SOLVER_GCR: st = solve_gcr(x, b, g, mp4, tm, p); break;
   case QCDGPU_SOLVER_BICGSTAB: st = solve_bicgstab(x, b, g, mp4, tm, p); break;
-  case QCDGPU_SOLVER_CGNR: st = solve_cgnr(x, b, g, mp4, tm, p); break;
+  case QCDGPU_SOLVER_CGNR: st = solve_cgnr_engine(x, b, g, mp4, tm, p); break;
   default: set_error("solve: unknown solver %d", p->solver); st = 3;
   }
   p->status = st;

@@ -110,31 +110,38 @@ template <bool DAG, int SP, int GP, int RECON, typename R>
 __global__ void __launch_bounds__(128) k_wilson(const DArgs a)
 {
   int x = (int)(blockIdx.x * blockDim.x + threadIdx.x);
-  if (x >= a.V) return;
-  int c[4];
-  coords(a.geo, x, c);
-  C<R> acc[12];
+  double n2 = 0.0;
+  if (x < a.V) {
+    int c[4];
+    coords(a.geo, x, c);
+    C<R> acc[12];
+    const R zero = Scalar<R>::get(0.0, 0.0f, 0.0f);
 #pragma unroll
-  const R zero = Scalar<R>::get(0.0, 0.0f, 0.0f);
-  for (int k = 0; k < 12; k++) acc[k] = C<R>{zero, zero};
-  hop_pair<0, DAG, SP, GP, RECON, R>(a, x, c, acc);
-  hop_pair<1, DAG, SP, GP, RECON, R>(a, x, c, acc);
-  hop_pair<2, DAG, SP, GP, RECON, R>(a, x, c, acc);
-  hop_pair<3, DAG, SP, GP, RECON, R>(a, x, c, acc);
-  C<R> s[12];
-  Spinor<SP, R>::load(a.in, a.in_norm, a.stride, x, s);
-  const R mp4 = Scalar<R>::get(a.mp4, a.mp4_h, a.mp4_l), tm = Scalar<R>::get(a.tm, a.tm_h, a.tm_l);
-  const R half = Scalar<R>::get(0.5, 0.5f, 0.0f);
+    for (int k = 0; k < 12; k++) acc[k] = C<R>{zero, zero};
+    hop_pair<0, DAG, SP, GP, RECON, R>(a, x, c, acc);
+    hop_pair<1, DAG, SP, GP, RECON, R>(a, x, c, acc);
+    hop_pair<2, DAG, SP, GP, RECON, R>(a, x, c, acc);
+    hop_pair<3, DAG, SP, GP, RECON, R>(a, x, c, acc);
+    C<R> s[12];
+    Spinor<SP, R>::load(a.in, a.in_norm, a.stride, x, s);
+    const R mp4 = Scalar<R>::get(a.mp4, a.mp4_h, a.mp4_l), tm = Scalar<R>::get(a.tm, a.tm_h, a.tm_l);
+    const R half = Scalar<R>::get(0.5, 0.5f, 0.0f);
 #pragma unroll
-  for (int k = 0; k < 12; k++) {
-    // (m+4) s + i tm g5 s - acc/2 ; g5 = +1 for spins 0,1, -1 for spins 2,3
-    R g5tm = k < 6 ? tm : -tm;
-    C<R> d{mp4 * s[k].re - g5tm * s[k].im, mp4 * s[k].im + g5tm * s[k].re};
-    d = d - half * acc[k];
-    if (a.op_q) d = k < 6 ? mul_i(d) : -mul_i(d);
-    acc[k] = d;
+    for (int k = 0; k < 12; k++) {
+      // (m+4) s + i tm g5 s - acc/2 ; g5 = +1 for spins 0,1, -1 for spins 2,3
+      R g5tm = k < 6 ? tm : -tm;
+      C<R> d{mp4 * s[k].re - g5tm * s[k].im, mp4 * s[k].im + g5tm * s[k].re};
+      d = d - half * acc[k];
+      if (a.op_q) d = k < 6 ? mul_i(d) : -mul_i(d);
+      acc[k] = d;
+    }
+    Spinor<SP, R>::store(a.out, a.out_norm, a.stride, x, acc);
+    if (a.partials) {
+#pragma unroll
+      for (int k = 0; k < 12; k++) n2 += (double)acc[k].re * (double)acc[k].re + (double)acc[k].im * (double)acc[k].im;
+    }
   }
-  Spinor<SP, R>::store(a.out, a.out_norm, a.stride, x, acc);
+  if (a.partials) block_partial(n2, a.partials);
 }
 
 }  // namespace qg

@@ -1,0 +1,130 @@
+"""Batched multi-RHS solver with continuous admission (qcdgpu_batch).
+
+Every right-hand side is checked by its FP64 true residual computed by the
+oracle, so the bar is the same as for the single-RHS solvers: |b - op x| / |b|
+<= tol for each request, whatever it was batched with."""
+import numpy as np
+import pytest
+
+import qcd_gb300 as q
+from tests.conftest import EPS_PLAQ_060
+
+pytestmark = pytest.mark.gpu
+L = (16, 8, 8, 8)
+TH = (np.pi, 0.0, 0.0, 0.0)
+
+
+def _run(batch, pending, max_steps=4000):
+    """Feed (tag, x, b, kappa, mu, op, tol) requests as slots free up; returns {tag: (status, iters, res)}."""
+    out = {}
+    queue = list(pending)
+    for _ in range(max_steps):
+        while queue and batch.free_slots > 0:
+            tag, fx, fb, kappa, mu, op, tol = queue.pop(0)
+            k = batch.add(fx, fb, kappa, mu, op, tol=tol, maxiter=20000, tag=tag)
+            assert k >= 0
+        for tag, st, it, res in batch.poll():
+            out[tag] = (st, it, res)
+        if not queue and batch.active == 0:
+            break
+        batch.step(16)
+    for tag, st, it, res in batch.poll():
+        out[tag] = (st, it, res)
+    return out
+
+
+def test_batch_mixed_kappa_mu_op_each_converges(gpu, orc):
+    u = orc.gauge_synthetic(L, 11, EPS_PLAQ_060)
+    g = q.Gauge(L, TH).load(u)
+    params = [(0.15, 0.0, q.OP_D, 1e-10), (0.14, 0.02, q.OP_D, 1e-10), (0.155, 0.0, q.OP_D, 1e-8),
+              (0.145, 0.01, q.OP_Q, 1e-10), (0.15, 0.0, q.OP_Q, 1e-9), (0.12, 0.0, q.OP_D, 1e-10)]
+    reqs, fields, srcs = [], [], []
+    for i, (kappa, mu, op, tol) in enumerate(params):
+        b = orc.gaussian_spinor(L, 300 + i)
+        fb, fx = q.Field(L).load(b), q.Field(L)
+        srcs.append(b)
+        fields += [fb, fx]
+        reqs.append((i, fx, fb, kappa, mu, op, tol))
+    batch = q.Batch(g, 8)
+    res = _run(batch, reqs)
+    assert sorted(res) == list(range(len(params)))
+    for i, (kappa, mu, op, tol) in enumerate(params):
+        st, it, tr = res[i]
+        assert st == 0, (i, res[i])
+        x = reqs[i][1].store()
+        true = orc.true_residual(x, srcs[i], u, L, TH, kappa, mu, op="Q" if op == q.OP_Q else "D")
+        assert true <= tol, (i, true, tol)
+        assert abs(true - tr) <= 1e-3 * tol + 1e-15
+    batch.close()
+    for f in fields + [g]:
+        f.close()
+
+
+def test_batch_continuous_admission_more_requests_than_slots(gpu, orc):
+    u = orc.gauge_synthetic(L, 12, EPS_PLAQ_060)
+    g = q.Gauge(L, TH).load(u)
+    n = 9
+    reqs, fields, srcs = [], [], []
+    for i in range(n):
+        b = orc.gaussian_spinor(L, 400 + i) * (10.0 ** (i % 3 - 1))
+        fb, fx = q.Field(L).load(b), q.Field(L)
+        srcs.append(b)
+        fields += [fb, fx]
+        kappa = 0.13 + 0.0025 * i
+        reqs.append((i, fx, fb, kappa, 0.0, q.OP_D, 1e-10))
+    batch = q.Batch(g, 3)
+    res = _run(batch, reqs)
+    assert sorted(res) == list(range(n))
+    for i in range(n):
+        assert res[i][0] == 0, (i, res[i])
+        x = reqs[i][1].store()
+        assert orc.true_residual(x, srcs[i], u, L, TH, reqs[i][3]) <= 1e-10
+    batch.close()
+    for f in fields + [g]:
+        f.close()
+
+
+def test_batch_result_independent_of_the_mix(gpu, orc):
+    """Per-slot reductions sum in a fixed order and the tensor-core product of
+    one RHS row does not involve the others, so a request solved alone and in
+    a mix (same capacity) gives bit-identical solutions."""
+    u = orc.gauge_synthetic(L, 13, EPS_PLAQ_060)
+    g = q.Gauge(L, TH).load(u)
+    b = orc.gaussian_spinor(L, 500)
+    fb, fx_alone = q.Field(L).load(b), q.Field(L)
+    batch = q.Batch(g, 4)
+    _run(batch, [(0, fx_alone, fb, 0.15, 0.01, q.OP_D, 1e-10)])
+    others = []
+    reqs = []
+    for i in range(3):
+        ob = q.Field(L).load(orc.gaussian_spinor(L, 600 + i))
+        ox = q.Field(L)
+        others += [ob, ox]
+        reqs.append((10 + i, ox, ob, 0.14 + 0.005 * i, 0.0, q.OP_D, 1e-10))
+    fx_mix = q.Field(L)
+    # the request under test enters the last slot, behind three others
+    res = _run(batch, reqs + [(0, fx_mix, fb, 0.15, 0.01, q.OP_D, 1e-10)])
+    assert res[0][0] == 0
+    assert np.array_equal(fx_alone.store(), fx_mix.store())
+    batch.close()
+    for f in others + [fb, fx_alone, fx_mix, g]:
+        f.close()
+
+
+def test_batch_full_and_zero_rhs(gpu, orc):
+    u = orc.gauge_synthetic(L, 14, EPS_PLAQ_060)
+    g = q.Gauge(L, TH).load(u)
+    batch = q.Batch(g, 1)
+    fb = q.Field(L).load(orc.gaussian_spinor(L, 700))
+    fz = q.Field(L)  # b = 0: solved by x = 0 without taking a slot
+    x1, x2, xz = q.Field(L), q.Field(L), q.Field(L)
+    assert batch.add(xz, fz, 0.15, tag=7) >= 0
+    assert batch.active == 0
+    assert batch.poll() == [(7, 0, 0, 0.0)]
+    assert batch.add(x1, fb, 0.15, tag=1) == 0
+    assert batch.add(x2, fb, 0.15, tag=2) == -1
+    with pytest.raises(q.QcdGpuError):
+        batch.add(x1, x1, 0.15)
+    batch.close()
+    for f in (fb, fz, x1, x2, xz, g):
+        f.close()
