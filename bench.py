@@ -36,6 +36,8 @@ sys.path.insert(0, ROOT)
 
 L_BENCH = (48, 24, 24, 24)  # t, x, y, z
 KAPPA = 0.150
+L_PREC, KAPPA_PREC = (64, 32, 32, 32), 0.155  # precision / batching comparison
+L_MRHS = (96, 48, 48, 48)  # multi-RHS operator sweep
 THETA = (3.141592653589793, 0.0, 0.0, 0.0)
 EPS_PLAQ_060 = 0.43374
 FLOPS_PER_SITE = 1320
@@ -243,6 +245,111 @@ def solve_bench(q, orc_check, g, L, n_rhs):
     return out
 
 
+def mrhs_bench(q, torch, stream, L, nrhs_list, steps):
+    """multi-RHS operator (FP16 spinors, one link read per site for all RHS):
+    time per apply and algorithmic GB/s for each RHS-per-block count"""
+    V = L[0] * L[1] * L[2] * L[3]
+    g = q.Gauge(L, THETA).synthetic(3, EPS_PLAQ_060)
+    f = q.Field(L)
+    rows = []
+    for N in nrhs_list:
+        mi, mo = q.MField(L, N), q.MField(L, N)
+        for r in range(N):
+            mi.set(r, f.gaussian(500 + r))
+        for _ in range(3):  # the first call tunes the kernel variant for (V, N)
+            q.dslash_mrhs(mo, mi, g, KAPPA, 0.0, q.OP_D, N)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            q.dslash_mrhs(mo, mi, g, KAPPA, 0.0, q.OP_D, N)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        byts = V * (N * 104 + 288)  # N x (FP16 spinor + norm, in and out) + 4 FP32 links once per site
+        rows.append({"rhs_per_block": N, "ms_per_apply": ms, "us_per_rhs_apply": 1e3 * ms / N,
+                     "gbs": byts / (ms * 1e-3) / 1e9, "tuned": q.mrhs_tuned(L, N),
+                     "gflops": V * N * FLOPS_PER_SITE / (ms * 1e-3) / 1e9})
+        mi.close()
+        mo.close()
+    g.close()
+    f.close()
+    return {"lattice_txyz": list(L), "bytes_per_site": "104 * N + 288", "sweep": rows}
+
+
+def precision_bench(q, L, kappa, n_batch, cap):
+    """point-source columns at L, kappa, to a true residual of 1e-10: the plain
+    FP64 GPU solve (one RHS at a time) against single-RHS mixed precision and
+    the batched multi-RHS solver; RHS-solves/s over the same columns"""
+    out = {"lattice_txyz": list(L), "kappa": kappa, "tol": 1e-10}
+    g = q.Gauge(L, THETA).synthetic(2, EPS_PLAQ_060)
+    b, x = q.Field(L), q.Field(L)
+    for name, prec in (("fp64_cgnr", q.F64), ("mixed_cgnr_f32", q.F32), ("mixed_cgnr_f16", q.F16)):
+        b.point((0, 0, 0, 0), 0, 0)
+        q.sync()
+        t0 = time.perf_counter()
+        p = q.solve(x, b, g, kappa, 0.0, solver=q.SOLVER_CGNR, inner_prec=prec, tol=1e-10, maxiter=40000)
+        q.sync()
+        dt = time.perf_counter() - t0
+        out[name] = {"rhs_solves_per_s": 1.0 / dt if p.status == 0 else None, "s_per_solve": dt, "iters": p.iters,
+                     "reliable_updates": p.reliable_updates, "true_residual": p.true_residual, "status": p.status}
+    srcs = [q.Field(L).point((0, 0, 0, 0), c % 12 // 3, c % 3) if c < 12 else
+            q.Field(L).point((L[0] // 2, (c // 12) % L[1], 0, 0), c % 12 // 3, c % 3) for c in range(n_batch)]
+    xs = [q.Field(L) for _ in range(n_batch)]
+    batch = q.Batch(g, cap)
+    q.sync()
+    t0 = time.perf_counter()
+    queue = list(range(n_batch))
+    done = []
+    lat = {}
+    while queue or batch.active:
+        while queue and batch.free_slots > 0:
+            c = queue.pop(0)
+            batch.add(xs[c], srcs[c], kappa, 0.0, q.OP_D, tol=1e-10, maxiter=40000, tag=c)
+        batch.step(16)
+        for d in batch.poll():
+            done.append(d)
+            lat[d[0]] = time.perf_counter() - t0
+    q.sync()
+    dt = time.perf_counter() - t0
+    ok = len(done) == n_batch and all(d[1] == 0 for d in done)
+    ls = sorted(lat.values())
+    out["batched_mrhs"] = {"rhs": n_batch, "slots": cap, "rhs_solves_per_s": n_batch / dt if ok else None,
+                           "wall_s": dt, "iters_max": max(d[2] for d in done), "iters_min": min(d[2] for d in done),
+                           "max_true_residual": max(d[3] for d in done), "status": sorted({d[1] for d in done}),
+                           "p50_s": ls[len(ls) // 2], "p99_s": ls[min(len(ls) - 1, int(0.99 * len(ls)))],
+                           "tuned": q.mrhs_tuned(L, cap)}
+    base = out["fp64_cgnr"]["rhs_solves_per_s"]
+    if base:
+        for k in ("mixed_cgnr_f32", "mixed_cgnr_f16"):
+            if out[k]["rhs_solves_per_s"]:
+                out["speedup_" + k + "_vs_fp64"] = out[k]["rhs_solves_per_s"] / base
+        if out["batched_mrhs"]["rhs_solves_per_s"]:
+            out["speedup_batched_mrhs_vs_fp64"] = out["batched_mrhs"]["rhs_solves_per_s"] / base
+    batch.close()
+    for f in srcs + xs + [g, b, x]:
+        f.close()
+    return out
+
+
+def serving_bench(q, seconds, rate, slots, budget_gb):
+    """Poisson stream over four resident gauge fields (one per volume)"""
+    from qcd_gb300 import serving
+
+    gauges = serving.build_gauges()
+    srv = q.Server(int(budget_gb * 2**30), slots)
+    ids = [srv.add_gauge(g) for g in gauges]
+    arr = serving.make_stream(rate, seconds, len(ids), seed=7)
+    res = serving.run_stream(srv, ids, arr, max_wall_s=seconds * 6 + 60)
+    res.update({"rate_hz": rate, "arrival_s": seconds, "slots": slots, "budget_gb": budget_gb,
+                "volumes_txyz": [list(L) for L in serving.SERVE_VOLUMES], "kappa": [0.14, 0.155],
+                "rhs_per_request": [1, 48], "tols": [1e-8, 1e-10]})
+    srv.close()
+    for g in gauges:
+        g.close()
+    return res
+
+
 def run_ours(args, rank, world, local_rank):
     import numpy as np
     import torch
@@ -289,6 +396,13 @@ def run_ours(args, rank, world, local_rank):
         solve = solve_bench(q, None, g, L_BENCH, args.solve_rhs)
     for f in (g, fin, fout):
         f.close()
+    mrhs = precision = serving = None
+    if rank == 0 and not args.no_mrhs:
+        mrhs = mrhs_bench(q, torch, stream, L_MRHS, (4, 8, 16, 32, 48, 64), 10)
+    if rank == 0 and not args.no_solve:
+        precision = precision_bench(q, L_PREC, KAPPA_PREC, args.batch_rhs, args.batch_slots)
+    if rank == 0 and not args.no_serve:
+        serving = serving_bench(q, args.serve_seconds, args.serve_rate, args.serve_slots, args.serve_budget_gb)
     if rank != 0:
         return None
     peaks = measured_peaks()
@@ -313,6 +427,9 @@ def run_ours(args, rank, world, local_rank):
         "gpu_launches": launches,
         "clocks": clocks,
         "solve": solve,
+        "precision_32x64": precision,
+        "mrhs_operator": mrhs,
+        "serving": serving,
     }
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds, 1)
@@ -325,6 +442,12 @@ def run_only(args):
 
     import qcd_gb300 as q
 
+    if args.only == "mrhs":
+        stream = torch.cuda.current_stream()
+        q.set_stream(stream.cuda_stream)
+        q.set_mrhs_variant(args.mrhs_variant)
+        res = mrhs_bench(q, torch, stream, L_BENCH, (args.mrhs_n,), args.steps)
+        return {"only": "mrhs", "variant": args.mrhs_variant, **res["sweep"][0]}
     prec = {"f64": q.F64, "df64": q.F64, "f32": q.F32, "f16": q.F16}[args.only]
     arith = q.ARITH_DF64 if args.only == "df64" else q.ARITH_F64
     g64 = q.Gauge(L_BENCH, THETA).synthetic(1000, EPS_PLAQ_060)
@@ -367,9 +490,20 @@ def main():
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--solve-rhs", type=int, default=4)
+    ap.add_argument("--no-mrhs", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--batch-rhs", type=int, default=48, help="point-source columns of the batched 32^3x64 solve")
+    ap.add_argument("--batch-slots", type=int, default=48)
+    ap.add_argument("--serve-seconds", type=float, default=30.0)
+    ap.add_argument("--serve-rate", type=float, default=2.0, help="request arrivals per second")
+    ap.add_argument("--serve-slots", type=int, default=32)
+    ap.add_argument("--serve-budget-gb", type=float, default=120.0)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-seconds", type=float, default=20.0)
-    ap.add_argument("--only", choices=["f64", "df64", "f32", "f16"],
+    ap.add_argument("--mrhs-n", type=int, default=16, help="--only mrhs: RHS per block")
+    ap.add_argument("--mrhs-variant", type=int, default=-1,
+                    help="--only mrhs: -1 tuned, 1 tensor cores, 64/128/256 SIMT block size")
+    ap.add_argument("--only", choices=["f64", "df64", "f32", "f16", "mrhs"],
                     help="profiling target: time only this operator variant (a few launches under ncu)")
     args = ap.parse_args()
     if args.warmup < 3:

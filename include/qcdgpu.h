@@ -163,6 +163,18 @@ qcd_real_8 qcd_normVector(qcd_vector *vec);
 /* include/qcd_gamma.h (lib/src/qcd_gamma.c:521) */
 void qcd_gamma5Vector(qcd_vector *v);
 
+/* Source construction, computed on the GPU.
+ * include/qcd_smearing.h:41 (lib/src/qcd_smearing.c:209): one 3D APE step,
+ * apeu_mu = Proj_SU3(u_mu + alpha * spatial staples) for mu = 1..3, temporal
+ * links copied; apeu must be a different field of the same lattice.
+ * include/qcd_smearing.h:39 (lib/src/qcd_smearing.c:25): one Gaussian step
+ * v <- (v + alpha H v) / (1 + 6 alpha) on time-slice t.
+ * include/qcd_observables.h:12 (lib/src/qcd_observables.c:15): mean
+ * plaquette, 1 on the unit field (NaN on error). */
+int qcd_apeSmear3d(qcd_gaugeField *apeu, qcd_gaugeField *u, qcd_real_8 alpha);
+int qcd_gaussIteration3d(qcd_vector *v, qcd_gaugeField *u, qcd_real_8 alpha, qcd_uint_4 t);
+qcd_real_8 qcd_calculatePlaquette(qcd_gaugeField *u);
+
 /* include/qcd_communication.h:12,21 (lib/src/qcd_communication.c:20,:343).
  * One GPU holds the whole lattice: no halo exists, both are no-ops that keep
  * the reference's "communication already in flight" check. */
@@ -321,6 +333,16 @@ int qcdgpu_solve(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double kappa, d
  * stream capture. Returns 0, or 1 on error (qcdgpu_last_error). */
 int qcdgpu_dot_noalloc(const double *a, const double *b, int64_t n, double *result, void *stream);
 
+/* Source construction on device fields (FP64): n APE steps out <- in (out
+ * != in); n Gaussian steps of v on time-slice t; and the smeared point source
+ * of the 24^3 x 48 workload: a unit point at x (t, x, y, z), spin, colour,
+ * Gaussian-smeared gauss_n times with gauss_alpha on links APE-smeared ape_n
+ * times with ape_alpha (on time-slice x[0]). Return 0, or 1 on error. */
+int qcdgpu_gauge_ape3d(qcdgpu_gauge out, qcdgpu_gauge in, double alpha, int n);
+int qcdgpu_field_gauss3d(qcdgpu_field v, qcdgpu_gauge g, double alpha, int t, int n);
+int qcdgpu_smeared_source(qcdgpu_field f, qcdgpu_gauge g, const int x[4], int spin, int colour, double ape_alpha,
+                          int ape_n, double gauss_alpha, int gauss_n);
+
 /* ---------------------------------------------------------------------- */
 /* Multi-RHS (no reference counterpart: qcd_lib solves one column at a time,
  * invert.c:255). A multi-RHS field holds up to 64 spinors in FP16 with one
@@ -336,6 +358,16 @@ int qcdgpu_mfield_get(qcdgpu_field f, qcdgpu_mfield m, int r);
  * the FP64 gauge field */
 int qcdgpu_dslash_mrhs(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_gauge g, double kappa, double mu, int op,
                        int nact);
+/* The operator has two kernels: SIMT (one thread per site and RHS, links
+ * shared through L1) and tensor cores (one warp per site, link x RHS block
+ * products as TF32 MMAs). By default (-1) the first call for a lattice
+ * volume and slot count times the SIMT kernel with 64-, 128- and 256-thread
+ * blocks and the tensor-core kernel and keeps the fastest; 1 forces the
+ * tensor-core kernel, 64 / 128 / 256 the SIMT kernel with that block size. */
+int qcdgpu_set_mrhs_variant(int variant);
+/* the tuned choice for (L, nrhs): variant 0 SIMT / 1 tensor cores and the
+ * SIMT block size; returns 1 when nothing has been tuned for it yet */
+int qcdgpu_mrhs_tuned(const int L[4], int nrhs, int *variant, int *threads);
 
 /* Batched solver with continuous admission (no reference counterpart). A
  * batch of `capacity` slots (1..64) runs mixed-precision CG on the normal
@@ -363,6 +395,52 @@ int qcdgpu_batch_free_slots(qcdgpu_batch b);
 int qcdgpu_batch_poll(qcdgpu_batch b, int *tags, int *status, int *iters, double *true_residual, int max);
 /* device bytes held by the batch */
 size_t qcdgpu_batch_bytes(qcdgpu_batch b);
+
+/* Request server (no reference counterpart): solve requests of different
+ * lattices, kappas, twisted masses, RHS counts and tolerances arrive at any
+ * time and are served with continuous batching. Each resident gauge field
+ * has one batch (qcdgpu_batch) of `slots` slots on its own stream; the
+ * batches of different gauge fields run concurrently. A request is admitted
+ * (its FP64 solution and source fields allocated) in arrival order when its
+ * bytes, and those of its gauge field's batch if that is not yet built, fit
+ * in the HBM budget; its right-hand sides enter the batch as slots free up
+ * and leave it one by one as they converge. Latencies are wall-clock seconds
+ * from submission. */
+typedef struct qcdgpu_server_s *qcdgpu_server;
+typedef struct {
+  int tag;
+  int status;               /* 0 all RHS converged, else the worst RHS status */
+  int nrhs;
+  int max_iters;            /* largest iteration count among the RHS */
+  double max_true_residual; /* largest FP64 |b - op x| / |b| among the RHS */
+  double queue_s;           /* submission -> admission */
+  double latency_s;         /* submission -> last RHS retired */
+} qcdgpu_server_result;
+int qcdgpu_server_create(qcdgpu_server *s, size_t hbm_budget_bytes, int slots);
+int qcdgpu_server_destroy(qcdgpu_server s);
+/* register a resident FP64 gauge field (owned by the caller); returns its
+ * id >= 0, or -1 on error */
+int qcdgpu_server_add_gauge(qcdgpu_server s, qcdgpu_gauge g);
+/* queue a request of nrhs (1..64) right-hand sides on gauge `gauge_id`:
+ * op x = b with op QCDGPU_OP_D or QCDGPU_OP_Q. sources: nrhs FP64 fields,
+ * copied at admission (they must live until then), or NULL for the
+ * spin-colour columns of point sources: column c is spin (c % 12) / 3,
+ * colour c % 3 of a point at a position drawn from (seed, c / 12).
+ * Returns 0, or 1 on error. */
+int qcdgpu_server_submit(qcdgpu_server s, int gauge_id, int nrhs, const qcdgpu_field *sources, uint64_t seed,
+                         double kappa, double mu, int op, double tol, int maxiter, int tag);
+/* one scheduling round: admission, slot filling, one chunk of iterations
+ * on every busy batch, retirement. Returns 0, or 3 on a CUDA error. */
+int qcdgpu_server_progress(qcdgpu_server s);
+/* completed requests, oldest first; returns the count */
+int qcdgpu_server_poll(qcdgpu_server s, qcdgpu_server_result *out, int max);
+/* copy column `col` of a completed request's solution into dst (FP64) */
+int qcdgpu_server_fetch(qcdgpu_server s, int tag, int col, qcdgpu_field dst);
+/* free a completed request's fields (and return its bytes to the budget) */
+int qcdgpu_server_release(qcdgpu_server s, int tag);
+/* bytes held, requests waiting for admission, and admitted RHS not yet
+ * retired (in a batch or waiting for a slot) */
+int qcdgpu_server_stats(qcdgpu_server s, size_t *bytes_used, int *queued, int *active_rhs);
 
 #ifdef __cplusplus
 }

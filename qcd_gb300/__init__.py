@@ -171,6 +171,26 @@ def lib() -> C.CDLL:
     L.qcdgpu_mfield_set.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
     L.qcdgpu_mfield_get.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
     L.qcdgpu_dslash_mrhs.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_int]
+    L.qcd_apeSmear3d.argtypes = [up, up, C.c_double]
+    L.qcd_gaussIteration3d.argtypes = [vp, up, C.c_double, C.c_uint32]
+    L.qcd_calculatePlaquette.argtypes = [up]
+    L.qcd_calculatePlaquette.restype = C.c_double
+    L.qcdgpu_gauge_ape3d.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_int]
+    L.qcdgpu_field_gauss3d.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_int]
+    L.qcdgpu_smeared_source.argtypes = [C.c_void_p, C.c_void_p, _ip, C.c_int, C.c_int, C.c_double, C.c_int,
+                                        C.c_double, C.c_int]
+    L.qcdgpu_set_mrhs_variant.argtypes = [C.c_int]
+    L.qcdgpu_mrhs_tuned.argtypes = [_ip, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.qcdgpu_server_create.argtypes = [vpp, C.c_size_t, C.c_int]
+    L.qcdgpu_server_destroy.argtypes = [C.c_void_p]
+    L.qcdgpu_server_add_gauge.argtypes = [C.c_void_p, C.c_void_p]
+    L.qcdgpu_server_submit.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_uint64, C.c_double, C.c_double,
+                                       C.c_int, C.c_double, C.c_int, C.c_int]
+    L.qcdgpu_server_progress.argtypes = [C.c_void_p]
+    L.qcdgpu_server_poll.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+    L.qcdgpu_server_fetch.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    L.qcdgpu_server_release.argtypes = [C.c_void_p, C.c_int]
+    L.qcdgpu_server_stats.argtypes = [C.c_void_p, C.POINTER(C.c_size_t), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.qcdgpu_batch_create.argtypes = [vpp, C.c_void_p, C.c_int]
     L.qcdgpu_batch_destroy.argtypes = [C.c_void_p]
     L.qcdgpu_batch_add.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_double,
@@ -416,6 +436,39 @@ class MField:
             self.h = None
 
 
+def ape3d(out: "Gauge", inp: "Gauge", alpha: float, n: int = 1) -> "Gauge":
+    """n 3D APE smearing steps out <- inp (device FP64 gauge fields)."""
+    _check(lib().qcdgpu_gauge_ape3d(out.h, inp.h, alpha, n), "qcdgpu_gauge_ape3d")
+    return out
+
+
+def gauss3d(v: "Field", g: "Gauge", alpha: float, t: int, n: int = 1) -> "Field":
+    """n 3D Gaussian smearing steps of v on time-slice t."""
+    _check(lib().qcdgpu_field_gauss3d(v.h, g.h, alpha, t, n), "qcdgpu_field_gauss3d")
+    return v
+
+
+def smeared_source(f: "Field", g: "Gauge", x, spin: int, colour: int, ape_alpha: float = 0.5, ape_n: int = 20,
+                   gauss_alpha: float = 4.0, gauss_n: int = 50) -> "Field":
+    """point source at x = (t, x, y, z), Gaussian-smeared on APE-smeared links."""
+    _check(lib().qcdgpu_smeared_source(f.h, g.h, np.ascontiguousarray(x, dtype=np.int32), spin, colour, ape_alpha,
+                                       ape_n, gauss_alpha, gauss_n), "qcdgpu_smeared_source")
+    return f
+
+
+def set_mrhs_variant(v: int) -> None:
+    """-1: tuned; 1: tensor-core kernel; 64 / 128 / 256: SIMT kernel with that block size."""
+    _check(lib().qcdgpu_set_mrhs_variant(v), "qcdgpu_set_mrhs_variant")
+
+
+def mrhs_tuned(L, nrhs):
+    """(variant, threads) the tuner chose for this volume and slot count, or None."""
+    v, t = C.c_int(), C.c_int()
+    if lib().qcdgpu_mrhs_tuned(np.asarray(L, np.int32), nrhs, C.byref(v), C.byref(t)) != 0:
+        return None
+    return ("simt" if v.value == 0 else "mma", t.value)
+
+
 def dslash_mrhs(out: MField, inp: MField, g: Gauge, kappa: float, mu: float = 0.0, op: int = OP_D, nact=None):
     _check(lib().qcdgpu_dslash_mrhs(out.h, inp.h, g.h, kappa, mu, op, inp.n if nact is None else nact),
            "qcdgpu_dslash_mrhs")
@@ -464,6 +517,68 @@ class Batch:
     def close(self):
         if self.h:
             lib().qcdgpu_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class ServerResult(C.Structure):
+    _fields_ = [("tag", C.c_int), ("status", C.c_int), ("nrhs", C.c_int), ("max_iters", C.c_int),
+                ("max_true_residual", C.c_double), ("queue_s", C.c_double), ("latency_s", C.c_double)]
+
+
+class Server:
+    """Request server with continuous batching and HBM-budget admission (qcdgpu_server)."""
+
+    def __init__(self, hbm_budget_bytes: int, slots: int = 32):
+        self.h = C.c_void_p()
+        _check(lib().qcdgpu_server_create(C.byref(self.h), int(hbm_budget_bytes), slots), "qcdgpu_server_create")
+
+    def add_gauge(self, g: Gauge) -> int:
+        gid = lib().qcdgpu_server_add_gauge(self.h, g.h)
+        if gid < 0:
+            raise QcdGpuError(f"qcdgpu_server_add_gauge failed: {lib().qcdgpu_last_error().decode()}")
+        return gid
+
+    def submit(self, gauge_id: int, nrhs: int, kappa: float, mu: float = 0.0, op: int = OP_D, tol: float = 1e-10,
+               tag: int = 0, sources=None, seed: int = 0, maxiter: int = 0) -> None:
+        src = None
+        if sources is not None:
+            arr = (C.c_void_p * nrhs)(*[f.h.value for f in sources])
+            src = C.cast(arr, C.c_void_p)
+        _check(lib().qcdgpu_server_submit(self.h, gauge_id, nrhs, src, seed, kappa, mu, op, tol, maxiter, tag),
+               "qcdgpu_server_submit")
+
+    def progress(self) -> None:
+        _check(lib().qcdgpu_server_progress(self.h), "qcdgpu_server_progress")
+
+    def poll(self, max_n: int = 256):
+        out = (ServerResult * max_n)()
+        n = lib().qcdgpu_server_poll(self.h, C.cast(out, C.c_void_p), max_n)
+        return [dict(tag=r.tag, status=r.status, nrhs=r.nrhs, max_iters=r.max_iters,
+                     max_true_residual=r.max_true_residual, queue_s=r.queue_s, latency_s=r.latency_s)
+                for r in out[:n]]
+
+    def fetch(self, tag: int, col: int, dst: Field) -> Field:
+        _check(lib().qcdgpu_server_fetch(self.h, tag, col, dst.h), "qcdgpu_server_fetch")
+        return dst
+
+    def release(self, tag: int) -> None:
+        _check(lib().qcdgpu_server_release(self.h, tag), "qcdgpu_server_release")
+
+    def stats(self):
+        used, queued, active = C.c_size_t(), C.c_int(), C.c_int()
+        _check(lib().qcdgpu_server_stats(self.h, C.byref(used), C.byref(queued), C.byref(active)),
+               "qcdgpu_server_stats")
+        return dict(bytes_used=used.value, queued=queued.value, active_rhs=active.value)
+
+    def close(self):
+        if self.h:
+            lib().qcdgpu_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -6,6 +6,7 @@
 // output back to host memory before returning, so the caller observes the
 // reference's synchronous semantics. qcd_initVector / qcd_initGaugeField
 // allocate page-locked host memory so these copies run at full link speed.
+#include <math.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -481,6 +482,56 @@ int qcd_communicateVectorPMGaugeP(qcd_vector *v, qcd_gaugeField *u)
 }
 
 void qcd_waitall(qcd_geometry *geo) { geo->numOfRequests = 0; }
+
+// ------------------------------------------------------ source construction
+// include/qcd_smearing.h:41 (lib/src/qcd_smearing.c:209): one 3D APE step
+int qcd_apeSmear3d(qcd_gaugeField *apeu, qcd_gaugeField *u, qcd_real_8 alpha)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!apeu || !apeu->initialized || !apeu->D || !apeu->geo || apeu->geo->initialized != 1 || apeu->D == u->D) {
+    set_error("qcd_apeSmear3d: output gauge field not initialized or the same as the input");
+    return 1;
+  }
+  qcdgpu_gauge gin = gauge_in(u);
+  if (!gin) return 1;
+  int L[4];
+  geo_L(apeu->geo, L);
+  if (!same_L(L, gin->L)) {
+    set_error("qcd_apeSmear3d: lattices differ");
+    return 1;
+  }
+  GaugeMirror &m = g_gauge[(const void *)apeu->D];
+  if (m.g && (!same_L(m.g->L, L) || memcmp(m.g->theta, apeu->geo->theta, sizeof(m.g->theta)) != 0)) {
+    gauge_forget(m.g);
+    gauge_free(m.g);
+    m.g = nullptr;
+    m.resident = false;
+  }
+  if (!m.g) m.g = gauge_new(L, apeu->geo->theta, QCDGPU_F64, 18);
+  if (!m.g || !ape3d(m.g, gin, alpha)) return 1;
+  if (m.resident) return QG_CUDA(cudaStreamSynchronize(stream())) ? 0 : 1;
+  return download_gauge_aos(m.g, (double *)apeu->D) ? 0 : 1;
+}
+
+// include/qcd_smearing.h:39 (lib/src/qcd_smearing.c:25): one Gaussian step on time-slice t
+int qcd_gaussIteration3d(qcd_vector *v, qcd_gaugeField *u, qcd_real_8 alpha, qcd_uint_4 t)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  qcdgpu_field f = vec_in(v);
+  qcdgpu_gauge g = f ? gauge_in(u) : nullptr;
+  if (!f || !g) return 1;
+  if (!gauss3d(f, g, alpha, (int)t, 1)) return 1;
+  return vec_done(v) ? 0 : 1;
+}
+
+// include/qcd_observables.h:12 (lib/src/qcd_observables.c:15): mean plaquette
+qcd_real_8 qcd_calculatePlaquette(qcd_gaugeField *u)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  qcdgpu_gauge g = gauge_in(u);
+  if (!g) return NAN;
+  return plaquette(g);
+}
 
 // --------------------------------------------------------------- solvers
 qcd_int_4 gcr(qcd_vector *sol, qcd_vector *src, qcd_gaugeField *u, qcd_real_8 kappa, qcd_real_8 muTM,

@@ -44,16 +44,19 @@ __global__ void __launch_bounds__(128) k_cg_update(void *xs, float *xsn, const v
   int x = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   double n2 = 0.0;
   if (x < V) {
+    // FP16 iterations keep the solution increment in FP32: rounding every
+    // increment to 11 bits would cost iterations
+    constexpr int PX = P == QCDGPU_F16 ? QCDGPU_F32 : P;
     const R alpha = (R)s[S_ALPHA];
     C<R> vx[12], vp[12];
-    Spinor<P, R>::load(xs, xsn, stride, x, vx);
+    Spinor<PX, R>::load(xs, xsn, stride, x, vx);
     Spinor<P, R>::load(ps, psn, stride, x, vp);
 #pragma unroll
     for (int k = 0; k < 12; k++) {
       vx[k].re = qfma(alpha, vp[k].re, vx[k].re);
       vx[k].im = qfma(alpha, vp[k].im, vx[k].im);
     }
-    Spinor<P, R>::store(xs, xsn, stride, x, vx);
+    Spinor<PX, R>::store(xs, xsn, stride, x, vx);
     Spinor<P, R>::load(rs, rsn, stride, x, vx);
     Spinor<P, R>::load(aps, apsn, stride, x, vp);
 #pragma unroll
@@ -164,7 +167,8 @@ int solve_cgnr_engine(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4
   const int prec = p->inner_prec;
   qcdgpu_gauge gi = gauge_at(g, prec);
   qcdgpu_field rt = w.get(b->L, QCDGPU_F64), r = w.get(b->L, QCDGPU_F64), up = w.get(b->L, QCDGPU_F64);
-  qcdgpu_field rs = w.get(b->L, prec), xs = w.get(b->L, prec), ps = w.get(b->L, prec);
+  qcdgpu_field rs = w.get(b->L, prec), ps = w.get(b->L, prec);
+  qcdgpu_field xs = w.get(b->L, prec == QCDGPU_F16 ? QCDGPU_F32 : prec);
   qcdgpu_field t = w.get(b->L, prec), aps = w.get(b->L, prec);
   if (!gi || !rt || !r || !up || !rs || !xs || !ps || !t || !aps) return 3;
   const int V = (int)b->V;

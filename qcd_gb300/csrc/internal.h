@@ -40,6 +40,17 @@ bool after_launch(const char *what);
 extern std::atomic<uint64_t> g_launches;
 
 cudaStream_t stream();
+cudaStream_t swap_stream(cudaStream_t s);  // returns the previous stream
+inline void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+// the library's calls go to `s` while the scope lives
+struct StreamScope {
+  cudaStream_t prev;
+  explicit StreamScope(cudaStream_t s) : prev(swap_stream(s)) {}
+  ~StreamScope() { swap_stream(prev); }
+  StreamScope(const StreamScope &) = delete;
+  StreamScope &operator=(const StreamScope &) = delete;
+};
 
 // ------------------------------------------------------------------ fields
 inline int64_t pad_stride(int64_t V) { return (V + 127) / 128 * 128; }
@@ -137,6 +148,11 @@ bool field_gaussian(qcdgpu_field f, uint64_t seed);
 bool field_z4(qcdgpu_field f, uint64_t seed);
 bool field_point(qcdgpu_field f, const int x[4], int spin, int colour);
 double plaquette(qcdgpu_gauge g);
+
+// smear.cu: one 3D APE step out <- in, and n Gaussian steps of v on
+// time-slice t (both FP64)
+bool ape3d(qcdgpu_gauge out, qcdgpu_gauge in, double alpha);
+bool gauss3d(qcdgpu_field v, qcdgpu_gauge g, double alpha, int t, int n);
 
 // solvers.cu
 int solve(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, double tm,

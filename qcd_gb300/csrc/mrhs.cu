@@ -18,16 +18,11 @@
 // small residual vectors need no rescaling.
 #include <string.h>
 
-#include "dslash_args.h"
+#include <map>
+#include <utility>
 
-struct qcdgpu_mfield_s {
-  int L[4];
-  int64_t V;
-  int N;     // RHS slots
-  void *data;
-  float *norm;
-  size_t bytes;
-};
+#include "mrhs.h"
+#include "wilson_kernel.cuh"
 
 namespace qg {
 
@@ -222,6 +217,145 @@ __global__ void __launch_bounds__(128) k_wilson_mrhs(const MArgs a)
     }
 }
 
+// ------------------------------------------------ SIMT variant (FP32 cores)
+// One thread per site and RP adjacent RHS slots, block (N / RP threads, SB
+// sites): the threads of one site read the same links (L1 broadcast), so
+// the gauge field is fetched once per site for all RHS, while the per-RHS
+// spin projection, link products and reconstruction run as FP32 FMAs. With
+// RP = 2 a thread loads the two slots' half2 values of a component as one
+// 8-byte word and applies each link it loads to both. With `partials` the
+// epilogue also writes, per block and slot, the sum of |out|^2 over the
+// block's sites (partials[block * N + slot]) in a fixed order.
+template <int RP>
+__device__ __forceinline__ void mload_rp(const MArgs &a, int y, int r0, C<float> s[RP][12], float nrm[RP])
+{
+  if (RP == 2) {
+    const float2 n2 = *(const float2 *)(a.in_norm + (int64_t)y * a.N + r0);
+    nrm[0] = n2.x;
+    nrm[RP - 1] = n2.y;
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      const uint2 w = *(const uint2 *)(a.in + ((int64_t)k * a.V + y) * a.N + r0);
+      const float2 f0 = __half22float2(*(const __half2 *)&w.x), f1 = __half22float2(*(const __half2 *)&w.y);
+      s[0][k] = C<float>{f0.x, f0.y};
+      s[RP - 1][k] = C<float>{f1.x, f1.y};
+    }
+  } else {
+    nrm[0] = a.in_norm[(int64_t)y * a.N + r0];
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      const float2 f = __half22float2(a.in[((int64_t)k * a.V + y) * a.N + r0]);
+      s[0][k] = C<float>{f.x, f.y};
+    }
+  }
+}
+
+template <int MU, bool DAG, int RP>
+__device__ __forceinline__ void mhop_pair(const MArgs &a, int x, const int c[4], int r0, C<float> acc[RP][12])
+{
+  constexpr int SF = DAG ? +1 : -1;
+  const bool twisted = (a.twist_mask >> MU) & 1;
+#pragma unroll
+  for (int dir = 0; dir < 2; dir++) {
+    const bool back = dir == 1;
+    const int y = back ? bwd(a.geo, x, c, MU) : fwd(a.geo, x, c, MU);
+    C<float> s[RP][12], U[9];
+    float nrm[RP];
+    mload_rp<RP>(a, y, r0, s, nrm);
+    Link<QCDGPU_F32, 18, float>::load(a.gauge, a.gstride, back ? y : x, MU, U);
+#pragma unroll
+    for (int q = 0; q < RP; q++) {
+      C<float> h[6], uh[6];
+      if (back) project<MU, -SF>(s[q], h);
+      else project<MU, SF>(s[q], h);
+#pragma unroll
+      for (int k = 0; k < 6; k++) h[k] = C<float>{h[k].re * nrm[q], h[k].im * nrm[q]};
+#pragma unroll
+      for (int j = 0; j < 2; j++)
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+          uh[3 * j + i] = back ? cdot(U[i], h[3 * j]) + cdot(U[3 + i], h[3 * j + 1]) + cdot(U[6 + i], h[3 * j + 2])
+                               : U[3 * i] * h[3 * j] + U[3 * i + 1] * h[3 * j + 1] + U[3 * i + 2] * h[3 * j + 2];
+      if (twisted) {
+        C<float> ph{a.phr[MU], back ? -a.phi[MU] : a.phi[MU]};
+#pragma unroll
+        for (int k = 0; k < 6; k++) uh[k] = uh[k] * ph;
+      }
+      if (back) accumulate<MU, -SF>(acc[q], uh);
+      else accumulate<MU, SF>(acc[q], uh);
+    }
+  }
+}
+
+template <bool DAG, int RP>
+__global__ void __launch_bounds__(256) k_wilson_mrhs_simt(const MArgs a, double *partials)
+{
+  const int r0 = threadIdx.x * RP;
+  const int x = blockIdx.x * blockDim.y + threadIdx.y;
+  double n2[RP];
+#pragma unroll
+  for (int q = 0; q < RP; q++) n2[q] = 0.0;
+  if (r0 < a.nact && x < a.V) {
+    int c[4];
+    coords(a.geo, x, c);
+    C<float> acc[RP][12];
+#pragma unroll
+    for (int q = 0; q < RP; q++)
+#pragma unroll
+      for (int k = 0; k < 12; k++) acc[q][k] = C<float>{0.f, 0.f};
+    mhop_pair<0, DAG, RP>(a, x, c, r0, acc);
+    mhop_pair<1, DAG, RP>(a, x, c, r0, acc);
+    mhop_pair<2, DAG, RP>(a, x, c, r0, acc);
+    mhop_pair<3, DAG, RP>(a, x, c, r0, acc);
+    C<float> s[RP][12];
+    float nrm[RP];
+    mload_rp<RP>(a, x, r0, s, nrm);
+#pragma unroll
+    for (int q = 0; q < RP; q++) {
+      const int r = r0 + q;
+      // slots past nact hold zeros; their results are not stored
+      const float mp4r = (a.mp4s ? a.mp4s[r] : a.mp4) * nrm[q];
+      const float tmr = (a.tms ? (DAG ? -a.tms[r] : a.tms[r]) : a.tm) * nrm[q];
+      float mx = 0.f;
+#pragma unroll
+      for (int k = 0; k < 12; k++) {
+        const float g5tm = k < 6 ? tmr : -tmr;
+        acc[q][k] = C<float>{mp4r * s[q][k].re - g5tm * s[q][k].im - 0.5f * acc[q][k].re,
+                             mp4r * s[q][k].im + g5tm * s[q][k].re - 0.5f * acc[q][k].im};
+        mx = fmaxf(mx, fmaxf(fabsf(acc[q][k].re), fabsf(acc[q][k].im)));
+      }
+      if (!(mx >= 1.17549435e-38f)) mx = 0.f;
+      const float inv = mx > 0.f ? 1.0f / mx : 0.f;
+      if (r < a.nact) {
+#pragma unroll
+        for (int k = 0; k < 12; k++) {
+          const __half2 h = __floats2half2_rn(acc[q][k].re * inv, acc[q][k].im * inv);
+          a.out[((int64_t)k * a.V + x) * a.N + r] = h;
+          if (partials) {
+            const float2 f = __half22float2(h);
+            n2[q] += (double)(f.x * mx) * (f.x * mx) + (double)(f.y * mx) * (f.y * mx);
+          }
+        }
+        a.out_norm[(int64_t)x * a.N + r] = mx;
+      }
+    }
+  }
+  if (partials) {
+    extern __shared__ double sh[];
+    const int N = a.N, y = threadIdx.y;
+#pragma unroll
+    for (int q = 0; q < RP; q++)
+      if (threadIdx.x * RP + q < N) sh[y * N + threadIdx.x * RP + q] = n2[q];
+    __syncthreads();
+    for (int r = threadIdx.x; r < N; r += blockDim.x)
+      if (y == 0) {
+        double t = 0.0;
+        for (int i = 0; i < (int)blockDim.y; i++) t += sh[i * N + r];
+        partials[(int64_t)blockIdx.x * N + r] = t;
+      }
+  }
+}
+
 // ------------------------------------------------------------ fields
 qcdgpu_mfield mfield_new(const int L[4], int N)
 {
@@ -321,8 +455,147 @@ bool mfield_get(qcdgpu_field f, qcdgpu_mfield m, int r)
 
 // out = D in (dag: D^+ in) for the first nact RHS of the two fields; with
 // mp4s / tms (device float arrays) each slot r uses its own diagonal
+// ------------------------------------------------------------ launch + tuner
+// per-slot sum of |v|^2 over the block's sites (for the tensor-core variant,
+// whose epilogue has no reduction); block (N, SB) like the SIMT variant
+__global__ void k_mnorm(const __half2 *d, const float *dn, int V, int N, int nact, double *partials)
+{
+  const int r = threadIdx.x, x = blockIdx.x * blockDim.y + threadIdx.y;
+  double n2 = 0.0;
+  if (r < nact && x < V) {
+    const float s = dn[(int64_t)x * N + r];
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      float2 f = __half22float2(d[((int64_t)k * V + x) * N + r]);
+      n2 += (double)(f.x * s) * (f.x * s) + (double)(f.y * s) * (f.y * s);
+    }
+  }
+  extern __shared__ double sh[];
+  const int y = threadIdx.y;
+  sh[y * N + r] = n2;
+  __syncthreads();
+  if (y == 0) {
+    double t = 0.0;
+    for (int i = 0; i < (int)blockDim.y; i++) t += sh[i * N + r];
+    partials[(int64_t)blockIdx.x * N + r] = t;
+  }
+}
+
+struct MrhsTune {
+  int variant;  // MRHS_SIMT or MRHS_MMA
+  int threads;  // SIMT: N x (sites per block) target, 64, 128 or 256
+  int rp;       // SIMT: RHS slots per thread (1, or 2 when N is even)
+};
+
+static int g_mrhs_variant = MRHS_AUTO;
+static std::map<std::pair<int64_t, int>, MrhsTune> g_mrhs_tuned;
+
+// block (N / rp slot threads, sites per block)
+static dim3 simt_block(int N, int threads, int rp = 1)
+{
+  const int sb = threads / N > 0 ? threads / N : 1;
+  return dim3((unsigned)((N + rp - 1) / rp), (unsigned)sb);
+}
+
+unsigned mrhs_max_blocks(int64_t V, int N)
+{
+  const dim3 b = simt_block(N, 64);  // the smallest sites-per-block of any shape
+  return (unsigned)((V + b.y - 1) / b.y);
+}
+
+static bool launch_mrhs(const MArgs &a, bool dag, MrhsTune t, double *partials, unsigned *nblocks)
+{
+  cudaStream_t s = stream();
+  const bool simt = t.variant == MRHS_SIMT;
+  const dim3 blk = simt_block(a.N, simt ? t.threads : 256, simt ? t.rp : 1);
+  const unsigned nb = (unsigned)((a.V + blk.y - 1) / blk.y);
+  const size_t shm = sizeof(double) * a.N * blk.y;
+  if (simt) {
+    const size_t sm = partials ? shm : 0;
+    if (t.rp == 2) {
+      if (dag) k_wilson_mrhs_simt<true, 2><<<nb, blk, sm, s>>>(a, partials);
+      else k_wilson_mrhs_simt<false, 2><<<nb, blk, sm, s>>>(a, partials);
+    } else {
+      if (dag) k_wilson_mrhs_simt<true, 1><<<nb, blk, sm, s>>>(a, partials);
+      else k_wilson_mrhs_simt<false, 1><<<nb, blk, sm, s>>>(a, partials);
+    }
+    if (!QG_LAUNCHED("wilson_mrhs_simt")) return false;
+  } else {
+    unsigned grid = (unsigned)((a.V + 3) / 4);
+    int mt = (a.nact + 15) / 16;
+#define QG_MRHS(MT)                                                      \
+  if (dag) k_wilson_mrhs<true, MT><<<grid, 128, 0, s>>>(a);              \
+  else k_wilson_mrhs<false, MT><<<grid, 128, 0, s>>>(a);
+    switch (mt) {
+    case 1: QG_MRHS(1) break;
+    case 2: QG_MRHS(2) break;
+    case 3: QG_MRHS(3) break;
+    default: QG_MRHS(4) break;
+    }
+#undef QG_MRHS
+    if (!QG_LAUNCHED("wilson_mrhs")) return false;
+    if (partials) {
+      k_mnorm<<<nb, simt_block(a.N, 256), shm, s>>>(a.out, a.out_norm, a.V, a.N, a.nact, partials);
+      if (!QG_LAUNCHED("mrhs_norm")) return false;
+    }
+  }
+  if (nblocks) *nblocks = nb;
+  return true;
+}
+
+// Pick the variant and block shape for (V, N) by timing each candidate
+// three times on the caller's fields (the output is overwritten with the
+// same result). Not while the stream is being captured: then the SIMT
+// variant with 256-thread blocks runs until a tuned choice exists.
+static MrhsTune mrhs_tune(const MArgs &a, bool dag, qcdgpu_mfield out, qcdgpu_mfield in)
+{
+  (void)out;
+  (void)in;
+  if (g_mrhs_variant == MRHS_MMA) return MrhsTune{MRHS_MMA, 256, 1};
+  if (g_mrhs_variant >= 64) {  // forced block size; +1: two slots per thread
+    const int rp = (g_mrhs_variant & 1) && a.N % 2 == 0 ? 2 : 1;
+    return MrhsTune{MRHS_SIMT, g_mrhs_variant & ~1, rp};
+  }
+  const auto key = std::make_pair((int64_t)a.V, a.N);
+  auto it = g_mrhs_tuned.find(key);
+  if (it != g_mrhs_tuned.end()) return it->second;
+  const MrhsTune fallback{MRHS_SIMT, 128, 1};
+  cudaStream_t s = stream();
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return fallback;
+  const MrhsTune cands[] = {{MRHS_SIMT, 64, 1}, {MRHS_SIMT, 128, 1}, {MRHS_SIMT, 256, 1}, {MRHS_SIMT, 64, 2},
+                            {MRHS_SIMT, 128, 2}, {MRHS_SIMT, 256, 2}, {MRHS_MMA, 256, 1}};
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return fallback;
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return fallback;
+  }
+  MrhsTune best = fallback;
+  float best_ms = 1e30f;
+  for (const MrhsTune &c : cands) {
+    if (c.variant == MRHS_SIMT && (c.threads < a.N || (c.rp == 2 && a.N % 2 != 0))) continue;
+    if (!launch_mrhs(a, dag, c, nullptr, nullptr)) break;  // warm-up
+    cudaEventRecord(e0, s);
+    bool ok = true;
+    for (int i = 0; i < 3 && ok; i++) ok = launch_mrhs(a, dag, c, nullptr, nullptr);
+    cudaEventRecord(e1, s);
+    if (!ok || cudaEventSynchronize(e1) != cudaSuccess) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  g_mrhs_tuned[key] = best;
+  return best;
+}
+
 bool dslash_mrhs(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_gauge g, double mp4, double tm, bool dag, int nact,
-                 const float *mp4s, const float *tms)
+                 const float *mp4s, const float *tms, double *partials, unsigned *nblocks)
 {
   if (!out || !in || !g || out == in || out->N != in->N || out->V != in->V || in->V != g->V ||
       memcmp(out->L, in->L, sizeof(in->L)) != 0 || memcmp(in->L, g->L, sizeof(g->L)) != 0) {
@@ -368,21 +641,13 @@ bool dslash_mrhs(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_gauge g, double mp4
   a.tm = (float)(dag ? -tm : tm);
   a.mp4s = mp4s;
   a.tms = tms;
-  if (nact == 0) return true;
-  unsigned grid = (unsigned)((a.V + 3) / 4);
-  cudaStream_t s = stream();
-  int mt = (nact + 15) / 16;
-#define QG_MRHS(MT)                                                      \
-  if (dag) k_wilson_mrhs<true, MT><<<grid, 128, 0, s>>>(a);              \
-  else k_wilson_mrhs<false, MT><<<grid, 128, 0, s>>>(a);
-  switch (mt) {
-  case 1: QG_MRHS(1) break;
-  case 2: QG_MRHS(2) break;
-  case 3: QG_MRHS(3) break;
-  default: QG_MRHS(4) break;
+  if (nact == 0) {
+    if (nblocks) *nblocks = 0;
+    return true;
   }
-#undef QG_MRHS
-  return QG_LAUNCHED("wilson_mrhs");
+  const MrhsTune tune = mrhs_tune(a, dag, out, in);
+  if (!launch_mrhs(a, dag, tune, partials, nblocks)) return false;
+  return true;
 }
 
 }  // namespace qg
@@ -401,6 +666,28 @@ int qcdgpu_mfield_destroy(qcdgpu_mfield m)
 }
 int qcdgpu_mfield_set(qcdgpu_mfield m, int r, qcdgpu_field f) { return qg::mfield_set(m, r, f) ? 0 : 1; }
 int qcdgpu_mfield_get(qcdgpu_field f, qcdgpu_mfield m, int r) { return qg::mfield_get(f, m, r) ? 0 : 1; }
+int qcdgpu_set_mrhs_variant(int v)
+{
+  if (v != qg::MRHS_AUTO && v != qg::MRHS_MMA && v != 64 && v != 128 && v != 256 && v != 65 && v != 129 &&
+      v != 257) {
+    qg::set_error("multi-RHS variant: -1 (tuned), 1 (tensor cores), 64 / 128 / 256 (SIMT, slots x sites per "
+                  "block), +1 for two slots per thread");
+    return 1;
+  }
+  qg::g_mrhs_variant = v;
+  return 0;
+}
+
+int qcdgpu_mrhs_tuned(const int L[4], int nrhs, int *variant, int *threads)
+{
+  const int64_t V = (int64_t)L[0] * L[1] * L[2] * L[3];
+  auto it = qg::g_mrhs_tuned.find(std::make_pair(V, nrhs));
+  if (it == qg::g_mrhs_tuned.end()) return 1;
+  *variant = it->second.variant;
+  *threads = it->second.threads + (it->second.rp == 2 ? 1 : 0);
+  return 0;
+}
+
 int qcdgpu_dslash_mrhs(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_gauge g, double kappa, double mu, int op,
                        int nact)
 {

@@ -2,11 +2,13 @@
 // with continuous admission and retirement (the engine behind the serving
 // loop).
 //
-// A batch owns multi-RHS work fields (FP16, tensor-core operator) with a
-// fixed number of slots and runs the mixed-precision reliable-update CG of
-// cg.cu for all occupied slots at once: every inner iteration is two
-// multi-RHS operator launches plus four per-(site, RHS) kernels, with
-// per-slot scalars kept on the device. The operator's hopping term does not
+// A batch owns multi-RHS work fields (FP16 with per-(site, slot) norms; the
+// solution increments in FP32) with a fixed number of slots and runs the
+// mixed-precision reliable-update CG of cg.cu for all occupied slots at once:
+// every inner iteration is two multi-RHS operator launches (the first also
+// sums |D p|^2 per slot) plus three small per-(site, slot) kernels, with
+// per-slot scalars kept on the device; a chunk of 16 iterations is one CUDA
+// graph launch. The operator's hopping term does not
 // depend on kappa or mu, so each slot carries its own diagonal and a batch
 // mixes requests of different kappa and twisted mass on one gauge field.
 // Between chunks of iterations the host reads the per-slot residual
@@ -21,27 +23,11 @@
 
 #include <vector>
 
-#include "internal.h"
-
-struct qcdgpu_mfield_s {
-  int L[4];
-  int64_t V;
-  int N;
-  void *data;
-  float *norm;
-  size_t bytes;
-};
+#include "mrhs.h"
 
 namespace qg {
 
 using namespace qgd;
-
-qcdgpu_mfield mfield_new(const int L[4], int N);
-void mfield_free(qcdgpu_mfield m);
-bool mfield_set(qcdgpu_mfield m, int r, qcdgpu_field f);
-bool mfield_get(qcdgpu_field f, qcdgpu_mfield m, int r);
-bool dslash_mrhs(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_gauge g, double mp4, double tm, bool dag, int nact,
-                 const float *mp4s, const float *tms);
 
 struct MV {
   __half2 *d;
@@ -91,34 +77,28 @@ __device__ __forceinline__ void slot_partial(double v, double *partials)
   }
 }
 
-// partials <- Re <a_r, b_r> per slot
-__global__ void k_mdot(MV a, MV b, int nact, double *partials)
-{
-  const int r = threadIdx.x, x = blockIdx.x * blockDim.y + threadIdx.y;
-  double d = 0.0;
-  if (r < nact && x < a.V) {
-    float2 va[12], vb[12];
-    mv_load(a, x, r, va);
-    mv_load(b, x, r, vb);
-#pragma unroll
-    for (int k = 0; k < 12; k++) d += (double)va[k].x * vb[k].x + (double)va[k].y * vb[k].y;
-  }
-  slot_partial(d, partials);
-}
+// FP32 solution increments of the slots, [component][site][slot] float2:
+// FP16 would round every increment to 11 bits and cost iterations
+struct MX {
+  float2 *d;
+  int V, N;
+};
 
 // xs += alpha p ; rs -= alpha Ap ; partials <- |rs|^2 per slot
-__global__ void k_mupdate(MV xs, MV ps, MV rs, MV aps, int nact, const double *alpha, double *partials)
+__global__ void k_mupdate(MX xs, MV ps, MV rs, MV aps, int nact, const double *alpha, double *partials)
 {
   const int r = threadIdx.x, x = blockIdx.x * blockDim.y + threadIdx.y;
   double n2 = 0.0;
   if (r < nact && x < xs.V) {
     const float al = (float)alpha[r];
     float2 a[12], b[12];
-    mv_load(xs, x, r, a);
     mv_load(ps, x, r, b);
 #pragma unroll
-    for (int k = 0; k < 12; k++) a[k] = make_float2(__fmaf_rn(al, b[k].x, a[k].x), __fmaf_rn(al, b[k].y, a[k].y));
-    mv_store(xs, x, r, a);
+    for (int k = 0; k < 12; k++) {
+      float2 &v = xs.d[((int64_t)k * xs.V + x) * xs.N + r];
+      float2 w = v;
+      v = make_float2(__fmaf_rn(al, b[k].x, w.x), __fmaf_rn(al, b[k].y, w.y));
+    }
     mv_load(rs, x, r, a);
     mv_load(aps, x, r, b);
 #pragma unroll
@@ -129,6 +109,32 @@ __global__ void k_mupdate(MV xs, MV ps, MV rs, MV aps, int nact, const double *a
     mv_store(rs, x, r, a);
   }
   slot_partial(n2, partials);
+}
+
+// f (FP64 field) += slot r of xs, then slot r of xs <- 0
+__global__ void k_mx_flush(double2 *f, int64_t fstride, MX xs, int r)
+{
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= xs.V) return;
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    float2 &v = xs.d[((int64_t)k * xs.V + x) * xs.N + r];
+    double2 &o = f[(int64_t)k * fstride + x];
+    o.x += (double)v.x;
+    o.y += (double)v.y;
+    v = make_float2(0.f, 0.f);
+  }
+}
+
+// slot `to` of xs <- slot `from` (zero == 1: <- 0)
+__global__ void k_mx_copy(MX xs, int from, int to, int zero)
+{
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= xs.V) return;
+#pragma unroll
+  for (int k = 0; k < 12; k++)
+    xs.d[((int64_t)k * xs.V + x) * xs.N + to] =
+        zero ? make_float2(0.f, 0.f) : xs.d[((int64_t)k * xs.V + x) * xs.N + from];
 }
 
 // ps = rs + beta ps
@@ -207,7 +213,8 @@ struct BDone {
 struct qcdgpu_batch_s {
   qcdgpu_gauge g;
   int cap, nact;
-  qcdgpu_mfield rs, xs, ps, t, aps;
+  qcdgpu_mfield rs, ps, t, aps;
+  float2 *xs;                  // FP32 solution increments, [12][V][cap]
   qcdgpu_field rt, r, up, bd;  // FP64 work shared by the slots' reliable updates
   double *s;                   // device scalars, (M_HIST + kMChunk) * cap
   float *mp4s, *tms;           // device per-slot diagonal
@@ -215,21 +222,36 @@ struct qcdgpu_batch_s {
   double *hs;                  // pinned host copy of the scalars
   std::vector<qg::BSlot> slots;
   std::vector<qg::BDone> done;
-  bool first;                  // no p update before the next iteration
+  cudaStream_t st;             // the stream the batch's work runs on
+  cudaEvent_t ev;              // end of the launched chunk
+  cudaEvent_t ev_in;           // caller's stream at admission
+  int nchunk;                  // occupied slots of the launched chunk
+  bool use_graphs;
+  bool tuned;                  // the operator variant has been chosen
+  std::vector<cudaGraphExec_t> graphs;  // chunk graph per occupied-slot count
+  std::vector<uint64_t> graph_launches;  // kernels in each graph
 };
 
 namespace qg {
 
+static MX mx(qcdgpu_batch B) { return MX{B->xs, (int)B->g->V, B->cap}; }
+
 static void batch_free(qcdgpu_batch b)
 {
   if (!b) return;
-  for (auto m : {b->rs, b->xs, b->ps, b->t, b->aps}) mfield_free(m);
+  for (auto m : {b->rs, b->ps, b->t, b->aps}) mfield_free(m);
+  cudaFree(b->xs);
   for (auto f : {b->rt, b->r, b->up, b->bd}) field_free(f);
   cudaFree(b->s);
   cudaFree(b->mp4s);
   cudaFree(b->tms);
   cudaFree(b->part);
   cudaFreeHost(b->hs);
+  for (auto e : b->graphs)
+    if (e) cudaGraphExecDestroy(e);
+  if (b->ev) cudaEventDestroy(b->ev);
+  if (b->ev_in) cudaEventDestroy(b->ev_in);
+  if (b->st) cudaStreamDestroy(b->st);
   delete b;
 }
 
@@ -243,9 +265,12 @@ static qcdgpu_batch batch_new(qcdgpu_gauge g, int cap)
   b->g = g;
   b->cap = cap;
   b->nact = 0;
-  b->first = true;
+  b->st = nullptr;
+  b->nchunk = 0;
+  b->use_graphs = true;
+  b->graphs.assign((size_t)cap + 1, nullptr);
+  b->graph_launches.assign((size_t)cap + 1, 0);
   b->rs = mfield_new(g->L, cap);
-  b->xs = mfield_new(g->L, cap);
   b->ps = mfield_new(g->L, cap);
   b->t = mfield_new(g->L, cap);
   b->aps = mfield_new(g->L, cap);
@@ -255,11 +280,16 @@ static qcdgpu_batch batch_new(qcdgpu_gauge g, int cap)
   b->bd = field_new(g->L, QCDGPU_F64);
   size_t ns = (size_t)(M_HIST + kMChunk) * cap;
   unsigned nb = mgrid((int)g->V, cap);
-  bool ok = b->rs && b->xs && b->ps && b->t && b->aps && b->rt && b->r && b->up && b->bd &&
+  if (mrhs_max_blocks(g->V, cap) > nb) nb = mrhs_max_blocks(g->V, cap);
+  bool ok = b->rs && b->ps && b->t && b->aps && b->rt && b->r && b->up && b->bd &&
+            QG_CUDA(cudaMalloc(&b->xs, (size_t)12 * g->V * cap * sizeof(float2))) &&
             QG_CUDA(cudaMalloc(&b->s, ns * sizeof(double))) && QG_CUDA(cudaMalloc(&b->mp4s, cap * sizeof(float))) &&
             QG_CUDA(cudaMalloc(&b->tms, cap * sizeof(float))) &&
             QG_CUDA(cudaMalloc(&b->part, (size_t)nb * cap * sizeof(double))) &&
-            QG_CUDA(cudaMallocHost(&b->hs, ns * sizeof(double)));
+            QG_CUDA(cudaMallocHost(&b->hs, ns * sizeof(double))) &&
+            QG_CUDA(cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming)) &&
+            QG_CUDA(cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming)) &&
+            QG_CUDA(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
   if (!ok) {
     batch_free(b);
     return nullptr;
@@ -299,10 +329,12 @@ static bool set_scalar(qcdgpu_batch B, int slot_kind, int k, double v)
 static bool copy_slot(qcdgpu_batch B, int from, int to)
 {
   unsigned g = (unsigned)((B->g->V + 127) / 128);
-  for (auto m : {B->rs, B->xs, B->ps}) {
+  for (auto m : {B->rs, B->ps}) {
     k_mcopy<<<g, 128, 0, stream()>>>(mv(m), from, to, 0);
     if (!QG_LAUNCHED("mrhs_copy_slot")) return false;
   }
+  k_mx_copy<<<g, 128, 0, stream()>>>(mx(B), from, to, 0);
+  if (!QG_LAUNCHED("mrhs_copy_slot")) return false;
   return QG_CUDA(cudaMemcpyAsync(B->mp4s + to, B->mp4s + from, sizeof(float), cudaMemcpyDeviceToDevice, stream())) &&
          QG_CUDA(cudaMemcpyAsync(B->tms + to, B->tms + from, sizeof(float), cudaMemcpyDeviceToDevice, stream()));
 }
@@ -316,6 +348,9 @@ int batch_add(qcdgpu_batch B, qcdgpu_field x, qcdgpu_field b, double kappa, doub
     return -2;
   }
   if (B->nact >= B->cap) return -1;
+  // the batch's stream starts after the caller's work on x and b
+  if (!QG_CUDA(cudaEventRecord(B->ev_in, stream())) || !QG_CUDA(cudaStreamWaitEvent(B->st, B->ev_in, 0))) return -2;
+  StreamScope scope(B->st);
   BSlot sl;
   sl.tag = tag;
   sl.x = x;
@@ -339,7 +374,7 @@ int batch_add(qcdgpu_batch B, qcdgpu_field x, qcdgpu_field b, double kappa, doub
   sl.maxr = sqrt(rr);
   sl.hint = tol * sl.maxr;
   unsigned g = (unsigned)((B->g->V + 127) / 128);
-  k_mcopy<<<g, 128, 0, stream()>>>(mv(B->xs), 0, k, 1);
+  k_mx_copy<<<g, 128, 0, stream()>>>(mx(B), 0, k, 1);
   if (!QG_LAUNCHED("mrhs_zero_slot")) return -2;
   if (!mfield_set(B->ps, k, B->r)) return -2;
   float mp = (float)sl.mp4, tmf = (float)mu;
@@ -381,9 +416,10 @@ static bool retire(qcdgpu_batch B, int k, int status)
   return QG_CUDA(cudaStreamSynchronize(stream()));
 }
 
-// run up to `iters` iterations (a multiple of the chunk), with reliable
-// updates and retirement at chunk boundaries; returns 0 or 3 on error
-int batch_step(qcdgpu_batch B, int iters)
+// Enqueue one chunk (kMChunk iterations of every occupied slot) and the copy
+// of the per-slot scalars to the host; the chunk is a CUDA graph per number
+// of occupied slots, captured on first use.
+static bool chunk_enqueue(qcdgpu_batch B, int n)
 {
   const int cap = B->cap;
   const int V = (int)B->g->V;
@@ -391,76 +427,132 @@ int batch_step(qcdgpu_batch B, int iters)
   const unsigned nb = mgrid(V, cap);
   const size_t shm = sizeof(double) * blk.x * blk.y;
   cudaStream_t st = stream();
-  for (int done_it = 0; done_it < iters && B->nact > 0; done_it += kMChunk) {
-    const int n = B->nact;
-    for (int j = 0; j < kMChunk; j++) {
-      // p = r + beta p (beta = 0 keeps a fresh slot's p = r)
-      k_mp<<<nb, blk, 0, st>>>(mv(B->ps), mv(B->rs), n, B->s + M_BETA * cap);
-      if (!QG_LAUNCHED("mrhs_p")) return 3;
-      if (!dslash_mrhs(B->t, B->ps, B->g, 4.0, 0.0, false, n, B->mp4s, B->tms)) return 3;
-      if (!dslash_mrhs(B->aps, B->t, B->g, 4.0, 0.0, true, n, B->mp4s, B->tms)) return 3;
-      k_mdot<<<nb, blk, shm, st>>>(mv(B->ps), mv(B->aps), n, B->part);
-      if (!QG_LAUNCHED("mrhs_dot")) return 3;
-      k_mscalars<<<n, 256, 0, st>>>(B->part, (int)nb, cap, B->s, 0, j);
-      if (!QG_LAUNCHED("mrhs_scalars")) return 3;
-      k_mupdate<<<nb, blk, shm, st>>>(mv(B->xs), mv(B->ps), mv(B->rs), mv(B->aps), n, B->s + M_ALPHA * cap, B->part);
-      if (!QG_LAUNCHED("mrhs_update")) return 3;
-      k_mscalars<<<n, 256, 0, st>>>(B->part, (int)nb, cap, B->s, 1, j);
-      if (!QG_LAUNCHED("mrhs_scalars")) return 3;
-    }
-    if (!QG_CUDA(cudaMemcpyAsync(B->hs, B->s, sizeof(double) * (M_HIST + kMChunk) * cap, cudaMemcpyDeviceToHost, st)) ||
-        !QG_CUDA(cudaStreamSynchronize(st)))
-      return 3;
-    std::vector<double> rr_iter(n), beta_iter(n);
-    std::vector<int> need(n, 0), fail(n, 0);
-    for (int k = 0; k < n; k++) {
-      BSlot &sl = B->slots[(size_t)k];
-      rr_iter[k] = B->hs[M_RR * cap + k];
-      beta_iter[k] = B->hs[M_BETA * cap + k];
-      bool update = false, hinted = false;
-      for (int j = 0; j < kMChunk; j++) {
-        double rn = sqrt(B->hs[(M_HIST + j) * cap + k]);
-        if (!(rn == rn)) {
-          fail[k] = 1;
-          break;
-        }
-        sl.iters++;
-        sl.since++;
-        if (rn <= sl.hint) hinted = true;
-        if (rn < sl.delta * sl.maxr) update = true;
-        if (!update && rn > sl.maxr) sl.maxr = rn;
-      }
-      need[k] = fail[k] || update || hinted || sl.iters >= sl.maxiter;
-      if (hinted) sl.hint *= 0.3;
-    }
-    // reliable updates, then retirement from the highest slot down
-    std::vector<int> retire_status(n, -1);
-    for (int k = 0; k < n; k++) {
-      if (!need[k]) continue;
-      BSlot &sl = B->slots[(size_t)k];
-      if (!mfield_get(B->up, B->xs, k) || !blas_axpby(sl.x, 1.0, 0.0, B->up, 1.0, 0.0, sl.x)) return 3;
-      k_mcopy<<<(unsigned)((V + 127) / 128), 128, 0, st>>>(mv(B->xs), 0, k, 1);
-      if (!QG_LAUNCHED("mrhs_zero_slot")) return 3;
-      double rel, rr;
-      if (!slot_residual(B, k, sl, &rel, &rr)) return 3;
-      sl.true_res = rel;
-      sl.updates++;
-      sl.since = 0;
-      if (rel <= sl.tol) {
-        retire_status[k] = 0;
-      } else if (fail[k]) {
-        retire_status[k] = 2;
-      } else if (sl.iters >= sl.maxiter) {
-        retire_status[k] = 1;
-      } else {
-        double bnew = (beta_iter[k] > 0.0 && rr_iter[k] > 0.0) ? rr * beta_iter[k] / rr_iter[k] : 0.0;
-        if (!set_scalar(B, M_RR, k, rr) || !set_scalar(B, M_BETA, k, bnew)) return 3;
-        sl.maxr = sqrt(rr);
-      }
-    }
-    for (int k = n - 1; k >= 0; k--)
-      if (retire_status[k] >= 0 && !retire(B, k, retire_status[k])) return 3;
+  for (int j = 0; j < kMChunk; j++) {
+    // p = r + beta p (beta = 0 keeps a fresh slot's p = r)
+    k_mp<<<nb, blk, 0, st>>>(mv(B->ps), mv(B->rs), n, B->s + M_BETA * cap);
+    if (!QG_LAUNCHED("mrhs_p")) return false;
+    // p^+ D^+ D p = |D p|^2, summed per slot in the first operator's epilogue
+    unsigned nbo = 0;
+    if (!dslash_mrhs(B->t, B->ps, B->g, 4.0, 0.0, false, n, B->mp4s, B->tms, B->part, &nbo)) return false;
+    k_mscalars<<<n, 256, 0, st>>>(B->part, (int)nbo, cap, B->s, 0, j);
+    if (!QG_LAUNCHED("mrhs_scalars")) return false;
+    if (!dslash_mrhs(B->aps, B->t, B->g, 4.0, 0.0, true, n, B->mp4s, B->tms)) return false;
+    k_mupdate<<<nb, blk, shm, st>>>(mx(B), mv(B->ps), mv(B->rs), mv(B->aps), n, B->s + M_ALPHA * cap, B->part);
+    if (!QG_LAUNCHED("mrhs_update")) return false;
+    k_mscalars<<<n, 256, 0, st>>>(B->part, (int)nb, cap, B->s, 1, j);
+    if (!QG_LAUNCHED("mrhs_scalars")) return false;
   }
+  return QG_CUDA(cudaMemcpyAsync(B->hs, B->s, sizeof(double) * (M_HIST + kMChunk) * cap, cudaMemcpyDeviceToHost, st));
+}
+
+bool batch_launch(qcdgpu_batch B)
+{
+  B->nchunk = B->nact;
+  if (B->nchunk == 0) return true;
+  StreamScope scope(B->st);
+  const int n = B->nchunk;
+  if (!gauge_at(B->g, kGaugeF32Full)) return false;  // resident before any capture
+  if (!B->tuned) {
+    // the operator's tuner times its variants outside stream capture; t is
+    // scratch (recomputed by every iteration)
+    if (!dslash_mrhs(B->t, B->ps, B->g, 4.0, 0.0, false, n, B->mp4s, B->tms)) return false;
+    B->tuned = true;
+  }
+  if (B->use_graphs) {
+    cudaGraphExec_t &ex = B->graphs[(size_t)n];
+    if (!ex) {
+      cudaGraph_t graph = nullptr;
+      if (!QG_CUDA(cudaStreamBeginCapture(B->st, cudaStreamCaptureModeThreadLocal))) return false;
+      const uint64_t counted = g_launches.load();
+      bool ok = chunk_enqueue(B, n);
+      cudaError_t e = cudaStreamEndCapture(B->st, &graph);
+      B->graph_launches[(size_t)n] = g_launches.load() - counted;
+      g_launches.store(counted);  // captured, not launched: counted at each graph launch
+      if (!ok || !QG_CUDA(e)) {
+        if (graph) cudaGraphDestroy(graph);
+        return false;
+      }
+      ok = QG_CUDA(cudaGraphInstantiate(&ex, graph, 0));
+      cudaGraphDestroy(graph);
+      if (!ok) {
+        ex = nullptr;
+        return false;
+      }
+    }
+    if (!QG_CUDA(cudaGraphLaunch(ex, B->st))) return false;
+    count_launches(B->graph_launches[(size_t)n]);
+  } else if (!chunk_enqueue(B, n)) {
+    return false;
+  }
+  return QG_CUDA(cudaEventRecord(B->ev, B->st));
+}
+
+// Wait for the launched chunk, then reliable updates and retirement
+bool batch_finish(qcdgpu_batch B)
+{
+  const int n = B->nchunk;
+  B->nchunk = 0;
+  if (n == 0) return true;
+  StreamScope scope(B->st);
+  const int cap = B->cap;
+  const int V = (int)B->g->V;
+  cudaStream_t st = B->st;
+  if (!QG_CUDA(cudaEventSynchronize(B->ev))) return false;
+  std::vector<double> rr_iter(n), beta_iter(n);
+  std::vector<int> need(n, 0), fail(n, 0);
+  for (int k = 0; k < n; k++) {
+    BSlot &sl = B->slots[(size_t)k];
+    rr_iter[k] = B->hs[M_RR * cap + k];
+    beta_iter[k] = B->hs[M_BETA * cap + k];
+    bool update = false, hinted = false;
+    for (int j = 0; j < kMChunk; j++) {
+      double rn = sqrt(B->hs[(M_HIST + j) * cap + k]);
+      if (!(rn == rn)) {
+        fail[k] = 1;
+        break;
+      }
+      sl.iters++;
+      if (rn <= sl.hint) hinted = true;
+      if (rn < sl.delta * sl.maxr) update = true;
+      if (!update && rn > sl.maxr) sl.maxr = rn;
+    }
+    need[k] = fail[k] || update || hinted || sl.iters >= sl.maxiter;
+    if (hinted) sl.hint *= 0.3;
+  }
+  // reliable updates, then retirement from the highest slot down
+  std::vector<int> retire_status(n, -1);
+  for (int k = 0; k < n; k++) {
+    if (!need[k]) continue;
+    BSlot &sl = B->slots[(size_t)k];
+    k_mx_flush<<<(unsigned)((V + 127) / 128), 128, 0, st>>>((double2 *)sl.x->data, sl.x->stride, mx(B), k);
+    if (!QG_LAUNCHED("mrhs_flush_slot")) return false;
+    double rel, rr;
+    if (!slot_residual(B, k, sl, &rel, &rr)) return false;
+    sl.true_res = rel;
+    sl.updates++;
+    if (rel <= sl.tol) {
+      retire_status[k] = 0;
+    } else if (fail[k]) {
+      retire_status[k] = 2;
+    } else if (sl.iters >= sl.maxiter) {
+      retire_status[k] = 1;
+    } else {
+      double bnew = (beta_iter[k] > 0.0 && rr_iter[k] > 0.0) ? rr * beta_iter[k] / rr_iter[k] : 0.0;
+      if (!set_scalar(B, M_RR, k, rr) || !set_scalar(B, M_BETA, k, bnew)) return false;
+      sl.maxr = sqrt(rr);
+    }
+  }
+  for (int k = n - 1; k >= 0; k--)
+    if (retire_status[k] >= 0 && !retire(B, k, retire_status[k])) return false;
+  return true;
+}
+
+// run up to `iters` iterations (whole chunks) with reliable updates and
+// retirement at chunk boundaries; returns 0, or 3 on error
+int batch_step(qcdgpu_batch B, int iters)
+{
+  for (int done_it = 0; done_it < iters && B->nact > 0; done_it += kMChunk)
+    if (!batch_launch(B) || !batch_finish(B)) return 3;
   return 0;
 }
 
@@ -503,7 +595,7 @@ int qcdgpu_batch_poll(qcdgpu_batch b, int *tags, int *status, int *iters, double
 size_t qcdgpu_batch_bytes(qcdgpu_batch b)
 {
   if (!b) return 0;
-  return 5 * b->rs->bytes + 4 * b->rt->bytes;
+  return 4 * b->rs->bytes + (size_t)12 * b->g->V * b->cap * sizeof(float2) + 4 * b->rt->bytes;
 }
 
 }  // extern "C"

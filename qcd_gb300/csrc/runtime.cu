@@ -39,6 +39,12 @@ bool after_launch(const char *what)
 }
 
 cudaStream_t stream() { return g_stream; }
+cudaStream_t swap_stream(cudaStream_t s)
+{
+  cudaStream_t p = g_stream;
+  g_stream = s;
+  return p;
+}
 
 static size_t spinor_bytes(int prec, int64_t stride)
 {

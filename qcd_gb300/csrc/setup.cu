@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "su3.cuh"
 
 namespace qg {
 
@@ -127,14 +128,6 @@ bool field_point(qcdgpu_field f, const int x[4], int spin, int colour)
 }
 
 // -------------------------------------------------------------------- gauge
-__device__ void m3mul(const C<double> a[9], const C<double> b[9], C<double> c[9])
-{
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) c[3 * i + j] = a[3 * i] * b[j] + a[3 * i + 1] * b[3 + j] + a[3 * i + 2] * b[6 + j];
-}
-
 __device__ double sinc_mp(double w)
 {
   if (fabs(w) < 0.05) {
@@ -181,31 +174,6 @@ __device__ void exp_iM(C<double> M[9])
   }
 }
 
-// Gram-Schmidt on columns 0,1 and col2 = conj(col0 x col1)
-__device__ void reunit_cols(C<double> U[9])
-{
-  double n = 0;
-#pragma unroll
-  for (int i = 0; i < 3; i++) n += U[3 * i].re * U[3 * i].re + U[3 * i].im * U[3 * i].im;
-  C<double> w{0, 0};
-#pragma unroll
-  for (int i = 0; i < 3; i++) w = w + cdot(U[3 * i], U[3 * i + 1]);
-  w = (1.0 / n) * w;
-#pragma unroll
-  for (int i = 0; i < 3; i++) U[3 * i + 1] = U[3 * i + 1] - w * U[3 * i];
-  double s = 1.0 / sqrt(n);
-#pragma unroll
-  for (int i = 0; i < 3; i++) U[3 * i] = s * U[3 * i];
-  n = 0;
-#pragma unroll
-  for (int i = 0; i < 3; i++) n += U[3 * i + 1].re * U[3 * i + 1].re + U[3 * i + 1].im * U[3 * i + 1].im;
-  s = 1.0 / sqrt(n);
-#pragma unroll
-  for (int i = 0; i < 3; i++) U[3 * i + 1] = s * U[3 * i + 1];
-  U[2] = conj(U[3] * U[7] - U[6] * U[4]);
-  U[5] = conj(U[6] * U[1] - U[0] * U[7]);
-  U[8] = conj(U[0] * U[4] - U[3] * U[1]);
-}
 
 // writes links in the host layout into aos[(4 site + mu) * 9 + k]
 __global__ void k_gauge_synth(double2 *aos, int64_t V, uint64_t key, double eps)

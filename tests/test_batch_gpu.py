@@ -47,6 +47,7 @@ def test_batch_mixed_kappa_mu_op_each_converges(gpu, orc):
         reqs.append((i, fx, fb, kappa, mu, op, tol))
     batch = q.Batch(g, 8)
     res = _run(batch, reqs)
+    assert q.mrhs_tuned(L, 8) is not None  # the operator variant was tuned before graph capture
     assert sorted(res) == list(range(len(params)))
     for i, (kappa, mu, op, tol) in enumerate(params):
         st, it, tr = res[i]

@@ -1,0 +1,147 @@
+"""Request server: continuous batching over resident gauge fields.
+
+Each request's right-hand sides are checked by their FP64 true residual
+(the oracle's operator on the fetched solution), the HBM budget must hold at
+every round, and a request gives the same solution alone and in a mix, within
+the stated tolerance (relative difference <= 1e-9 for solves to 1e-10)."""
+import numpy as np
+import pytest
+
+import qcd_gb300 as q
+from tests.conftest import EPS_PLAQ_060
+
+pytestmark = pytest.mark.gpu
+TH = (np.pi, 0.0, 0.0, 0.0)
+LA, LB = (16, 8, 8, 8), (8, 8, 8, 8)
+MB = 1 << 20
+
+
+def _drain(srv, budget, on_done=None, max_rounds=5000):
+    """Run rounds until nothing is queued or active; on_done(result) sees each
+    completed request (and may fetch and release it)."""
+    done = {}
+
+    def take():
+        for r in srv.poll():
+            done[r["tag"]] = r
+            if on_done:
+                on_done(r)
+
+    for _ in range(max_rounds):
+        srv.progress()
+        assert srv.stats()["bytes_used"] <= budget
+        take()
+        st = srv.stats()
+        if st["queued"] == 0 and st["active_rhs"] == 0:
+            break
+    take()
+    return done
+
+
+@pytest.fixture(scope="module")
+def gauges(gpu, orc):
+    ua = orc.gauge_synthetic(LA, 21, EPS_PLAQ_060)
+    ub = orc.gauge_synthetic(LB, 22, EPS_PLAQ_060)
+    ga, gb = q.Gauge(LA, TH).load(ua), q.Gauge(LB, TH).load(ub)
+    yield (ua, ga), (ub, gb)
+    ga.close()
+    gb.close()
+
+
+def test_server_stream_of_mixed_requests(gpu, orc, gauges):
+    (ua, ga), (ub, gb) = gauges
+    budget = 64 * MB  # both batches plus a few requests: later ones wait for admission
+    srv = q.Server(budget, slots=8)
+    ia, ib = srv.add_gauge(ga), srv.add_gauge(gb)
+    reqs = [  # (tag, gauge, L, u, nrhs, kappa, mu, op, tol, gaussian sources?)
+        (1, ia, LA, ua, 3, 0.15, 0.0, q.OP_D, 1e-10, True),
+        (2, ib, LB, ub, 2, 0.14, 0.02, q.OP_D, 1e-8, True),
+        (3, ia, LA, ua, 5, 0.145, 0.0, q.OP_Q, 1e-10, False),
+        (4, ib, LB, ub, 4, 0.155, 0.0, q.OP_D, 1e-10, True),
+        (5, ia, LA, ua, 1, 0.15, 0.01, q.OP_D, 1e-10, True),
+        (6, ia, LA, ua, 12, 0.15, 0.0, q.OP_D, 1e-10, False),
+    ]
+    srcs, keep = {}, []
+    for tag, gid, L, u, n, kappa, mu, op, tol, gauss in reqs:
+        sources = None
+        if gauss:
+            arrs = [orc.gaussian_spinor(L, 1000 * tag + c) for c in range(n)]
+            sources = [q.Field(L).load(a) for a in arrs]
+            srcs[tag] = arrs
+            keep += sources
+        srv.submit(gid, n, kappa, mu, op, tol, tag=tag, sources=sources, seed=tag)
+    x = {LA: q.Field(LA), LB: q.Field(LB)}
+    by_tag = {r[0]: r for r in reqs}
+    checked = []
+
+    def check(r):
+        # the budget only admits the 12-RHS request once earlier ones are released
+        tag, gid, L, u, n, kappa, mu, op, tol, gauss = by_tag[r["tag"]]
+        assert r["status"] == 0, r
+        assert r["max_true_residual"] <= tol, r
+        assert 0.0 <= r["queue_s"] <= r["latency_s"]
+        for c in range(n):
+            sol = srv.fetch(tag, c, x[L]).store()
+            opn = "Q" if op == q.OP_Q else "D"
+            if gauss:
+                res = orc.true_residual(sol, srcs[tag][c], u, L, TH, kappa, mu, op=opn)
+            else:  # point source: op x must be a unit vector in one spin-colour entry
+                ox = orc.dslash(sol, u, L, TH, kappa=kappa, tm=mu, op=opn)
+                flat = (ox[..., 0] + 1j * ox[..., 1]).reshape(-1)
+                k = int(np.argmax(np.abs(flat)))
+                assert k % 12 == c % 12
+                b = np.zeros_like(flat)
+                b[k] = 1.0
+                res = np.linalg.norm(flat - b)
+            assert res <= tol, (tag, c, res)
+        srv.release(tag)
+        checked.append(tag)
+
+    done = _drain(srv, budget, check)
+    assert sorted(done) == sorted(by_tag) == sorted(checked)
+    assert done[6]["queue_s"] > 0.0
+    for f in keep + list(x.values()):
+        f.close()
+    srv.close()
+
+
+def test_server_result_same_alone_and_in_mix(gpu, orc, gauges):
+    (ua, ga), (ub, gb) = gauges
+    b = orc.gaussian_spinor(LA, 77)
+    fb = q.Field(LA).load(b)
+    sols = []
+    for mix in (False, True):
+        srv = q.Server(512 * MB, slots=8)
+        ia, ib = srv.add_gauge(ga), srv.add_gauge(gb)
+        if mix:
+            srv.submit(ia, 4, 0.14, tag=10, seed=3)
+            srv.submit(ib, 3, 0.15, 0.01, tag=11, seed=4)
+        srv.submit(ia, 1, 0.15, 0.005, tag=1, sources=[fb])
+        if mix:
+            srv.submit(ia, 6, 0.145, tag=12, seed=5)
+        done = _drain(srv, 512 * MB)
+        assert done[1]["status"] == 0
+        sols.append(srv.fetch(1, 0, q.Field(LA)).store())
+        srv.close()
+    diff = np.linalg.norm(sols[0] - sols[1]) / np.linalg.norm(sols[0])
+    assert diff <= 1e-9, diff
+    fb.close()
+
+
+def test_server_rejects_bad_requests(gpu, gauges):
+    (ua, ga), _ = gauges
+    srv = q.Server(8 * MB, slots=4)
+    gid = srv.add_gauge(ga)
+    with pytest.raises(q.QcdGpuError):
+        srv.submit(gid, 48, 0.15, tag=1)  # more than the whole budget
+    with pytest.raises(q.QcdGpuError):
+        srv.submit(gid + 5, 1, 0.15, tag=2)
+    srv2 = q.Server(512 * MB, slots=4)
+    gid2 = srv2.add_gauge(ga)
+    srv2.submit(gid2, 1, 0.15, tag=3)
+    with pytest.raises(q.QcdGpuError):
+        srv2.submit(gid2, 1, 0.15, tag=3)  # tag in use
+    with pytest.raises(q.QcdGpuError):
+        srv2.release(3)  # not completed yet
+    srv.close()
+    srv2.close()
