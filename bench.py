@@ -219,7 +219,8 @@ def solve_bench(q, orc_check, g, L, n_rhs):
     out = {}
     b, x = q.Field(L), q.Field(L)
     for name, solver, prec in (("fp64_cgnr", q.SOLVER_CGNR, q.F64), ("mixed_cgnr_f16", q.SOLVER_CGNR, q.F16),
-                               ("mixed_cgnr_f32", q.SOLVER_CGNR, q.F32)):
+                               ("mixed_cgnr_f32", q.SOLVER_CGNR, q.F32), ("eo_cgnr_f32", q.SOLVER_CGNR_EO, q.F32),
+                               ("eo_cgnr_f16", q.SOLVER_CGNR_EO, q.F16)):
         lat, iters, res, status = [], [], [], []
         for col in range(n_rhs):
             b.point((0, 0, 0, 0), col // 3, col % 3)
@@ -237,7 +238,7 @@ def solve_bench(q, orc_check, g, L, n_rhs):
                      "p99_ms": 1e3 * lat[min(len(lat) - 1, int(0.99 * len(lat)))], "iters": iters,
                      "max_true_residual": max(res), "status": status}
     if out["fp64_cgnr"]["rhs_solves_per_s"]:
-        for k in ("mixed_cgnr_f16", "mixed_cgnr_f32"):
+        for k in ("mixed_cgnr_f16", "mixed_cgnr_f32", "eo_cgnr_f32", "eo_cgnr_f16"):
             if out[k]["rhs_solves_per_s"]:
                 out["speedup_" + k + "_vs_fp64"] = out[k]["rhs_solves_per_s"] / out["fp64_cgnr"]["rhs_solves_per_s"]
     b.close()
@@ -284,11 +285,13 @@ def precision_bench(q, L, kappa, n_batch, cap):
     out = {"lattice_txyz": list(L), "kappa": kappa, "tol": 1e-10}
     g = q.Gauge(L, THETA).synthetic(2, EPS_PLAQ_060)
     b, x = q.Field(L), q.Field(L)
-    for name, prec in (("fp64_cgnr", q.F64), ("mixed_cgnr_f32", q.F32), ("mixed_cgnr_f16", q.F16)):
+    for name, solver, prec in (("fp64_cgnr", q.SOLVER_CGNR, q.F64), ("mixed_cgnr_f32", q.SOLVER_CGNR, q.F32),
+                               ("mixed_cgnr_f16", q.SOLVER_CGNR, q.F16), ("eo_cgnr_f32", q.SOLVER_CGNR_EO, q.F32),
+                               ("eo_cgnr_f16", q.SOLVER_CGNR_EO, q.F16)):
         b.point((0, 0, 0, 0), 0, 0)
         q.sync()
         t0 = time.perf_counter()
-        p = q.solve(x, b, g, kappa, 0.0, solver=q.SOLVER_CGNR, inner_prec=prec, tol=1e-10, maxiter=40000)
+        p = q.solve(x, b, g, kappa, 0.0, solver=solver, inner_prec=prec, tol=1e-10, maxiter=40000)
         q.sync()
         dt = time.perf_counter() - t0
         out[name] = {"rhs_solves_per_s": 1.0 / dt if p.status == 0 else None, "s_per_solve": dt, "iters": p.iters,
@@ -321,7 +324,7 @@ def precision_bench(q, L, kappa, n_batch, cap):
                            "tuned": q.mrhs_tuned(L, cap)}
     base = out["fp64_cgnr"]["rhs_solves_per_s"]
     if base:
-        for k in ("mixed_cgnr_f32", "mixed_cgnr_f16"):
+        for k in ("mixed_cgnr_f32", "mixed_cgnr_f16", "eo_cgnr_f32", "eo_cgnr_f16"):
             if out[k]["rhs_solves_per_s"]:
                 out["speedup_" + k + "_vs_fp64"] = out[k]["rhs_solves_per_s"] / base
         if out["batched_mrhs"]["rhs_solves_per_s"]:
@@ -442,6 +445,26 @@ def run_only(args):
 
     import qcd_gb300 as q
 
+    if args.only == "batch":
+        # batched multi-RHS solve of point-source columns on the bench lattice
+        g = q.Gauge(L_BENCH, THETA).synthetic(1000, EPS_PLAQ_060)
+        n = args.mrhs_n
+        srcs = [q.Field(L_BENCH).point((0, 0, 0, 0), c % 12 // 3, c % 3) for c in range(n)]
+        xs = [q.Field(L_BENCH) for _ in range(n)]
+        batch = q.Batch(g, n)
+        q.sync()
+        t0 = time.perf_counter()
+        for c in range(n):
+            batch.add(xs[c], srcs[c], KAPPA, 0.0, q.OP_D, tol=1e-10, maxiter=args.steps, tag=c)
+        done = []
+        while batch.active:
+            batch.step(16)
+            done += batch.poll()
+        q.sync()
+        dt = time.perf_counter() - t0
+        return {"only": "batch", "rhs": n, "wall_s": dt, "rhs_solves_per_s": n / dt,
+                "iters": max(d[2] for d in done), "status": sorted({d[1] for d in done}),
+                "max_true_residual": max(d[3] for d in done), "tuned": q.mrhs_tuned(L_BENCH, n)}
     if args.only == "mrhs":
         stream = torch.cuda.current_stream()
         q.set_stream(stream.cuda_stream)
@@ -500,10 +523,10 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=120.0)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-seconds", type=float, default=20.0)
-    ap.add_argument("--mrhs-n", type=int, default=16, help="--only mrhs: RHS per block")
+    ap.add_argument("--mrhs-n", type=int, default=16, help="--only mrhs / batch: RHS per block / batch slots")
     ap.add_argument("--mrhs-variant", type=int, default=-1,
                     help="--only mrhs: -1 tuned, 1 tensor cores, 64/128/256 SIMT block size")
-    ap.add_argument("--only", choices=["f64", "df64", "f32", "f16", "mrhs"],
+    ap.add_argument("--only", choices=["f64", "df64", "f32", "f16", "mrhs", "batch"],
                     help="profiling target: time only this operator variant (a few launches under ncu)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -312,7 +312,10 @@ typedef struct {
 enum {
   QCDGPU_SOLVER_GCR = 0,
   QCDGPU_SOLVER_BICGSTAB = 1,
-  QCDGPU_SOLVER_CGNR = 2
+  QCDGPU_SOLVER_CGNR = 2,
+  /* CGNR on the even/odd (Schur) preconditioned system; the t extent must
+   * be even. Same convergence test on the full true residual. */
+  QCDGPU_SOLVER_CGNR_EO = 3
 };
 /* solve A x = b with A = op(g; kappa, mu); x, b FP64 device fields */
 int qcdgpu_solve(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double kappa, double mu,

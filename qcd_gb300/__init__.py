@@ -27,7 +27,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libqcdgpu.so")
 F64, F32, F16 = 0, 1, 2
 OP_D, OP_Q, OP_DDAG, OP_DDAGD = 0, 1, 2, 3
 ARITH_F64, ARITH_DF64 = 0, 1
-SOLVER_GCR, SOLVER_BICGSTAB, SOLVER_CGNR = 0, 1, 2
+SOLVER_GCR, SOLVER_BICGSTAB, SOLVER_CGNR, SOLVER_CGNR_EO = 0, 1, 2, 3
 
 _u8p = C.POINTER(C.c_uint64)
 

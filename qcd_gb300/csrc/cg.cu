@@ -1,11 +1,14 @@
 // cg.cu -- conjugate gradient on the normal equations D^+ D x = D^+ b with
 // device-resident scalars and reliable updates.
 //
-// One inner iteration is five launches and no host synchronisation:
-//   1. t = D p            (operator kernel; its epilogue also sums |t|^2 =
-//                          p^+ D^+ D p per block)
+// The iteration is written once (cgnr_core) for any system operator A given
+// as kernels: A = D on the full lattice, or the even/odd Schur complement
+// (solve_cgnr_eo). One inner iteration is six launches and no host
+// synchronisation:
+//   1. t = A p            (operator kernel; its epilogue also sums |t|^2 =
+//                          p^+ A^+ A p per block)
 //   2. scalar kernel:     pAp = sum of the block partials, alpha = rr / pAp
-//   3. Ap = D^+ t         (operator kernel)
+//   3. Ap = A^+ t         (operator kernel)
 //   4. update kernel:     x' += alpha p, r -= alpha Ap, per-block |r|^2
 //   5. scalar kernel:     rr' = sum, beta = rr'/rr, history[i] = rr'
 //   6. p = r + beta p     (reads beta from device memory)
@@ -19,7 +22,9 @@
 // Reductions sum block partials in a fixed order, so a solve is
 // deterministic.
 #include <math.h>
+#include <string.h>
 
+#include <functional>
 #include <vector>
 
 #include "dslash_args.h"
@@ -30,7 +35,15 @@ using namespace qgd;
 
 bool dslash_partials(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4, double tm, bool dag,
                      int arith, double *partials);
+bool dslash_eo(qcdgpu_field out, qcdgpu_field in, qcdgpu_field z, qcdgpu_gauge g, double mp4, double tm, bool dag,
+               int par, double ch, bool ainv, int zmode, double *partials);
 double *big_partials(int64_t n);
+
+// even/odd helpers (this file): full FP64 field <-> its two half fields, and
+// out = A in or A^{-1} in on a half field (A = mp4 + i tm g5)
+bool eo_split(qcdgpu_field e, qcdgpu_field o, qcdgpu_field full);
+bool eo_merge(qcdgpu_field full, qcdgpu_field e, qcdgpu_field o);
+bool eo_diag(qcdgpu_field out, qcdgpu_field in, double mp4, double tm, bool inverse);
 
 // scalar slots
 enum { S_RR = 0, S_PAP = 1, S_RRNEW = 2, S_ALPHA = 3, S_BETA = 4, S_HIST = 8 };
@@ -59,12 +72,14 @@ __global__ void __launch_bounds__(128) k_cg_update(void *xs, float *xsn, const v
     Spinor<PX, R>::store(xs, xsn, stride, x, vx);
     Spinor<P, R>::load(rs, rsn, stride, x, vx);
     Spinor<P, R>::load(aps, apsn, stride, x, vp);
+    R s2 = (R)0;  // per-site sum in the working precision, block sum in double
 #pragma unroll
     for (int k = 0; k < 12; k++) {
       vx[k].re = qfma(-alpha, vp[k].re, vx[k].re);
       vx[k].im = qfma(-alpha, vp[k].im, vx[k].im);
-      n2 += (double)vx[k].re * (double)vx[k].re + (double)vx[k].im * (double)vx[k].im;
+      s2 = s2 + vx[k].re * vx[k].re + vx[k].im * vx[k].im;
     }
+    n2 = (double)s2;
     Spinor<P, R>::store(rs, rsn, stride, x, vx);
   }
   block_partial(n2, partials);
@@ -101,7 +116,7 @@ __global__ void __launch_bounds__(128) k_dot_re(const void *a, const float *an, 
     Spinor<P, R>::load(a, an, stride, x, va);
     Spinor<P, R>::load(b, bn, stride, x, vb);
 #pragma unroll
-    for (int k = 0; k < 12; k++) d += (double)va[k].re * (double)vb[k].re + (double)va[k].im * (double)vb[k].im;
+    for (int k = 0; k < 12; k++) d += (double)(va[k].re * vb[k].re + va[k].im * vb[k].im);
   }
   block_partial(d, partials);
 }
@@ -137,41 +152,44 @@ __global__ void k_cg_scalars(const double *partials, int n, double *s, int mode,
     else KERNEL<QCDGPU_F16, float><<<nb, 128, 0, st>>>(__VA_ARGS__);                 \
   } while (0)
 
-// true residual rt = b - D x (FP64 operator), returns |rt| / |b|
-static bool true_res(qcdgpu_field rt, qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, double tm,
-                     double bn, double *rel)
-{
-  if (!dslash(rt, x, g, mp4, tm, QCDGPU_OP_D, -1)) return false;
-  if (!blas_axpby(rt, 1.0, 0.0, b, -1.0, 0.0, rt)) return false;
-  double n2;
-  if (!blas_norm2(rt, &n2)) return false;
-  *rel = bn > 0 ? sqrt(n2) / bn : 0.0;
-  return true;
-}
 
-int solve_cgnr_engine(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, double tm, qcdgpu_solve_params *p)
+// Operators of the system A y = c that cgnr_core solves through A^+ A.
+struct CgOps {
+  int L[4];  // lattice of the system's fields (the half lattice for even/odd)
+  // inner precision: t = A p (with partials: |t|^2 per 128-site block), aps = A^+ t
+  std::function<bool(qcdgpu_field, qcdgpu_field, double *)> op;
+  std::function<bool(qcdgpu_field, qcdgpu_field)> opdag;
+  // FP64 storage (accurate arithmetic): out = A in, out = A^+ in
+  std::function<bool(qcdgpu_field, qcdgpu_field)> op64, opdag64;
+};
+
+struct Held {
+  std::vector<qcdgpu_field> f;
+  ~Held()
+  {
+    for (auto q : f) work_put(q);
+  }
+  qcdgpu_field get(const int L[4], int prec)
+  {
+    qcdgpu_field q = work_get(L, prec);
+    if (q) f.push_back(q);
+    return q;
+  }
+};
+
+// CG on A^+ A y = A^+ c, x0 = 0, chunked with reliable updates; convergence
+// on the true residual |c - A y| / cn (cn: the norm the residual is relative
+// to). Returns 0 converged, 1 maxiter, 2 breakdown, 3 CUDA error.
+static int cgnr_core(qcdgpu_field y, qcdgpu_field c, double cn, const CgOps &ops, qcdgpu_solve_params *p)
 {
-  struct Held {
-    std::vector<qcdgpu_field> f;
-    ~Held()
-    {
-      for (auto q : f) work_put(q);
-    }
-    qcdgpu_field get(const int L[4], int prec)
-    {
-      qcdgpu_field q = work_get(L, prec);
-      if (q) f.push_back(q);
-      return q;
-    }
-  } w;
+  Held w;
   const int prec = p->inner_prec;
-  qcdgpu_gauge gi = gauge_at(g, prec);
-  qcdgpu_field rt = w.get(b->L, QCDGPU_F64), r = w.get(b->L, QCDGPU_F64), up = w.get(b->L, QCDGPU_F64);
-  qcdgpu_field rs = w.get(b->L, prec), ps = w.get(b->L, prec);
-  qcdgpu_field xs = w.get(b->L, prec == QCDGPU_F16 ? QCDGPU_F32 : prec);
-  qcdgpu_field t = w.get(b->L, prec), aps = w.get(b->L, prec);
-  if (!gi || !rt || !r || !up || !rs || !xs || !ps || !t || !aps) return 3;
-  const int V = (int)b->V;
+  qcdgpu_field rt = w.get(ops.L, QCDGPU_F64), r = w.get(ops.L, QCDGPU_F64), up = w.get(ops.L, QCDGPU_F64);
+  qcdgpu_field rs = w.get(ops.L, prec), ps = w.get(ops.L, prec);
+  qcdgpu_field xs = w.get(ops.L, prec == QCDGPU_F16 ? QCDGPU_F32 : prec);
+  qcdgpu_field t = w.get(ops.L, prec), aps = w.get(ops.L, prec);
+  if (!rt || !r || !up || !rs || !xs || !ps || !t || !aps) return 3;
+  const int V = (int)rt->V;
   const unsigned nb = (unsigned)((V + 127) / 128);
   double *part = big_partials(nb);
   double *s = reduce_scratch();
@@ -179,45 +197,34 @@ int solve_cgnr_engine(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4
   if (!part || !s || !h) return 3;
   s += 2 * kMaxPartials + 16;  // 16 + kChunk slots past the blas result words
   cudaStream_t st = stream();
-
-  double bn2;
-  if (!blas_norm2(b, &bn2)) return 3;
-  double bn = sqrt(bn2);
-  p->iters = 0;
-  p->reliable_updates = 0;
-  p->true_residual = 1.0;
-  if (!blas_zero(x)) return 3;
-  if (bn == 0.0) {
-    p->true_residual = 0.0;
-    return 0;
-  }
-  // the system matrix is D (op D) or Q = i g5 D (op Q): Q^+ Q = D^+ D and
-  // Q x = b <=> D x = -i g5 b, so both run the D^+ D iteration
-  qcdgpu_field bd = b;
-  if (p->op == QCDGPU_OP_Q) {
-    bd = w.get(b->L, QCDGPU_F64);
-    if (!bd || !blas_ig5(bd, b) || !blas_axpby(bd, -1.0, 0.0, bd, 0.0, 0.0, bd)) return 3;
-  }
-  if (!blas_copy(rt, bd)) return 3;
+  if (!blas_zero(y)) return 3;
+  // true residual rt = c - A y (FP64), returns |rt| / cn
+  auto true_res = [&](double *rel) -> bool {
+    if (!ops.op64(rt, y) || !blas_axpby(rt, 1.0, 0.0, c, -1.0, 0.0, rt)) return false;
+    double n2;
+    if (!blas_norm2(rt, &n2)) return false;
+    *rel = sqrt(n2) / cn;
+    return true;
+  };
+  // r = A^+ rt, rs = r (storage precision), s[RR] = |r|^2
   auto restart_residual = [&](double *rr_out) -> bool {
-    // r = D^+ rt, rs = r (storage precision), s[RR] = |r|^2
-    if (!dslash(r, rt, g, mp4, tm, QCDGPU_OP_DDAG, -1)) return false;
+    if (!ops.opdag64(r, rt)) return false;
     double rr;
     if (!blas_norm2(r, &rr)) return false;
     if (!convert_field(rs, r)) return false;
-    if (!QG_CUDA(cudaMemcpyAsync(s + S_RR, &rr, sizeof(double), cudaMemcpyHostToDevice, st))) return false;
+    h[0] = rr;
+    if (!QG_CUDA(cudaMemcpyAsync(s + S_RR, h, sizeof(double), cudaMemcpyHostToDevice, st))) return false;
+    if (!QG_CUDA(cudaStreamSynchronize(st))) return false;
     *rr_out = rr;
     return true;
   };
+  if (!blas_copy(rt, c)) return 3;
   double rr;
   if (!restart_residual(&rr)) return 3;
   if (!blas_copy(ps, rs) || !blas_zero(xs)) return 3;
-  // the scalar upload above reads host memory asynchronously: wait for it
-  if (!QG_CUDA(cudaStreamSynchronize(st))) return 3;
   double maxr = sqrt(rr), hint = p->tol * maxr;
   bool first = true;
   const double delta = p->delta > 0 ? p->delta : 0.1;
-  const int arith = -1;
   int since_update = 0;
   while (true) {
     int chunk = kChunk;
@@ -231,14 +238,13 @@ int solve_cgnr_engine(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4
       }
       first = false;
       if (prec != QCDGPU_F16) {
-        // p^+ A p = |D p|^2 summed in the epilogue of the first operator
-        if (!dslash_partials(t, ps, gi, mp4, tm, false, arith, part)) return 3;
+        // p^+ A^+ A p = |A p|^2 summed in the epilogue of the first operator
+        if (!ops.op(t, ps, part)) return 3;
         k_cg_scalars<<<1, 256, 0, st>>>(part, (int)nb, s, 0, j);
         if (!QG_LAUNCHED("cg_scalars")) return 3;
-        if (!dslash_partials(aps, t, gi, mp4, tm, true, arith, nullptr)) return 3;
+        if (!ops.opdag(aps, t)) return 3;
       } else {
-        if (!dslash_partials(t, ps, gi, mp4, tm, false, arith, nullptr)) return 3;
-        if (!dslash_partials(aps, t, gi, mp4, tm, true, arith, nullptr)) return 3;
+        if (!ops.op(t, ps, nullptr) || !ops.opdag(aps, t)) return 3;
         k_dot_re<QCDGPU_F16, float><<<nb, 128, 0, st>>>(ps->data, ps->norm, aps->data, aps->norm, ps->stride, V, part);
         if (!QG_LAUNCHED("cg_dot")) return 3;
         k_cg_scalars<<<1, 256, 0, st>>>(part, (int)nb, s, 0, j);
@@ -270,13 +276,13 @@ int solve_cgnr_engine(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4
     bool last = p->iters >= p->maxiter;
     if (update || hinted || last) {
       if (prec == QCDGPU_F64) {
-        if (!blas_axpby(x, 1.0, 0.0, xs, 1.0, 0.0, x)) return 3;
+        if (!blas_axpby(y, 1.0, 0.0, xs, 1.0, 0.0, y)) return 3;
       } else {
-        if (!convert_field(up, xs) || !blas_axpby(x, 1.0, 0.0, up, 1.0, 0.0, x)) return 3;
+        if (!convert_field(up, xs) || !blas_axpby(y, 1.0, 0.0, up, 1.0, 0.0, y)) return 3;
       }
       if (!blas_zero(xs)) return 3;
       double rel;
-      if (!true_res(rt, x, bd, g, mp4, tm, bn, &rel)) return 3;
+      if (!true_res(&rel)) return 3;
       p->true_residual = rel;
       p->reliable_updates++;
       since_update = 0;
@@ -293,6 +299,219 @@ int solve_cgnr_engine(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4
       maxr = sqrt(rr);
     }
   }
+}
+
+// b as seen by D: Q x = b <=> D x = -i g5 b (Q^+ Q = D^+ D)
+static qcdgpu_field system_rhs(Held &w, qcdgpu_field b, int op)
+{
+  if (op != QCDGPU_OP_Q) return b;
+  qcdgpu_field bd = w.get(b->L, QCDGPU_F64);
+  if (!bd || !blas_ig5(bd, b) || !blas_axpby(bd, -1.0, 0.0, bd, 0.0, 0.0, bd)) return nullptr;
+  return bd;
+}
+
+int solve_cgnr_engine(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, double tm, qcdgpu_solve_params *p)
+{
+  Held w;
+  p->iters = 0;
+  p->reliable_updates = 0;
+  p->true_residual = 1.0;
+  double bn2;
+  if (!blas_norm2(b, &bn2)) return 3;
+  if (bn2 == 0.0) {
+    p->true_residual = 0.0;
+    return blas_zero(x) ? 0 : 3;
+  }
+  qcdgpu_field bd = system_rhs(w, b, p->op);
+  qcdgpu_gauge gi = gauge_at(g, p->inner_prec);
+  if (!bd || !gi) return 3;
+  CgOps ops;
+  memcpy(ops.L, b->L, sizeof(ops.L));
+  ops.op = [&](qcdgpu_field o, qcdgpu_field i, double *part) {
+    return dslash_partials(o, i, gi, mp4, tm, false, -1, part);
+  };
+  ops.opdag = [&](qcdgpu_field o, qcdgpu_field i) { return dslash_partials(o, i, gi, mp4, tm, true, -1, nullptr); };
+  ops.op64 = [&](qcdgpu_field o, qcdgpu_field i) { return dslash(o, i, g, mp4, tm, QCDGPU_OP_D, QCDGPU_ARITH_DF64); };
+  ops.opdag64 = [&](qcdgpu_field o, qcdgpu_field i) {
+    return dslash(o, i, g, mp4, tm, QCDGPU_OP_DDAG, QCDGPU_ARITH_DF64);
+  };
+  return cgnr_core(x, bd, sqrt(bn2), ops, p);
+}
+
+// Even/odd preconditioned CGNR. With D = A - H/2 (A = m+4 + i tm g5 on each
+// site, H the hopping term) in even/odd blocks, x_o = A^{-1} (b_o + H_oe x_e / 2)
+// and the even sites solve the Schur complement
+//   M x_e = b_e + H_eo A^{-1} b_o / 2,   M = A - H_eo A^{-1} H_oe / 4,
+// whose residual equals the full residual b - D x (its odd part vanishes).
+// M is applied as two half-lattice kernels: t_o = A^{-1} H_oe x_e, then
+// A x_e - H_eo t_o / 4 (with |M x_e|^2 summed in the second epilogue).
+int solve_cgnr_eo(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, double tm, qcdgpu_solve_params *p)
+{
+  if (b->L[0] % 2 != 0) {
+    set_error("even/odd solve: the t extent must be even");
+    return 3;
+  }
+  Held w;
+  p->iters = 0;
+  p->reliable_updates = 0;
+  p->true_residual = 1.0;
+  double bn2;
+  if (!blas_norm2(b, &bn2)) return 3;
+  if (bn2 == 0.0) {
+    p->true_residual = 0.0;
+    return blas_zero(x) ? 0 : 3;
+  }
+  const int prec = p->inner_prec;
+  qcdgpu_field bd = system_rhs(w, b, p->op);
+  qcdgpu_gauge gi = gauge_at(g, prec);
+  const int Lh[4] = {b->L[0] / 2, b->L[1], b->L[2], b->L[3]};
+  qcdgpu_field be = w.get(Lh, QCDGPU_F64), bo = w.get(Lh, QCDGPU_F64), to = w.get(Lh, QCDGPU_F64);
+  qcdgpu_field ce = w.get(Lh, QCDGPU_F64), xe = w.get(Lh, QCDGPU_F64), xo = w.get(Lh, QCDGPU_F64);
+  qcdgpu_field ti = w.get(Lh, prec), t64 = w.get(Lh, QCDGPU_F64);  // odd intermediates
+  if (!bd || !gi || !be || !bo || !to || !ce || !xe || !xo || !ti || !t64) return 3;
+  // c_e = b_e + H_eo A^{-1} b_o / 2
+  if (!eo_split(be, bo, bd) || !eo_diag(to, bo, mp4, tm, true)) return 3;
+  if (!dslash_eo(ce, to, be, g, mp4, tm, false, 0, 0.5, false, 1, nullptr)) return 3;
+  CgOps ops;
+  memcpy(ops.L, Lh, sizeof(ops.L));
+  ops.op = [&](qcdgpu_field o, qcdgpu_field i, double *part) {
+    return dslash_eo(ti, i, nullptr, gi, mp4, tm, false, 1, 1.0, true, 0, nullptr) &&
+           dslash_eo(o, ti, i, gi, mp4, tm, false, 0, -0.25, false, 2, part);
+  };
+  ops.opdag = [&](qcdgpu_field o, qcdgpu_field i) {
+    return dslash_eo(ti, i, nullptr, gi, mp4, tm, true, 1, 1.0, true, 0, nullptr) &&
+           dslash_eo(o, ti, i, gi, mp4, tm, true, 0, -0.25, false, 2, nullptr);
+  };
+  ops.op64 = [&](qcdgpu_field o, qcdgpu_field i) {
+    return dslash_eo(t64, i, nullptr, g, mp4, tm, false, 1, 1.0, true, 0, nullptr) &&
+           dslash_eo(o, t64, i, g, mp4, tm, false, 0, -0.25, false, 2, nullptr);
+  };
+  ops.opdag64 = [&](qcdgpu_field o, qcdgpu_field i) {
+    return dslash_eo(t64, i, nullptr, g, mp4, tm, true, 1, 1.0, true, 0, nullptr) &&
+           dslash_eo(o, t64, i, g, mp4, tm, true, 0, -0.25, false, 2, nullptr);
+  };
+  const int st = cgnr_core(xe, ce, sqrt(bn2), ops, p);
+  if (st == 3) return 3;
+  // x_o = A^{-1} b_o + A^{-1} H_oe x_e / 2, then the full true residual
+  if (!dslash_eo(xo, xe, to, g, mp4, tm, false, 1, 0.5, true, 1, nullptr) || !eo_merge(x, xe, xo)) return 3;
+  qcdgpu_field rt = w.get(b->L, QCDGPU_F64);
+  double r2;
+  if (!rt || !dslash(rt, x, g, mp4, tm, QCDGPU_OP_D, QCDGPU_ARITH_DF64) ||
+      !blas_axpby(rt, 1.0, 0.0, bd, -1.0, 0.0, rt) || !blas_norm2(rt, &r2))
+    return 3;
+  p->true_residual = sqrt(r2 / bn2);
+  return st == 0 && p->true_residual > p->tol ? 1 : st;
+}
+
+}  // namespace qg
+
+// ------------------------------------------------------------ even/odd helpers
+namespace qg {
+
+// t-row parity trick: sites 2e and 2e + 1 of the full lattice have opposite
+// parities (even t extent); the one of parity `par` goes to index e
+__device__ __forceinline__ int eo_site(const Geom &g, int e, int par)
+{
+  int c[4];
+  coords(g, 2 * e, c);
+  return 2 * e + ((par ^ c[1] ^ c[2] ^ c[3]) & 1);
+}
+
+__global__ void k_eo_split(double2 *e, double2 *o, int64_t hstride, const double2 *f, int64_t fstride, Geom g, int Vh)
+{
+  const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (i >= Vh) return;
+  const int xe = eo_site(g, i, 0), xo = eo_site(g, i, 1);
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    e[k * hstride + i] = f[k * fstride + xe];
+    o[k * hstride + i] = f[k * fstride + xo];
+  }
+}
+
+__global__ void k_eo_merge(double2 *f, int64_t fstride, const double2 *e, const double2 *o, int64_t hstride, Geom g,
+                           int Vh)
+{
+  const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (i >= Vh) return;
+  const int xe = eo_site(g, i, 0), xo = eo_site(g, i, 1);
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    f[k * fstride + xe] = e[k * hstride + i];
+    f[k * fstride + xo] = o[k * hstride + i];
+  }
+}
+
+// out = (ar + i ai g5) in
+__global__ void k_eo_diag(double2 *out, const double2 *in, int64_t stride, int Vh, double ar, double ai)
+{
+  const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (i >= Vh) return;
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    const double2 v = in[k * stride + i];
+    const double g = k < 6 ? ai : -ai;
+    out[k * stride + i] = make_double2(ar * v.x - g * v.y, ar * v.y + g * v.x);
+  }
+}
+
+static Geom full_geom(const int L[4])
+{
+  Geom g;
+  for (int i = 0; i < 4; i++) g.L[i] = L[i];
+  g.st[0] = 1;
+  g.st[1] = L[0];
+  g.st[2] = L[0] * L[1];
+  g.st[3] = L[0] * L[1] * L[2];
+  return g;
+}
+
+static bool halves_of(qcdgpu_field e, qcdgpu_field o, qcdgpu_field full)
+{
+  if (e->prec != QCDGPU_F64 || o->prec != QCDGPU_F64 || full->prec != QCDGPU_F64 || !same_shape(e, o) ||
+      full->L[0] % 2 != 0 || e->L[0] * 2 != full->L[0] || e->L[1] != full->L[1] || e->L[2] != full->L[2] ||
+      e->L[3] != full->L[3]) {
+    set_error("even/odd split: FP64 half fields of the full field's lattice");
+    return false;
+  }
+  return true;
+}
+
+bool eo_split(qcdgpu_field e, qcdgpu_field o, qcdgpu_field full)
+{
+  if (!halves_of(e, o, full)) return false;
+  const int Vh = (int)e->V;
+  k_eo_split<<<(unsigned)((Vh + 127) / 128), 128, 0, stream()>>>((double2 *)e->data, (double2 *)o->data, e->stride,
+                                                                  (const double2 *)full->data, full->stride,
+                                                                  full_geom(full->L), Vh);
+  return QG_LAUNCHED("eo_split");
+}
+
+bool eo_merge(qcdgpu_field full, qcdgpu_field e, qcdgpu_field o)
+{
+  if (!halves_of(e, o, full)) return false;
+  const int Vh = (int)e->V;
+  k_eo_merge<<<(unsigned)((Vh + 127) / 128), 128, 0, stream()>>>((double2 *)full->data, full->stride,
+                                                                  (const double2 *)e->data, (const double2 *)o->data,
+                                                                  e->stride, full_geom(full->L), Vh);
+  return QG_LAUNCHED("eo_merge");
+}
+
+bool eo_diag(qcdgpu_field out, qcdgpu_field in, double mp4, double tm, bool inverse)
+{
+  if (out->prec != QCDGPU_F64 || in->prec != QCDGPU_F64 || !same_shape(out, in)) {
+    set_error("even/odd diagonal: FP64 fields of one shape");
+    return false;
+  }
+  double ar = mp4, ai = tm;
+  if (inverse) {
+    const double den = mp4 * mp4 + tm * tm;
+    ar = mp4 / den;
+    ai = -tm / den;
+  }
+  k_eo_diag<<<(unsigned)((in->V + 127) / 128), 128, 0, stream()>>>((double2 *)out->data, (const double2 *)in->data,
+                                                                    in->stride, (int)in->V, ar, ai);
+  return QG_LAUNCHED("eo_diag");
 }
 
 }  // namespace qg

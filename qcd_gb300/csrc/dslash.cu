@@ -120,6 +120,82 @@ bool dslash(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4, doubl
   }
 }
 
+// Even/odd kernel on half fields (FP64, FP32 or FP16 with a gauge field of
+// the same precision): out (parity par) = ch * [A^{-1}] H in + {0 | z | A z}
+// with A = mp4 + i tm g5 (D^+: tm -> -tm and the hopping term of D^+).
+// in, out, z are fields on the half lattice {L_t / 2, L_x, L_y, L_z}.
+bool dslash_eo(qcdgpu_field out, qcdgpu_field in, qcdgpu_field z, qcdgpu_gauge g, double mp4, double tm, bool dag,
+               int par, double ch, bool ainv, int zmode, double *partials)
+{
+  if (!out || !in || !g || out == in || (zmode && (!z || z == out)) || in->prec != out->prec ||
+      in->prec != g->prec || (z && z->prec != in->prec) || g->L[0] % 2 != 0 || in->L[0] * 2 != g->L[0] ||
+      in->L[1] != g->L[1] || in->L[2] != g->L[2] || in->L[3] != g->L[3] || !same_shape(out, in) ||
+      (z && !same_shape(z, in))) {
+    set_error("even/odd operator: half fields of one precision on the gauge field's half lattice");
+    return false;
+  }
+  DArgs a;
+  a.partials = partials;
+  a.out = out->data;
+  a.out_norm = out->norm;
+  a.in = in->data;
+  a.in_norm = in->norm;
+  a.z = z ? z->data : nullptr;
+  a.z_norm = z ? z->norm : nullptr;
+  a.gauge = g->data;
+  for (int i = 0; i < 4; i++) a.geo.L[i] = g->L[i];
+  a.geo.st[0] = 1;
+  a.geo.st[1] = g->L[0];
+  a.geo.st[2] = g->L[0] * g->L[1];
+  a.geo.st[3] = g->L[0] * g->L[1] * g->L[2];
+  a.V = (int)in->V;
+  a.stride = in->stride;
+  a.gstride = g->stride;
+  a.twist_mask = 0;
+  for (int mu = 0; mu < 4; mu++) {
+    a.phr[mu] = 1.0;
+    a.phi[mu] = 0.0;
+    if (g->theta[mu] != 0.0) {
+      a.twist_mask |= 1 << mu;
+      a.phr[mu] = cos(g->theta[mu] / (double)g->L[mu]);
+      a.phi[mu] = sin(g->theta[mu] / (double)g->L[mu]);
+    }
+    split_host(a.phr[mu], &a.phr_h[mu], &a.phr_l[mu]);
+    split_host(a.phi[mu], &a.phi_h[mu], &a.phi_l[mu]);
+  }
+  a.mp4 = mp4;
+  a.tm = dag ? -tm : tm;
+  a.op_q = 0;
+  a.eo_par = par;
+  a.zmode = zmode;
+  a.ainv = ainv ? 1 : 0;
+  a.ch = ch;
+  const double den = a.mp4 * a.mp4 + a.tm * a.tm;
+  a.ai_r = a.mp4 / den;
+  a.ai_i = -a.tm / den;
+  split_host(a.mp4, &a.mp4_h, &a.mp4_l);
+  split_host(a.tm, &a.tm_h, &a.tm_l);
+  split_host(a.ch, &a.ch_h, &a.ch_l);
+  split_host(a.ai_r, &a.ai_r_h, &a.ai_r_l);
+  split_host(a.ai_i, &a.ai_i_h, &a.ai_i_l);
+  const unsigned grid = (unsigned)((a.V + 127) / 128);
+  cudaStream_t s = stream();
+#define QG_EO(SP, RECON, R)                                                        \
+  if (dag) k_wilson_eo<true, SP, SP, RECON, R><<<grid, 128, 0, s>>>(a);            \
+  else k_wilson_eo<false, SP, SP, RECON, R><<<grid, 128, 0, s>>>(a);
+  if (in->prec == QCDGPU_F64) {
+    QG_EO(QCDGPU_F64, 18, double)
+  } else if (in->prec == QCDGPU_F32 && g->recon == 12) {
+    QG_EO(QCDGPU_F32, 12, float)
+  } else if (in->prec == QCDGPU_F32) {
+    QG_EO(QCDGPU_F32, 18, float)
+  } else {
+    QG_EO(QCDGPU_F16, 12, float)
+  }
+#undef QG_EO
+  return QG_LAUNCHED("wilson_eo");
+}
+
 // out = D in (dag: D^+ in) on fields checked by the caller; when partials is
 // non-null, block b of the launch (128 sites each) also writes the sum of
 // |out|^2 over its sites to partials[b]

@@ -22,6 +22,17 @@ struct DArgs {
   int twist_mask;
   int op_q;          // multiply the result by i g5
   double *partials;  // non-null: block b writes sum over its sites of |out|^2 to partials[b]
+  // even/odd kernels (k_wilson_eo): the sites of parity eo_par only, V = half
+  // volume; in, out and z are half fields indexed by (full site index) >> 1
+  // (t extent even). out = ch * [A^{-1}] H in + {0 | z | A z}, with
+  // A = mp4 + i tm g5 and H the hopping sum of the operator.
+  int eo_par;
+  const void *z;
+  const float *z_norm;
+  int zmode;  // 0: no addend, 1: + z, 2: + A z
+  int ainv;   // 1: hopping term multiplied by A^{-1}
+  double ch, ai_r, ai_i;  // A^{-1} = ai_r + i ai_i g5
+  float ch_h, ch_l, ai_r_h, ai_r_l, ai_i_h, ai_i_l;
 };
 
 // |v|^2 summed over the block into partials[blockIdx.x]; every thread of the

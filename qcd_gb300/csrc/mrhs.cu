@@ -47,7 +47,7 @@ struct MArgs {
 
 __device__ __forceinline__ float2 mload(const __half2 *d, const float *nrm, int V, int N, int k, int site, int r)
 {
-  float2 f = __half22float2(d[((int64_t)k * V + site) * N + r]);
+  float2 f = __half22float2(d[mhalf2_index(V, N, k, site, r)]);
   float s = nrm[(int64_t)site * N + r];
   return make_float2(f.x * s, f.y * s);
 }
@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(128) k_wilson_mrhs(const MArgs a)
 #pragma unroll
         for (int nt = 0; nt < 3; nt++) {
           const int q = 4 * nt + t;
-          a.out[((int64_t)q * a.V + x) * a.N + r] = __floats2half2_rn(o[nt].x * inv, o[nt].y * inv);
+          a.out[mhalf2_index(a.V, a.N, q, x, r)] = __floats2half2_rn(o[nt].x * inv, o[nt].y * inv);
         }
         if (t == 0) a.out_norm[(int64_t)x * a.N + r] = mx;
       }
@@ -233,20 +233,15 @@ __device__ __forceinline__ void mload_rp(const MArgs &a, int y, int r0, C<float>
     const float2 n2 = *(const float2 *)(a.in_norm + (int64_t)y * a.N + r0);
     nrm[0] = n2.x;
     nrm[RP - 1] = n2.y;
-#pragma unroll
-    for (int k = 0; k < 12; k++) {
-      const uint2 w = *(const uint2 *)(a.in + ((int64_t)k * a.V + y) * a.N + r0);
-      const float2 f0 = __half22float2(*(const __half2 *)&w.x), f1 = __half22float2(*(const __half2 *)&w.y);
-      s[0][k] = C<float>{f0.x, f0.y};
-      s[RP - 1][k] = C<float>{f1.x, f1.y};
-    }
   } else {
     nrm[0] = a.in_norm[(int64_t)y * a.N + r0];
+  }
 #pragma unroll
-    for (int k = 0; k < 12; k++) {
-      const float2 f = __half22float2(a.in[((int64_t)k * a.V + y) * a.N + r0]);
-      s[0][k] = C<float>{f.x, f.y};
-    }
+  for (int q = 0; q < RP; q++) {
+    float2 v[12];
+    mload_raw(a.in, a.V, a.N, y, r0 + q, v);
+#pragma unroll
+    for (int k = 0; k < 12; k++) s[q][k] = C<float>{v[k].x, v[k].y};
   }
 }
 
@@ -327,16 +322,20 @@ __global__ void __launch_bounds__(256) k_wilson_mrhs_simt(const MArgs a, double 
       if (!(mx >= 1.17549435e-38f)) mx = 0.f;
       const float inv = mx > 0.f ? 1.0f / mx : 0.f;
       if (r < a.nact) {
+        float2 o[12];
 #pragma unroll
-        for (int k = 0; k < 12; k++) {
-          const __half2 h = __floats2half2_rn(acc[q][k].re * inv, acc[q][k].im * inv);
-          a.out[((int64_t)k * a.V + x) * a.N + r] = h;
-          if (partials) {
-            const float2 f = __half22float2(h);
-            n2[q] += (double)(f.x * mx) * (f.x * mx) + (double)(f.y * mx) * (f.y * mx);
+        for (int k = 0; k < 12; k++) o[k] = make_float2(acc[q][k].re, acc[q][k].im);
+        mstore_raw(a.out, a.V, a.N, x, r, o, inv);
+        float s2 = 0.f;
+        if (partials) {  // |out|^2 of the stored (rounded) values
+#pragma unroll
+          for (int k = 0; k < 12; k++) {
+            const float2 f = __half22float2(__floats2half2_rn(o[k].x * inv, o[k].y * inv));
+            s2 += f.x * f.x + f.y * f.y;
           }
         }
         a.out_norm[(int64_t)x * a.N + r] = mx;
+        n2[q] = (double)(s2 * mx * mx);  // per-site sum in FP32, block sum in double
       }
     }
   }
@@ -405,8 +404,10 @@ __global__ void k_pack(__half2 *d, float *dn, int V, int N, int r, const void *f
   for (int k = 0; k < 12; k++) mx = fmaxf(mx, fmaxf(fabsf(s[k].re), fabsf(s[k].im)));
   if (!(mx >= 1.17549435e-38f)) mx = 0.f;
   float inv = mx > 0.f ? 1.0f / mx : 0.f;
+  float2 v[12];
 #pragma unroll
-  for (int k = 0; k < 12; k++) d[((int64_t)k * V + x) * N + r] = __floats2half2_rn(s[k].re * inv, s[k].im * inv);
+  for (int k = 0; k < 12; k++) v[k] = make_float2(s[k].re, s[k].im);
+  mstore_raw(d, V, N, x, r, v, inv);
   dn[(int64_t)x * N + r] = mx;
 }
 
@@ -464,11 +465,13 @@ __global__ void k_mnorm(const __half2 *d, const float *dn, int V, int N, int nac
   double n2 = 0.0;
   if (r < nact && x < V) {
     const float s = dn[(int64_t)x * N + r];
+    float s2 = 0.f;  // per-site sum in FP32, block sum in double
 #pragma unroll
     for (int k = 0; k < 12; k++) {
-      float2 f = __half22float2(d[((int64_t)k * V + x) * N + r]);
-      n2 += (double)(f.x * s) * (f.x * s) + (double)(f.y * s) * (f.y * s);
+      float2 f = __half22float2(d[mhalf2_index(V, N, k, x, r)]);
+      s2 += (f.x * s) * (f.x * s) + (f.y * s) * (f.y * s);
     }
+    n2 = (double)s2;
   }
   extern __shared__ double sh[];
   const int y = threadIdx.y;

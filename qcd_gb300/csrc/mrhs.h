@@ -4,9 +4,12 @@
 
 #include "internal.h"
 
-// N spinors in FP16 with one float norm per (site, RHS), laid out
-// [component 0..11][site][rhs] as half2 (re, im): the RHS of one site and
-// component are contiguous
+// N spinors in FP16 with one float norm per (site, RHS). The 12 complex
+// components of a spinor form three groups of four; group j of slot r at
+// site x is one 16-byte word (8 halves: re, im of components 4j..4j+3) at
+// uint4 index (j * V + x) * N + r. A thread reads a whole spinor with three
+// 128-bit loads, and the threads of consecutive (site, slot) pairs read
+// consecutive words. Norms are [site][slot] floats.
 struct qcdgpu_mfield_s {
   int L[4];
   int64_t V;
@@ -17,6 +20,44 @@ struct qcdgpu_mfield_s {
 };
 
 namespace qg {
+
+// spinor (x, r) of a multi-RHS field as 12 float2 (without the norm)
+__device__ __forceinline__ void mload_raw(const __half2 *d, int64_t V, int N, int x, int r, float2 v[12])
+{
+  const uint4 *p = (const uint4 *)d;
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const uint4 w = p[((int64_t)j * V + x) * N + r];
+    v[4 * j + 0] = __half22float2(*(const __half2 *)&w.x);
+    v[4 * j + 1] = __half22float2(*(const __half2 *)&w.y);
+    v[4 * j + 2] = __half22float2(*(const __half2 *)&w.z);
+    v[4 * j + 3] = __half22float2(*(const __half2 *)&w.w);
+  }
+}
+
+// spinor (x, r) <- 12 float2 multiplied by inv, rounded to FP16
+__device__ __forceinline__ void mstore_raw(__half2 *d, int64_t V, int N, int x, int r, const float2 v[12], float inv)
+{
+  uint4 *p = (uint4 *)d;
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    __half2 h[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) h[i] = __floats2half2_rn(v[4 * j + i].x * inv, v[4 * j + i].y * inv);
+    uint4 w;
+    w.x = *(const unsigned *)&h[0];
+    w.y = *(const unsigned *)&h[1];
+    w.z = *(const unsigned *)&h[2];
+    w.w = *(const unsigned *)&h[3];
+    p[((int64_t)j * V + x) * N + r] = w;
+  }
+}
+
+// component k of spinor (x, r) as one half2
+__device__ __forceinline__ int64_t mhalf2_index(int64_t V, int N, int k, int x, int r)
+{
+  return (((int64_t)(k >> 2) * V + x) * N + r) * 4 + (k & 3);
+}
 
 qcdgpu_mfield mfield_new(const int L[4], int N);
 void mfield_free(qcdgpu_mfield m);

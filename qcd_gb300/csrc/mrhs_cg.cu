@@ -39,11 +39,9 @@ static MV mv(qcdgpu_mfield m) { return MV{(__half2 *)m->data, m->norm, (int)m->V
 __device__ __forceinline__ void mv_load(const MV &m, int x, int r, float2 v[12])
 {
   const float s = m.n[(int64_t)x * m.N + r];
+  mload_raw(m.d, m.V, m.N, x, r, v);
 #pragma unroll
-  for (int k = 0; k < 12; k++) {
-    float2 f = __half22float2(m.d[((int64_t)k * m.V + x) * m.N + r]);
-    v[k] = make_float2(f.x * s, f.y * s);
-  }
+  for (int k = 0; k < 12; k++) v[k] = make_float2(v[k].x * s, v[k].y * s);
 }
 __device__ __forceinline__ void mv_store(const MV &m, int x, int r, const float2 v[12])
 {
@@ -52,8 +50,7 @@ __device__ __forceinline__ void mv_store(const MV &m, int x, int r, const float2
   for (int k = 0; k < 12; k++) mx = fmaxf(mx, fmaxf(fabsf(v[k].x), fabsf(v[k].y)));
   if (!(mx >= 1.17549435e-38f)) mx = 0.f;
   const float inv = mx > 0.f ? 1.0f / mx : 0.f;
-#pragma unroll
-  for (int k = 0; k < 12; k++) m.d[((int64_t)k * m.V + x) * m.N + r] = __floats2half2_rn(v[k].x * inv, v[k].y * inv);
+  mstore_raw(m.d, m.V, m.N, x, r, v, inv);
   m.n[(int64_t)x * m.N + r] = mx;
 }
 
@@ -77,10 +74,11 @@ __device__ __forceinline__ void slot_partial(double v, double *partials)
   }
 }
 
-// FP32 solution increments of the slots, [component][site][slot] float2:
-// FP16 would round every increment to 11 bits and cost iterations
+// FP32 solution increments of the slots: components 2j, 2j+1 of slot r at
+// site x form the float4 at index (j * V + x) * N + r, j = 0..5. FP16 would
+// round every increment to 11 bits and cost iterations.
 struct MX {
-  float2 *d;
+  float4 *d;
   int V, N;
 };
 
@@ -94,19 +92,22 @@ __global__ void k_mupdate(MX xs, MV ps, MV rs, MV aps, int nact, const double *a
     float2 a[12], b[12];
     mv_load(ps, x, r, b);
 #pragma unroll
-    for (int k = 0; k < 12; k++) {
-      float2 &v = xs.d[((int64_t)k * xs.V + x) * xs.N + r];
-      float2 w = v;
-      v = make_float2(__fmaf_rn(al, b[k].x, w.x), __fmaf_rn(al, b[k].y, w.y));
+    for (int j = 0; j < 6; j++) {
+      float4 &v = xs.d[((int64_t)j * xs.V + x) * xs.N + r];
+      const float4 w = v;
+      v = make_float4(__fmaf_rn(al, b[2 * j].x, w.x), __fmaf_rn(al, b[2 * j].y, w.y),
+                      __fmaf_rn(al, b[2 * j + 1].x, w.z), __fmaf_rn(al, b[2 * j + 1].y, w.w));
     }
     mv_load(rs, x, r, a);
     mv_load(aps, x, r, b);
+    float s2 = 0.f;  // per-site sum in FP32, block sum in double
 #pragma unroll
     for (int k = 0; k < 12; k++) {
       a[k] = make_float2(__fmaf_rn(-al, b[k].x, a[k].x), __fmaf_rn(-al, b[k].y, a[k].y));
-      n2 += (double)a[k].x * a[k].x + (double)a[k].y * a[k].y;
+      s2 += a[k].x * a[k].x + a[k].y * a[k].y;
     }
     mv_store(rs, x, r, a);
+    n2 = (double)s2;
   }
   slot_partial(n2, partials);
 }
@@ -117,12 +118,16 @@ __global__ void k_mx_flush(double2 *f, int64_t fstride, MX xs, int r)
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= xs.V) return;
 #pragma unroll
-  for (int k = 0; k < 12; k++) {
-    float2 &v = xs.d[((int64_t)k * xs.V + x) * xs.N + r];
-    double2 &o = f[(int64_t)k * fstride + x];
-    o.x += (double)v.x;
-    o.y += (double)v.y;
-    v = make_float2(0.f, 0.f);
+  for (int j = 0; j < 6; j++) {
+    float4 &v = xs.d[((int64_t)j * xs.V + x) * xs.N + r];
+    double2 &o0 = f[(int64_t)(2 * j) * fstride + x];
+    double2 &o1 = f[(int64_t)(2 * j + 1) * fstride + x];
+    const float4 w = v;
+    o0.x += (double)w.x;
+    o0.y += (double)w.y;
+    o1.x += (double)w.z;
+    o1.y += (double)w.w;
+    v = make_float4(0.f, 0.f, 0.f, 0.f);
   }
 }
 
@@ -132,9 +137,9 @@ __global__ void k_mx_copy(MX xs, int from, int to, int zero)
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= xs.V) return;
 #pragma unroll
-  for (int k = 0; k < 12; k++)
-    xs.d[((int64_t)k * xs.V + x) * xs.N + to] =
-        zero ? make_float2(0.f, 0.f) : xs.d[((int64_t)k * xs.V + x) * xs.N + from];
+  for (int j = 0; j < 6; j++)
+    xs.d[((int64_t)j * xs.V + x) * xs.N + to] =
+        zero ? make_float4(0.f, 0.f, 0.f, 0.f) : xs.d[((int64_t)j * xs.V + x) * xs.N + from];
 }
 
 // ps = rs + beta ps
@@ -156,9 +161,10 @@ __global__ void k_mcopy(MV m, int from, int to, int zero)
 {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= m.V) return;
+  uint4 *p = (uint4 *)m.d;
 #pragma unroll
-  for (int k = 0; k < 12; k++)
-    m.d[((int64_t)k * m.V + x) * m.N + to] = zero ? __floats2half2_rn(0.f, 0.f) : m.d[((int64_t)k * m.V + x) * m.N + from];
+  for (int j = 0; j < 3; j++)
+    p[((int64_t)j * m.V + x) * m.N + to] = zero ? make_uint4(0u, 0u, 0u, 0u) : p[((int64_t)j * m.V + x) * m.N + from];
   m.n[(int64_t)x * m.N + to] = zero ? 0.f : m.n[(int64_t)x * m.N + from];
 }
 
@@ -214,7 +220,7 @@ struct qcdgpu_batch_s {
   qcdgpu_gauge g;
   int cap, nact;
   qcdgpu_mfield rs, ps, t, aps;
-  float2 *xs;                  // FP32 solution increments, [12][V][cap]
+  float4 *xs;                  // FP32 solution increments (layout of MX)
   qcdgpu_field rt, r, up, bd;  // FP64 work shared by the slots' reliable updates
   double *s;                   // device scalars, (M_HIST + kMChunk) * cap
   float *mp4s, *tms;           // device per-slot diagonal
@@ -308,12 +314,12 @@ static bool slot_bd(qcdgpu_batch B, const BSlot &sl)
 static bool slot_residual(qcdgpu_batch B, int k, const BSlot &sl, double *rel, double *rr)
 {
   if (!slot_bd(B, sl)) return false;
-  if (!dslash(B->rt, sl.x, B->g, sl.mp4, sl.tm, QCDGPU_OP_D, -1)) return false;
+  if (!dslash(B->rt, sl.x, B->g, sl.mp4, sl.tm, QCDGPU_OP_D, QCDGPU_ARITH_DF64)) return false;
   if (!blas_axpby(B->rt, 1.0, 0.0, B->bd, -1.0, 0.0, B->rt)) return false;
   double n2;
   if (!blas_norm2(B->rt, &n2)) return false;
   *rel = sl.bn > 0 ? sqrt(n2) / sl.bn : 0.0;
-  if (!dslash(B->r, B->rt, B->g, sl.mp4, sl.tm, QCDGPU_OP_DDAG, -1)) return false;
+  if (!dslash(B->r, B->rt, B->g, sl.mp4, sl.tm, QCDGPU_OP_DDAG, QCDGPU_ARITH_DF64)) return false;
   if (!blas_norm2(B->r, rr)) return false;
   return mfield_set(B->rs, k, B->r);
 }

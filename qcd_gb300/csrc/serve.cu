@@ -4,8 +4,9 @@
 // Scheduling round (qcdgpu_server_progress):
 //   1. admission: requests are admitted strictly in arrival order while the
 //      head's bytes (FP64 x and b per RHS, plus its gauge field's batch when
-//      that is not yet built) fit in the budget; admission allocates and
-//      fills the request's fields;
+//      that is not yet built) fit in the budget -- idle batches of other
+//      gauge fields are freed to make room; admission allocates and fills
+//      the request's fields;
 //   2. slot filling: each gauge field's pending RHS (admitted requests in
 //      order, columns in order) enter its batch while slots are free;
 //   3. iteration: one chunk is launched on every busy batch -- each on its
@@ -169,7 +170,18 @@ int progress(qcdgpu_server S)
     SrvRequest &r = S->reqs[S->queue.front()];
     SrvGauge &G = S->gauges[(size_t)r.gauge];
     size_t need = r.bytes + (G.batch ? 0 : batch_bytes_est(G.g->L, S->slots));
-    if (S->used + need > S->budget) break;
+    if (S->used + need > S->budget) {
+      // free the batches of idle gauge fields (no RHS in or waiting for
+      // them): they are rebuilt when a request for them is admitted again
+      for (SrvGauge &O : S->gauges)
+        if (&O != &G && O.batch && O.pending.empty() && qcdgpu_batch_active(O.batch) == 0) {
+          collect(S, O);
+          S->used -= qcdgpu_batch_bytes(O.batch);
+          qcdgpu_batch_destroy(O.batch);
+          O.batch = nullptr;
+        }
+      if (S->used + need > S->budget) break;
+    }
     if (!admit(S, r)) {
       free_request_fields(r);
       return 3;

@@ -63,7 +63,7 @@ __device__ __forceinline__ void accumulate(C<R> acc[12], const C<R> h[6])
   }
 }
 
-template <int MU, bool DAG, int SP, int GP, int RECON, typename R>
+template <int MU, bool DAG, int SP, int GP, int RECON, typename R, bool EO = false>
 __device__ __forceinline__ void hop_pair(const DArgs &a, int x, const int c[4], C<R> acc[12])
 {
   constexpr int SF = DAG ? +1 : -1;  // projector sign of the forward hop
@@ -71,7 +71,7 @@ __device__ __forceinline__ void hop_pair(const DArgs &a, int x, const int c[4], 
   {
     int y = fwd(a.geo, x, c, MU);
     C<R> s[12], h[6], uh[6], U[9];
-    Spinor<SP, R>::load(a.in, a.in_norm, a.stride, y, s);
+    Spinor<SP, R>::load(a.in, a.in_norm, a.stride, EO ? (y >> 1) : y, s);
     project<MU, SF>(s, h);
     Link<GP, RECON, R>::load(a.gauge, a.gstride, x, MU, U);
 #pragma unroll
@@ -89,7 +89,7 @@ __device__ __forceinline__ void hop_pair(const DArgs &a, int x, const int c[4], 
   {
     int y = bwd(a.geo, x, c, MU);
     C<R> s[12], h[6], uh[6], U[9];
-    Spinor<SP, R>::load(a.in, a.in_norm, a.stride, y, s);
+    Spinor<SP, R>::load(a.in, a.in_norm, a.stride, EO ? (y >> 1) : y, s);
     project<MU, -SF>(s, h);
     Link<GP, RECON, R>::load(a.gauge, a.gstride, y, MU, U);
 #pragma unroll
@@ -138,7 +138,71 @@ __global__ void __launch_bounds__(128) k_wilson(const DArgs a)
     Spinor<SP, R>::store(a.out, a.out_norm, a.stride, x, acc);
     if (a.partials) {
 #pragma unroll
-      for (int k = 0; k < 12; k++) n2 += (double)acc[k].re * (double)acc[k].re + (double)acc[k].im * (double)acc[k].im;
+      // per-site sum in the working precision (FP64 arithmetic is scarce on
+      // this part); the block sum is double
+      R s2 = acc[0].re * acc[0].re + acc[0].im * acc[0].im;
+#pragma unroll
+      for (int k = 1; k < 12; k++) s2 = s2 + acc[k].re * acc[k].re + acc[k].im * acc[k].im;
+      n2 = (double)s2;
+    }
+  }
+  if (a.partials) block_partial(n2, a.partials);
+}
+
+// Even/odd kernel: thread e handles the site of parity a.eo_par whose full
+// index is 2e or 2e + 1 (the t extent is even, so the two sites 2e, 2e + 1
+// of a t-row have opposite parities); neighbours are read from the half
+// field of the other parity at (full index) >> 1.
+template <bool DAG, int SP, int GP, int RECON, typename R>
+__global__ void __launch_bounds__(128) k_wilson_eo(const DArgs a)
+{
+  const int e = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  double n2 = 0.0;
+  if (e < a.V) {
+    int c[4];
+    coords(a.geo, 2 * e, c);
+    const int b = (a.eo_par ^ c[1] ^ c[2] ^ c[3]) & 1;
+    const int x = 2 * e + b;
+    c[0] += b;
+    C<R> acc[12];
+    const R zero = Scalar<R>::get(0.0, 0.0f, 0.0f);
+#pragma unroll
+    for (int k = 0; k < 12; k++) acc[k] = C<R>{zero, zero};
+    hop_pair<0, DAG, SP, GP, RECON, R, true>(a, x, c, acc);
+    hop_pair<1, DAG, SP, GP, RECON, R, true>(a, x, c, acc);
+    hop_pair<2, DAG, SP, GP, RECON, R, true>(a, x, c, acc);
+    hop_pair<3, DAG, SP, GP, RECON, R, true>(a, x, c, acc);
+    const R ch = Scalar<R>::get(a.ch, a.ch_h, a.ch_l);
+    if (a.ainv) {
+      const R ar = Scalar<R>::get(a.ai_r, a.ai_r_h, a.ai_r_l), ai = Scalar<R>::get(a.ai_i, a.ai_i_h, a.ai_i_l);
+#pragma unroll
+      for (int k = 0; k < 12; k++) {
+        const R g5ai = k < 6 ? ai : -ai;
+        acc[k] = C<R>{ar * acc[k].re - g5ai * acc[k].im, ar * acc[k].im + g5ai * acc[k].re};
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 12; k++) acc[k] = C<R>{ch * acc[k].re, ch * acc[k].im};
+    if (a.zmode) {
+      C<R> s[12];
+      Spinor<SP, R>::load(a.z, a.z_norm, a.stride, e, s);
+      if (a.zmode == 2) {
+        const R mp4 = Scalar<R>::get(a.mp4, a.mp4_h, a.mp4_l), tm = Scalar<R>::get(a.tm, a.tm_h, a.tm_l);
+#pragma unroll
+        for (int k = 0; k < 12; k++) {
+          const R g5tm = k < 6 ? tm : -tm;
+          s[k] = C<R>{mp4 * s[k].re - g5tm * s[k].im, mp4 * s[k].im + g5tm * s[k].re};
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 12; k++) acc[k] = acc[k] + s[k];
+    }
+    Spinor<SP, R>::store(a.out, a.out_norm, a.stride, e, acc);
+    if (a.partials) {
+      R s2 = acc[0].re * acc[0].re + acc[0].im * acc[0].im;
+#pragma unroll
+      for (int k = 1; k < 12; k++) s2 = s2 + acc[k].re * acc[k].re + acc[k].im * acc[k].im;
+      n2 = (double)s2;
     }
   }
   if (a.partials) block_partial(n2, a.partials);

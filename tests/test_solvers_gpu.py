@@ -91,10 +91,12 @@ def test_bicgstab_dropin_converges_where_bicgstab_does(gpu, orc):
 
 
 @pytest.mark.parametrize("solver,prec", [(q.SOLVER_CGNR, q.F64), (q.SOLVER_CGNR, q.F32), (q.SOLVER_CGNR, q.F16),
-                                         (q.SOLVER_BICGSTAB, q.F32), (q.SOLVER_GCR, q.F64)])
+                                         (q.SOLVER_CGNR_EO, q.F64), (q.SOLVER_CGNR_EO, q.F32),
+                                         (q.SOLVER_CGNR_EO, q.F16), (q.SOLVER_BICGSTAB, q.F32),
+                                         (q.SOLVER_GCR, q.F64)])
 def test_device_solver_true_residual(gpu, orc, solver, prec):
     L = (16, 8, 8, 8)
-    kappa = 0.15 if solver == q.SOLVER_CGNR else 0.12
+    kappa = 0.15 if solver in (q.SOLVER_CGNR, q.SOLVER_CGNR_EO) else 0.12
     u = orc.gauge_synthetic(L, 4, EPS_PLAQ_060)
     b = orc.gaussian_spinor(L, 5)
     g = q.Gauge(L, TH).load(u)
@@ -130,3 +132,26 @@ def test_mixed_precision_cgnr_matches_fp64_solution(gpu, orc):
         assert np.linalg.norm(xs[prec] - xs[q.F64]) / np.linalg.norm(xs[q.F64]) <= 1e-9
     g.close()
     fb.close()
+
+
+@pytest.mark.parametrize("op", [q.OP_D, q.OP_Q])
+def test_even_odd_solve_matches_full_solve(gpu, orc, op):
+    """The Schur-complement solve gives the full system's solution: the same x
+    as the unpreconditioned CGNR within the solve tolerance, with twisted mass
+    and theta phases in two directions."""
+    L = (8, 8, 4, 6)
+    th = (np.pi, 0.0, 0.4, 0.0)
+    u = orc.gauge_synthetic(L, 8, EPS_PLAQ_060)
+    b = orc.gaussian_spinor(L, 9)
+    g = q.Gauge(L, th).load(u)
+    fb, x0, x1 = q.Field(L).load(b), q.Field(L), q.Field(L)
+    p0 = q.solve(x0, fb, g, 0.15, 0.03, solver=q.SOLVER_CGNR, op=op, inner_prec=q.F64, tol=1e-12)
+    p1 = q.solve(x1, fb, g, 0.15, 0.03, solver=q.SOLVER_CGNR_EO, op=op, inner_prec=q.F32, tol=1e-12)
+    assert p0.status == 0 and p1.status == 0, (p0.status, p1.status)
+    opn = "Q" if op == q.OP_Q else "D"
+    assert orc.true_residual(x1.store(), b, u, L, th, 0.15, 0.03, op=opn) <= 1e-12
+    a0, a1 = x0.store(), x1.store()
+    assert np.linalg.norm(a1 - a0) / np.linalg.norm(a0) <= 1e-9
+    assert p1.iters < p0.iters
+    for f in (g, fb, x0, x1):
+        f.close()
