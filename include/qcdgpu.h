@@ -380,6 +380,10 @@ int qcdgpu_mrhs_tuned(const int L[4], int nrhs, int *variant, int *threads);
  * reaches tol and new right-hand sides enter free slots between steps. */
 typedef struct qcdgpu_batch_s *qcdgpu_batch;
 int qcdgpu_batch_create(qcdgpu_batch *b, qcdgpu_gauge g, int capacity);
+/* the same, solving each system through its even/odd Schur complement on
+ * the half lattice (t extent even): fewer iterations, same FP64 true
+ * residual test; each slot holds three more FP64 half-lattice fields */
+int qcdgpu_batch_create_eo(qcdgpu_batch *b, qcdgpu_gauge g, int capacity);
 int qcdgpu_batch_destroy(qcdgpu_batch b);
 /* Solve op x = rhs (op QCDGPU_OP_D or QCDGPU_OP_Q; x, rhs FP64 fields that
  * stay owned by the caller and untouched by it until polled). maxiter <= 0:

@@ -192,6 +192,7 @@ def lib() -> C.CDLL:
     L.qcdgpu_server_release.argtypes = [C.c_void_p, C.c_int]
     L.qcdgpu_server_stats.argtypes = [C.c_void_p, C.POINTER(C.c_size_t), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.qcdgpu_batch_create.argtypes = [vpp, C.c_void_p, C.c_int]
+    L.qcdgpu_batch_create_eo.argtypes = [vpp, C.c_void_p, C.c_int]
     L.qcdgpu_batch_destroy.argtypes = [C.c_void_p]
     L.qcdgpu_batch_add.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_double,
                                    C.c_int, C.c_double, C.c_int]
@@ -477,10 +478,12 @@ def dslash_mrhs(out: MField, inp: MField, g: Gauge, kappa: float, mu: float = 0.
 class Batch:
     """Batched multi-RHS solver with continuous admission (qcdgpu_batch)."""
 
-    def __init__(self, g: Gauge, capacity: int):
+    def __init__(self, g: Gauge, capacity: int, eo: bool = False):
+        """eo: solve each system through its even/odd Schur complement."""
         self.h = C.c_void_p()
         self.capacity = capacity
-        _check(lib().qcdgpu_batch_create(C.byref(self.h), g.h, capacity), "qcdgpu_batch_create")
+        create = lib().qcdgpu_batch_create_eo if eo else lib().qcdgpu_batch_create
+        _check(create(C.byref(self.h), g.h, capacity), "qcdgpu_batch_create")
 
     def add(self, x: Field, b: Field, kappa: float, mu: float = 0.0, op: int = OP_D, tol: float = 1e-10,
             maxiter: int = 0, delta: float = 0.1, tag: int = 0) -> int:

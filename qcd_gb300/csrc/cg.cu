@@ -35,15 +35,7 @@ using namespace qgd;
 
 bool dslash_partials(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4, double tm, bool dag,
                      int arith, double *partials);
-bool dslash_eo(qcdgpu_field out, qcdgpu_field in, qcdgpu_field z, qcdgpu_gauge g, double mp4, double tm, bool dag,
-               int par, double ch, bool ainv, int zmode, double *partials);
 double *big_partials(int64_t n);
-
-// even/odd helpers (this file): full FP64 field <-> its two half fields, and
-// out = A in or A^{-1} in on a half field (A = mp4 + i tm g5)
-bool eo_split(qcdgpu_field e, qcdgpu_field o, qcdgpu_field full);
-bool eo_merge(qcdgpu_field full, qcdgpu_field e, qcdgpu_field o);
-bool eo_diag(qcdgpu_field out, qcdgpu_field in, double mp4, double tm, bool inverse);
 
 // scalar slots
 enum { S_RR = 0, S_PAP = 1, S_RRNEW = 2, S_ALPHA = 3, S_BETA = 4, S_HIST = 8 };
@@ -161,6 +153,10 @@ struct CgOps {
   std::function<bool(qcdgpu_field, qcdgpu_field)> opdag;
   // FP64 storage (accurate arithmetic): out = A in, out = A^+ in
   std::function<bool(qcdgpu_field, qcdgpu_field)> op64, opdag64;
+  // optional: rs = A^+ rt in the inner precision with |rs|^2 (instead of
+  // opdag64 + conversion): the true residual rt is FP64-accurate, and its
+  // image only seeds the low-precision iteration
+  std::function<bool(qcdgpu_field, qcdgpu_field, double *)> restart;
 };
 
 struct Held {
@@ -208,10 +204,12 @@ static int cgnr_core(qcdgpu_field y, qcdgpu_field c, double cn, const CgOps &ops
   };
   // r = A^+ rt, rs = r (storage precision), s[RR] = |r|^2
   auto restart_residual = [&](double *rr_out) -> bool {
-    if (!ops.opdag64(r, rt)) return false;
     double rr;
-    if (!blas_norm2(r, &rr)) return false;
-    if (!convert_field(rs, r)) return false;
+    if (ops.restart) {
+      if (!ops.restart(rs, rt, &rr)) return false;
+    } else if (!ops.opdag64(r, rt) || !blas_norm2(r, &rr) || !convert_field(rs, r)) {
+      return false;
+    }
     h[0] = rr;
     if (!QG_CUDA(cudaMemcpyAsync(s + S_RR, h, sizeof(double), cudaMemcpyHostToDevice, st))) return false;
     if (!QG_CUDA(cudaStreamSynchronize(st))) return false;
@@ -368,7 +366,8 @@ int solve_cgnr_eo(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, do
   qcdgpu_field be = w.get(Lh, QCDGPU_F64), bo = w.get(Lh, QCDGPU_F64), to = w.get(Lh, QCDGPU_F64);
   qcdgpu_field ce = w.get(Lh, QCDGPU_F64), xe = w.get(Lh, QCDGPU_F64), xo = w.get(Lh, QCDGPU_F64);
   qcdgpu_field ti = w.get(Lh, prec), t64 = w.get(Lh, QCDGPU_F64);  // odd intermediates
-  if (!bd || !gi || !be || !bo || !to || !ce || !xe || !xo || !ti || !t64) return 3;
+  qcdgpu_field tin = w.get(Lh, prec);
+  if (!bd || !gi || !be || !bo || !to || !ce || !xe || !xo || !ti || !t64 || !tin) return 3;
   // c_e = b_e + H_eo A^{-1} b_o / 2
   if (!eo_split(be, bo, bd) || !eo_diag(to, bo, mp4, tm, true)) return 3;
   if (!dslash_eo(ce, to, be, g, mp4, tm, false, 0, 0.5, false, 1, nullptr)) return 3;
@@ -390,6 +389,10 @@ int solve_cgnr_eo(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, do
     return dslash_eo(t64, i, nullptr, g, mp4, tm, true, 1, 1.0, true, 0, nullptr) &&
            dslash_eo(o, t64, i, g, mp4, tm, true, 0, -0.25, false, 2, nullptr);
   };
+  if (prec != QCDGPU_F64)
+    ops.restart = [&](qcdgpu_field rs, qcdgpu_field rt, double *rr) {
+      return convert_field(tin, rt) && ops.opdag(rs, tin) && blas_norm2(rs, rr);
+    };
   const int st = cgnr_core(xe, ce, sqrt(bn2), ops, p);
   if (st == 3) return 3;
   // x_o = A^{-1} b_o + A^{-1} H_oe x_e / 2, then the full true residual

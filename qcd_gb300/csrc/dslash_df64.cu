@@ -191,7 +191,7 @@ __device__ __forceinline__ CF coef(CF z, bool ifl, bool ng)
 constexpr int kFFSites = 128;
 
 template <bool DAG>
-__global__ void __launch_bounds__(384) k_wilson_ff(const DArgs a)
+__global__ void __launch_bounds__(384, 3) k_wilson_ff(const DArgs a)
 {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int grp = w / 3, col = w - 3 * grp;

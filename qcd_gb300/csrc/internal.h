@@ -121,6 +121,16 @@ bool pack_gauge(qcdgpu_gauge g, const void *dev_aos);
 // dslash.cu: out = op(in) with diagonal mp4 = m + 4 and twisted mass tm
 bool dslash(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4, double tm, int op,
             int arith);
+// even/odd kernel on half fields {L_t/2, L_x, L_y, L_z} (native arithmetic):
+// out (parity par) = ch * [A^{-1}] H in + {0 | z | A z}, A = mp4 + i tm g5
+bool dslash_eo(qcdgpu_field out, qcdgpu_field in, qcdgpu_field z, qcdgpu_gauge g, double mp4, double tm, bool dag,
+               int par, double ch, bool ainv, int zmode, double *partials);
+
+// cg.cu: even/odd helpers -- full FP64 field <-> its two half fields, and
+// out = A in or A^{-1} in on a half field (A = mp4 + i tm g5)
+bool eo_split(qcdgpu_field e, qcdgpu_field o, qcdgpu_field full);
+bool eo_merge(qcdgpu_field full, qcdgpu_field e, qcdgpu_field o);
+bool eo_diag(qcdgpu_field out, qcdgpu_field in, double mp4, double tm, bool inverse);
 
 // blas.cu (all precisions; arithmetic in the storage's working precision,
 // reductions accumulated in double)

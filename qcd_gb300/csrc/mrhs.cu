@@ -43,6 +43,14 @@ struct MArgs {
   // per-slot diagonal (m+4 and tm of each RHS) when non-null; the hopping
   // term does not depend on kappa or mu, so one batch may mix both
   const float *mp4s, *tms;
+  // SIMT kernel epilogue: out = ch * [A^{-1}] H in + {0 | z | A z} with A the
+  // slot's diagonal (m+4) + i tm g5; the full-lattice operator is ch = -1/2,
+  // z = in, zmode 2. Even/odd kernels: sites of parity eo_par, fields on the
+  // half lattice (V = half volume) indexed by (full site index) >> 1.
+  const __half2 *z;
+  const float *z_norm;
+  int zmode, ainv, eo_par;
+  float ch;
 };
 
 __device__ __forceinline__ float2 mload(const __half2 *d, const float *nrm, int V, int N, int k, int site, int r)
@@ -227,25 +235,26 @@ __global__ void __launch_bounds__(128) k_wilson_mrhs(const MArgs a)
 // epilogue also writes, per block and slot, the sum of |out|^2 over the
 // block's sites (partials[block * N + slot]) in a fixed order.
 template <int RP>
-__device__ __forceinline__ void mload_rp(const MArgs &a, int y, int r0, C<float> s[RP][12], float nrm[RP])
+__device__ __forceinline__ void mload_rp(const MArgs &a, const __half2 *d, const float *dn, int y, int r0,
+                                         C<float> s[RP][12], float nrm[RP])
 {
   if (RP == 2) {
-    const float2 n2 = *(const float2 *)(a.in_norm + (int64_t)y * a.N + r0);
+    const float2 n2 = *(const float2 *)(dn + (int64_t)y * a.N + r0);
     nrm[0] = n2.x;
     nrm[RP - 1] = n2.y;
   } else {
-    nrm[0] = a.in_norm[(int64_t)y * a.N + r0];
+    nrm[0] = dn[(int64_t)y * a.N + r0];
   }
 #pragma unroll
   for (int q = 0; q < RP; q++) {
     float2 v[12];
-    mload_raw(a.in, a.V, a.N, y, r0 + q, v);
+    mload_raw(d, a.V, a.N, y, r0 + q, v);
 #pragma unroll
     for (int k = 0; k < 12; k++) s[q][k] = C<float>{v[k].x, v[k].y};
   }
 }
 
-template <int MU, bool DAG, int RP>
+template <int MU, bool DAG, int RP, bool EO>
 __device__ __forceinline__ void mhop_pair(const MArgs &a, int x, const int c[4], int r0, C<float> acc[RP][12])
 {
   constexpr int SF = DAG ? +1 : -1;
@@ -256,7 +265,7 @@ __device__ __forceinline__ void mhop_pair(const MArgs &a, int x, const int c[4],
     const int y = back ? bwd(a.geo, x, c, MU) : fwd(a.geo, x, c, MU);
     C<float> s[RP][12], U[9];
     float nrm[RP];
-    mload_rp<RP>(a, y, r0, s, nrm);
+    mload_rp<RP>(a, a.in, a.in_norm, EO ? (y >> 1) : y, r0, s, nrm);
     Link<QCDGPU_F32, 18, float>::load(a.gauge, a.gstride, back ? y : x, MU, U);
 #pragma unroll
     for (int q = 0; q < RP; q++) {
@@ -282,41 +291,59 @@ __device__ __forceinline__ void mhop_pair(const MArgs &a, int x, const int c[4],
   }
 }
 
-template <bool DAG, int RP>
+template <bool DAG, int RP, bool EO>
 __global__ void __launch_bounds__(256) k_wilson_mrhs_simt(const MArgs a, double *partials)
 {
   const int r0 = threadIdx.x * RP;
-  const int x = blockIdx.x * blockDim.y + threadIdx.y;
+  const int e = blockIdx.x * blockDim.y + threadIdx.y;  // output index
   double n2[RP];
 #pragma unroll
   for (int q = 0; q < RP; q++) n2[q] = 0.0;
-  if (r0 < a.nact && x < a.V) {
-    int c[4];
-    coords(a.geo, x, c);
+  if (r0 < a.nact && e < a.V) {
+    int c[4], x = e;
+    if (EO) {  // the site of parity eo_par among full indices 2e, 2e + 1 (even t extent)
+      coords(a.geo, 2 * e, c);
+      const int b = (a.eo_par ^ c[1] ^ c[2] ^ c[3]) & 1;
+      x = 2 * e + b;
+      c[0] += b;
+    } else {
+      coords(a.geo, x, c);
+    }
     C<float> acc[RP][12];
 #pragma unroll
     for (int q = 0; q < RP; q++)
 #pragma unroll
       for (int k = 0; k < 12; k++) acc[q][k] = C<float>{0.f, 0.f};
-    mhop_pair<0, DAG, RP>(a, x, c, r0, acc);
-    mhop_pair<1, DAG, RP>(a, x, c, r0, acc);
-    mhop_pair<2, DAG, RP>(a, x, c, r0, acc);
-    mhop_pair<3, DAG, RP>(a, x, c, r0, acc);
+    mhop_pair<0, DAG, RP, EO>(a, x, c, r0, acc);
+    mhop_pair<1, DAG, RP, EO>(a, x, c, r0, acc);
+    mhop_pair<2, DAG, RP, EO>(a, x, c, r0, acc);
+    mhop_pair<3, DAG, RP, EO>(a, x, c, r0, acc);
     C<float> s[RP][12];
     float nrm[RP];
-    mload_rp<RP>(a, x, r0, s, nrm);
+    if (a.zmode) mload_rp<RP>(a, a.z, a.z_norm, e, r0, s, nrm);
 #pragma unroll
     for (int q = 0; q < RP; q++) {
       const int r = r0 + q;
       // slots past nact hold zeros; their results are not stored
-      const float mp4r = (a.mp4s ? a.mp4s[r] : a.mp4) * nrm[q];
-      const float tmr = (a.tms ? (DAG ? -a.tms[r] : a.tms[r]) : a.tm) * nrm[q];
+      const float mp4r = a.mp4s ? a.mp4s[r] : a.mp4;
+      const float tmr = a.tms ? (DAG ? -a.tms[r] : a.tms[r]) : a.tm;
+      if (a.ainv) {  // A^{-1} = (mp4 - i tm g5) / (mp4^2 + tm^2)
+        const float den = 1.0f / (mp4r * mp4r + tmr * tmr), ar = mp4r * den, ai = -tmr * den;
+#pragma unroll
+        for (int k = 0; k < 12; k++) {
+          const float g5ai = k < 6 ? ai : -ai;
+          acc[q][k] = C<float>{ar * acc[q][k].re - g5ai * acc[q][k].im, ar * acc[q][k].im + g5ai * acc[q][k].re};
+        }
+      }
+      const float zs = a.zmode ? nrm[q] : 0.f;
+      const float zm = a.zmode == 2 ? mp4r * zs : zs, zt = a.zmode == 2 ? tmr * zs : 0.f;
       float mx = 0.f;
 #pragma unroll
       for (int k = 0; k < 12; k++) {
-        const float g5tm = k < 6 ? tmr : -tmr;
-        acc[q][k] = C<float>{mp4r * s[q][k].re - g5tm * s[q][k].im - 0.5f * acc[q][k].re,
-                             mp4r * s[q][k].im + g5tm * s[q][k].re - 0.5f * acc[q][k].im};
+        const float g5tm = k < 6 ? zt : -zt;
+        const C<float> zk = a.zmode ? s[q][k] : C<float>{0.f, 0.f};
+        acc[q][k] = C<float>{zm * zk.re - g5tm * zk.im + a.ch * acc[q][k].re,
+                             zm * zk.im + g5tm * zk.re + a.ch * acc[q][k].im};
         mx = fmaxf(mx, fmaxf(fabsf(acc[q][k].re), fabsf(acc[q][k].im)));
       }
       if (!(mx >= 1.17549435e-38f)) mx = 0.f;
@@ -325,7 +352,7 @@ __global__ void __launch_bounds__(256) k_wilson_mrhs_simt(const MArgs a, double 
         float2 o[12];
 #pragma unroll
         for (int k = 0; k < 12; k++) o[k] = make_float2(acc[q][k].re, acc[q][k].im);
-        mstore_raw(a.out, a.V, a.N, x, r, o, inv);
+        mstore_raw(a.out, a.V, a.N, e, r, o, inv);
         float s2 = 0.f;
         if (partials) {  // |out|^2 of the stored (rounded) values
 #pragma unroll
@@ -334,7 +361,7 @@ __global__ void __launch_bounds__(256) k_wilson_mrhs_simt(const MArgs a, double 
             s2 += f.x * f.x + f.y * f.y;
           }
         }
-        a.out_norm[(int64_t)x * a.N + r] = mx;
+        a.out_norm[(int64_t)e * a.N + r] = mx;
         n2[q] = (double)(s2 * mx * mx);  // per-site sum in FP32, block sum in double
       }
     }
@@ -515,13 +542,20 @@ static bool launch_mrhs(const MArgs &a, bool dag, MrhsTune t, double *partials, 
   const size_t shm = sizeof(double) * a.N * blk.y;
   if (simt) {
     const size_t sm = partials ? shm : 0;
-    if (t.rp == 2) {
-      if (dag) k_wilson_mrhs_simt<true, 2><<<nb, blk, sm, s>>>(a, partials);
-      else k_wilson_mrhs_simt<false, 2><<<nb, blk, sm, s>>>(a, partials);
+    const bool eo = a.eo_par >= 0;
+#define QG_SIMT(RP, EO)                                                             \
+  if (dag) k_wilson_mrhs_simt<true, RP, EO><<<nb, blk, sm, s>>>(a, partials);       \
+  else k_wilson_mrhs_simt<false, RP, EO><<<nb, blk, sm, s>>>(a, partials);
+    if (t.rp == 2 && eo) {
+      QG_SIMT(2, true)
+    } else if (t.rp == 2) {
+      QG_SIMT(2, false)
+    } else if (eo) {
+      QG_SIMT(1, true)
     } else {
-      if (dag) k_wilson_mrhs_simt<true, 1><<<nb, blk, sm, s>>>(a, partials);
-      else k_wilson_mrhs_simt<false, 1><<<nb, blk, sm, s>>>(a, partials);
+      QG_SIMT(1, false)
     }
+#undef QG_SIMT
     if (!QG_LAUNCHED("wilson_mrhs_simt")) return false;
   } else {
     unsigned grid = (unsigned)((a.V + 3) / 4);
@@ -644,6 +678,12 @@ bool dslash_mrhs(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_gauge g, double mp4
   a.tm = (float)(dag ? -tm : tm);
   a.mp4s = mp4s;
   a.tms = tms;
+  a.z = a.in;  // full-lattice operator: (m+4) in + i tm g5 in - H in / 2
+  a.z_norm = a.in_norm;
+  a.zmode = 2;
+  a.ainv = 0;
+  a.ch = -0.5f;
+  a.eo_par = -1;
   if (nact == 0) {
     if (nblocks) *nblocks = 0;
     return true;
@@ -651,6 +691,66 @@ bool dslash_mrhs(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_gauge g, double mp4
   const MrhsTune tune = mrhs_tune(a, dag, out, in);
   if (!launch_mrhs(a, dag, tune, partials, nblocks)) return false;
   return true;
+}
+
+// Even/odd multi-RHS kernel (SIMT) on half-lattice fields: slots 0..nact-1 of
+// out (parity par) = ch * [A^{-1}] H in + {0 | z | A z}, A the slot's diagonal
+// (mp4s, tms; D^+: tm -> -tm and the hopping term of D^+). partials as in
+// dslash_mrhs. g is the FP64 gauge field of the full lattice.
+bool dslash_mrhs_eo(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_mfield z, qcdgpu_gauge g, bool dag, int nact,
+                    const float *mp4s, const float *tms, int par, double ch, bool ainv, int zmode, double *partials,
+                    unsigned *nblocks)
+{
+  if (!out || !in || !g || out == in || out->N != in->N || out->V != in->V || (zmode && (!z || z == out)) ||
+      (z && (z->N != in->N || z->V != in->V)) || g->prec != QCDGPU_F64 || g->L[0] % 2 != 0 ||
+      in->L[0] * 2 != g->L[0] || in->L[1] != g->L[1] || in->L[2] != g->L[2] || in->L[3] != g->L[3] ||
+      memcmp(out->L, in->L, sizeof(in->L)) != 0 || nact < 0 || nact > in->N || !mp4s || !tms) {
+    set_error("even/odd multi-RHS operator: half-lattice fields of one shape, per-slot diagonal");
+    return false;
+  }
+  qcdgpu_gauge g32 = gauge_at(g, kGaugeF32Full);
+  if (!g32) return false;
+  MArgs a;
+  a.out = (__half2 *)out->data;
+  a.out_norm = out->norm;
+  a.in = (const __half2 *)in->data;
+  a.in_norm = in->norm;
+  a.gauge = (const float2 *)g32->data;
+  for (int i = 0; i < 4; i++) a.geo.L[i] = g->L[i];
+  a.geo.st[0] = 1;
+  a.geo.st[1] = g->L[0];
+  a.geo.st[2] = g->L[0] * g->L[1];
+  a.geo.st[3] = g->L[0] * g->L[1] * g->L[2];
+  a.V = (int)in->V;
+  a.N = in->N;
+  a.nact = nact;
+  a.gstride = g32->stride;
+  a.twist_mask = 0;
+  for (int mu = 0; mu < 4; mu++) {
+    a.phr[mu] = 1.f;
+    a.phi[mu] = 0.f;
+    if (g->theta[mu] != 0.0) {
+      a.twist_mask |= 1 << mu;
+      a.phr[mu] = (float)cos(g->theta[mu] / (double)g->L[mu]);
+      a.phi[mu] = (float)sin(g->theta[mu] / (double)g->L[mu]);
+    }
+  }
+  a.mp4 = 4.f;
+  a.tm = 0.f;
+  a.mp4s = mp4s;
+  a.tms = tms;
+  a.z = z ? (const __half2 *)z->data : nullptr;
+  a.z_norm = z ? z->norm : nullptr;
+  a.zmode = zmode;
+  a.ainv = ainv ? 1 : 0;
+  a.ch = (float)ch;
+  a.eo_par = par;
+  if (nact == 0) {
+    if (nblocks) *nblocks = 0;
+    return true;
+  }
+  const MrhsTune t{MRHS_SIMT, 128, in->N % 2 == 0 ? 2 : 1};
+  return launch_mrhs(a, dag, t, partials, nblocks);
 }
 
 }  // namespace qg

@@ -72,6 +72,11 @@ bool mfield_get(qcdgpu_field f, qcdgpu_mfield m, int r);
 bool dslash_mrhs(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_gauge g, double mp4, double tm, bool dag, int nact,
                  const float *mp4s, const float *tms, double *partials = nullptr, unsigned *nblocks = nullptr);
 unsigned mrhs_max_blocks(int64_t V, int N);
+// even/odd kernel on half-lattice fields (SIMT): out (parity par) =
+// ch * [A^{-1}] H in + {0 | z | A z} with the slots' diagonals A
+bool dslash_mrhs_eo(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_mfield z, qcdgpu_gauge g, bool dag, int nact,
+                    const float *mp4s, const float *tms, int par, double ch, bool ainv, int zmode, double *partials,
+                    unsigned *nblocks);
 
 // operator variants picked by the tuner
 enum { MRHS_AUTO = -1, MRHS_SIMT = 0, MRHS_MMA = 1 };

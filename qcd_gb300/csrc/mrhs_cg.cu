@@ -204,6 +204,9 @@ namespace qg {
 struct BSlot {
   int tag;
   qcdgpu_field x, b;  // caller's FP64 fields
+  // even/odd batches: the slot's FP64 half fields -- system right-hand side
+  // c_e = b_e + H_eo A^{-1} b_o / 2, A^{-1} b_o, and the solution x_e
+  qcdgpu_field ce, to, xe;
   int op;             // QCDGPU_OP_D or QCDGPU_OP_Q
   double mp4, tm, bn, tol, delta, maxr, hint, true_res;
   int iters, maxiter, updates, since;
@@ -219,9 +222,16 @@ struct BDone {
 struct qcdgpu_batch_s {
   qcdgpu_gauge g;
   int cap, nact;
-  qcdgpu_mfield rs, ps, t, aps;
+  // even/odd: the slots solve the Schur complement M x_e = c_e on the half
+  // lattice (Ls, Vs); otherwise D^+ D on the full lattice
+  bool eo;
+  int Ls[4];
+  int64_t Vs;
+  qcdgpu_mfield rs, ps, t, aps, u;  // u: odd intermediate (even/odd only)
   float4 *xs;                  // FP32 solution increments (layout of MX)
   qcdgpu_field rt, r, up, bd;  // FP64 work shared by the slots' reliable updates
+  qcdgpu_field u64, r32, u32, s32;  // even/odd: FP64 odd temp; FP32 restart fields
+  std::vector<std::vector<qcdgpu_field>> spare;  // even/odd: free (ce, to, xe) sets
   double *s;                   // device scalars, (M_HIST + kMChunk) * cap
   float *mp4s, *tms;           // device per-slot diagonal
   double *part;                // device partials
@@ -240,14 +250,18 @@ struct qcdgpu_batch_s {
 
 namespace qg {
 
-static MX mx(qcdgpu_batch B) { return MX{B->xs, (int)B->g->V, B->cap}; }
+static MX mx(qcdgpu_batch B) { return MX{B->xs, (int)B->Vs, B->cap}; }
 
 static void batch_free(qcdgpu_batch b)
 {
   if (!b) return;
-  for (auto m : {b->rs, b->ps, b->t, b->aps}) mfield_free(m);
+  for (auto m : {b->rs, b->ps, b->t, b->aps, b->u}) mfield_free(m);
   cudaFree(b->xs);
-  for (auto f : {b->rt, b->r, b->up, b->bd}) field_free(f);
+  for (auto f : {b->rt, b->r, b->up, b->bd, b->u64, b->r32, b->u32, b->s32}) field_free(f);
+  for (auto &sl : b->slots)
+    for (auto f : {sl.ce, sl.to, sl.xe}) field_free(f);
+  for (auto &set : b->spare)
+    for (auto f : set) field_free(f);
   cudaFree(b->s);
   cudaFree(b->mp4s);
   cudaFree(b->tms);
@@ -261,34 +275,52 @@ static void batch_free(qcdgpu_batch b)
   delete b;
 }
 
-static qcdgpu_batch batch_new(qcdgpu_gauge g, int cap)
+static qcdgpu_batch batch_new(qcdgpu_gauge g, int cap, bool eo)
 {
-  if (!g || g->prec != QCDGPU_F64 || cap < 1 || cap > 64) {
-    set_error("batch: FP64 gauge field and 1..64 slots required");
+  if (!g || g->prec != QCDGPU_F64 || cap < 1 || cap > 64 || (eo && g->L[0] % 2 != 0)) {
+    set_error("batch: FP64 gauge field, 1..64 slots, even t extent for even/odd");
     return nullptr;
   }
   auto *b = new qcdgpu_batch_s();
   b->g = g;
   b->cap = cap;
+  b->eo = eo;
+  memcpy(b->Ls, g->L, sizeof(b->Ls));
+  if (eo) b->Ls[0] /= 2;
+  b->Vs = (int64_t)b->Ls[0] * b->Ls[1] * b->Ls[2] * b->Ls[3];
   b->nact = 0;
   b->st = nullptr;
   b->nchunk = 0;
   b->use_graphs = true;
   b->graphs.assign((size_t)cap + 1, nullptr);
   b->graph_launches.assign((size_t)cap + 1, 0);
-  b->rs = mfield_new(g->L, cap);
-  b->ps = mfield_new(g->L, cap);
-  b->t = mfield_new(g->L, cap);
-  b->aps = mfield_new(g->L, cap);
-  b->rt = field_new(g->L, QCDGPU_F64);
-  b->r = field_new(g->L, QCDGPU_F64);
-  b->up = field_new(g->L, QCDGPU_F64);
+  b->rs = mfield_new(b->Ls, cap);
+  b->ps = mfield_new(b->Ls, cap);
+  b->t = mfield_new(b->Ls, cap);
+  b->aps = mfield_new(b->Ls, cap);
+  b->rt = field_new(b->Ls, QCDGPU_F64);
+  b->r = field_new(b->Ls, QCDGPU_F64);
+  b->up = field_new(b->Ls, QCDGPU_F64);
   b->bd = field_new(g->L, QCDGPU_F64);
+  bool ok = b->rs && b->ps && b->t && b->aps && b->rt && b->r && b->up && b->bd;
+  if (eo) {
+    b->u = mfield_new(b->Ls, cap);
+    b->u64 = field_new(b->Ls, QCDGPU_F64);
+    b->r32 = field_new(b->Ls, QCDGPU_F32);
+    b->u32 = field_new(b->Ls, QCDGPU_F32);
+    b->s32 = field_new(b->Ls, QCDGPU_F32);
+    ok = ok && b->u && b->u64 && b->r32 && b->u32 && b->s32;
+    for (int k = 0; ok && k < cap; k++) {
+      std::vector<qcdgpu_field> set;
+      for (int i = 0; i < 3; i++) set.push_back(field_new(b->Ls, QCDGPU_F64));
+      b->spare.push_back(set);
+      ok = set[0] && set[1] && set[2];
+    }
+  }
   size_t ns = (size_t)(M_HIST + kMChunk) * cap;
-  unsigned nb = mgrid((int)g->V, cap);
-  if (mrhs_max_blocks(g->V, cap) > nb) nb = mrhs_max_blocks(g->V, cap);
-  bool ok = b->rs && b->ps && b->t && b->aps && b->rt && b->r && b->up && b->bd &&
-            QG_CUDA(cudaMalloc(&b->xs, (size_t)12 * g->V * cap * sizeof(float2))) &&
+  unsigned nb = mgrid((int)b->Vs, cap);
+  if (mrhs_max_blocks(b->Vs, cap) > nb) nb = mrhs_max_blocks(b->Vs, cap);
+  ok = ok && QG_CUDA(cudaMalloc(&b->xs, (size_t)12 * b->Vs * cap * sizeof(float2))) &&
             QG_CUDA(cudaMalloc(&b->s, ns * sizeof(double))) && QG_CUDA(cudaMalloc(&b->mp4s, cap * sizeof(float))) &&
             QG_CUDA(cudaMalloc(&b->tms, cap * sizeof(float))) &&
             QG_CUDA(cudaMalloc(&b->part, (size_t)nb * cap * sizeof(double))) &&
@@ -310,9 +342,24 @@ static bool slot_bd(qcdgpu_batch B, const BSlot &sl)
   return blas_copy(B->bd, sl.b);
 }
 
-// rt = bd - D x (FP64), r = D^+ rt; slot k of rs <- r; returns |rt| / |b| and |r|^2
+// rt = bd - D x (FP64), r = D^+ rt; slot k of rs <- r; returns |rt| / |b| and |r|^2.
+// Even/odd: rt = c_e - M x_e in FP64 (equal to the full residual), and the
+// restart residual M^+ rt in FP32 (it only seeds the FP16 iteration).
 static bool slot_residual(qcdgpu_batch B, int k, const BSlot &sl, double *rel, double *rr)
 {
+  if (B->eo) {
+    qcdgpu_gauge g32 = gauge_at(B->g, QCDGPU_F32);
+    double n2;
+    if (!g32 || !dslash_eo(B->u64, sl.xe, nullptr, B->g, sl.mp4, sl.tm, false, 1, 1.0, true, 0, nullptr) ||
+        !dslash_eo(B->rt, B->u64, sl.xe, B->g, sl.mp4, sl.tm, false, 0, -0.25, false, 2, nullptr) ||
+        !blas_axpby(B->rt, 1.0, 0.0, sl.ce, -1.0, 0.0, B->rt) || !blas_norm2(B->rt, &n2))
+      return false;
+    *rel = sl.bn > 0 ? sqrt(n2) / sl.bn : 0.0;
+    return convert_field(B->r32, B->rt) &&
+           dslash_eo(B->u32, B->r32, nullptr, g32, sl.mp4, sl.tm, true, 1, 1.0, true, 0, nullptr) &&
+           dslash_eo(B->s32, B->u32, B->r32, g32, sl.mp4, sl.tm, true, 0, -0.25, false, 2, nullptr) &&
+           blas_norm2(B->s32, rr) && mfield_set(B->rs, k, B->s32);
+  }
   if (!slot_bd(B, sl)) return false;
   if (!dslash(B->rt, sl.x, B->g, sl.mp4, sl.tm, QCDGPU_OP_D, QCDGPU_ARITH_DF64)) return false;
   if (!blas_axpby(B->rt, 1.0, 0.0, B->bd, -1.0, 0.0, B->rt)) return false;
@@ -334,7 +381,7 @@ static bool set_scalar(qcdgpu_batch B, int slot_kind, int k, double v)
 
 static bool copy_slot(qcdgpu_batch B, int from, int to)
 {
-  unsigned g = (unsigned)((B->g->V + 127) / 128);
+  unsigned g = (unsigned)((B->Vs + 127) / 128);
   for (auto m : {B->rs, B->ps}) {
     k_mcopy<<<g, 128, 0, stream()>>>(mv(m), from, to, 0);
     if (!QG_LAUNCHED("mrhs_copy_slot")) return false;
@@ -348,8 +395,8 @@ static bool copy_slot(qcdgpu_batch B, int from, int to)
 int batch_add(qcdgpu_batch B, qcdgpu_field x, qcdgpu_field b, double kappa, double mu, int op, double tol,
               int maxiter, double delta, int tag)
 {
-  if (!x || !b || x->prec != QCDGPU_F64 || b->prec != QCDGPU_F64 || !same_shape(x, B->rt) ||
-      !same_shape(b, B->rt) || x == b || !(kappa > 0.0) || (op != QCDGPU_OP_D && op != QCDGPU_OP_Q)) {
+  if (!x || !b || x->prec != QCDGPU_F64 || b->prec != QCDGPU_F64 || !same_shape(x, B->bd) ||
+      !same_shape(b, B->bd) || x == b || !(kappa > 0.0) || (op != QCDGPU_OP_D && op != QCDGPU_OP_Q)) {
     set_error("batch add: FP64 x, b on the batch's lattice, kappa > 0, op D or Q");
     return -2;
   }
@@ -374,15 +421,38 @@ int batch_add(qcdgpu_batch B, qcdgpu_field x, qcdgpu_field b, double kappa, doub
   if (!blas_norm2(b, &bn2) || !blas_zero(x)) return -2;
   sl.bn = sqrt(bn2);
   const int k = B->nact;
+  sl.ce = sl.to = sl.xe = nullptr;
+  if (B->eo) {
+    // c_e = b_e + H_eo A^{-1} b_o / 2 with the slot's own half fields
+    std::vector<qcdgpu_field> set = B->spare.back();
+    B->spare.pop_back();
+    sl.ce = set[0];
+    sl.to = set[1];
+    sl.xe = set[2];
+    const bool ok = slot_bd(B, sl) && eo_split(B->rt, B->r, B->bd) && eo_diag(sl.to, B->r, sl.mp4, mu, true) &&
+                    dslash_eo(sl.ce, sl.to, B->rt, B->g, sl.mp4, mu, false, 0, 0.5, false, 1, nullptr) &&
+                    blas_zero(sl.xe);
+    if (!ok) {
+      B->spare.push_back(set);
+      return -2;
+    }
+  }
   double rel, rr;
-  if (!slot_residual(B, k, sl, &rel, &rr)) return -2;
+  auto give_back = [&]() {
+    if (B->eo) B->spare.push_back({sl.ce, sl.to, sl.xe});
+  };
+  if (!slot_residual(B, k, sl, &rel, &rr)) {
+    give_back();
+    return -2;
+  }
   sl.true_res = rel;
   sl.maxr = sqrt(rr);
   sl.hint = tol * sl.maxr;
-  unsigned g = (unsigned)((B->g->V + 127) / 128);
+  unsigned g = (unsigned)((B->Vs + 127) / 128);
   k_mx_copy<<<g, 128, 0, stream()>>>(mx(B), 0, k, 1);
   if (!QG_LAUNCHED("mrhs_zero_slot")) return -2;
-  if (!mfield_set(B->ps, k, B->r)) return -2;
+  // p = r (slot_residual left r in B->s32 for even/odd batches, else in B->r)
+  if (!mfield_set(B->ps, k, B->eo ? B->s32 : B->r)) return -2;
   float mp = (float)sl.mp4, tmf = (float)mu;
   if (!QG_CUDA(cudaMemcpyAsync(B->mp4s + k, &mp, sizeof(float), cudaMemcpyHostToDevice, stream())) ||
       !QG_CUDA(cudaMemcpyAsync(B->tms + k, &tmf, sizeof(float), cudaMemcpyHostToDevice, stream())))
@@ -391,6 +461,7 @@ int batch_add(qcdgpu_batch B, qcdgpu_field x, qcdgpu_field b, double kappa, doub
   if (!set_scalar(B, M_RR, k, rr) || !set_scalar(B, M_BETA, k, 0.0)) return -2;
   if (bn2 == 0.0 || rel <= tol) {
     B->done.push_back(BDone{tag, 0, 0, 0, rel});
+    give_back();
     return k;
   }
   B->slots.push_back(sl);
@@ -402,6 +473,13 @@ int batch_add(qcdgpu_batch B, qcdgpu_field x, qcdgpu_field b, double kappa, doub
 static bool retire(qcdgpu_batch B, int k, int status)
 {
   BSlot &sl = B->slots[(size_t)k];
+  if (B->eo) {
+    // x_o = A^{-1} b_o + A^{-1} H_oe x_e / 2, then x = (x_e, x_o)
+    if (!dslash_eo(B->r, sl.xe, sl.to, B->g, sl.mp4, sl.tm, false, 1, 0.5, true, 1, nullptr) ||
+        !eo_merge(sl.x, sl.xe, B->r))
+      return false;
+    B->spare.push_back({sl.ce, sl.to, sl.xe});
+  }
   B->done.push_back(BDone{sl.tag, status, sl.iters, sl.updates, sl.true_res});
   const int last = B->nact - 1;
   if (k != last) {
@@ -428,7 +506,7 @@ static bool retire(qcdgpu_batch B, int k, int status)
 static bool chunk_enqueue(qcdgpu_batch B, int n)
 {
   const int cap = B->cap;
-  const int V = (int)B->g->V;
+  const int V = (int)B->Vs;
   const dim3 blk = mblock(cap);
   const unsigned nb = mgrid(V, cap);
   const size_t shm = sizeof(double) * blk.x * blk.y;
@@ -437,12 +515,26 @@ static bool chunk_enqueue(qcdgpu_batch B, int n)
     // p = r + beta p (beta = 0 keeps a fresh slot's p = r)
     k_mp<<<nb, blk, 0, st>>>(mv(B->ps), mv(B->rs), n, B->s + M_BETA * cap);
     if (!QG_LAUNCHED("mrhs_p")) return false;
-    // p^+ D^+ D p = |D p|^2, summed per slot in the first operator's epilogue
+    // p^+ A^+ A p = |A p|^2, summed per slot in the epilogue of t = A p
+    // (A = D, or the Schur complement M = A_ee - H_eo A_oo^{-1} H_oe / 4 as
+    // u = A^{-1} H_oe p, t = A p - H_eo u / 4)
     unsigned nbo = 0;
-    if (!dslash_mrhs(B->t, B->ps, B->g, 4.0, 0.0, false, n, B->mp4s, B->tms, B->part, &nbo)) return false;
+    if (B->eo) {
+      if (!dslash_mrhs_eo(B->u, B->ps, nullptr, B->g, false, n, B->mp4s, B->tms, 1, 1.0, true, 0, nullptr, nullptr) ||
+          !dslash_mrhs_eo(B->t, B->u, B->ps, B->g, false, n, B->mp4s, B->tms, 0, -0.25, false, 2, B->part, &nbo))
+        return false;
+    } else if (!dslash_mrhs(B->t, B->ps, B->g, 4.0, 0.0, false, n, B->mp4s, B->tms, B->part, &nbo)) {
+      return false;
+    }
     k_mscalars<<<n, 256, 0, st>>>(B->part, (int)nbo, cap, B->s, 0, j);
     if (!QG_LAUNCHED("mrhs_scalars")) return false;
-    if (!dslash_mrhs(B->aps, B->t, B->g, 4.0, 0.0, true, n, B->mp4s, B->tms)) return false;
+    if (B->eo) {
+      if (!dslash_mrhs_eo(B->u, B->t, nullptr, B->g, true, n, B->mp4s, B->tms, 1, 1.0, true, 0, nullptr, nullptr) ||
+          !dslash_mrhs_eo(B->aps, B->u, B->t, B->g, true, n, B->mp4s, B->tms, 0, -0.25, false, 2, nullptr, nullptr))
+        return false;
+    } else if (!dslash_mrhs(B->aps, B->t, B->g, 4.0, 0.0, true, n, B->mp4s, B->tms)) {
+      return false;
+    }
     k_mupdate<<<nb, blk, shm, st>>>(mx(B), mv(B->ps), mv(B->rs), mv(B->aps), n, B->s + M_ALPHA * cap, B->part);
     if (!QG_LAUNCHED("mrhs_update")) return false;
     k_mscalars<<<n, 256, 0, st>>>(B->part, (int)nb, cap, B->s, 1, j);
@@ -458,7 +550,7 @@ bool batch_launch(qcdgpu_batch B)
   StreamScope scope(B->st);
   const int n = B->nchunk;
   if (!gauge_at(B->g, kGaugeF32Full)) return false;  // resident before any capture
-  if (!B->tuned) {
+  if (!B->tuned && !B->eo) {
     // the operator's tuner times its variants outside stream capture; t is
     // scratch (recomputed by every iteration)
     if (!dslash_mrhs(B->t, B->ps, B->g, 4.0, 0.0, false, n, B->mp4s, B->tms)) return false;
@@ -501,7 +593,7 @@ bool batch_finish(qcdgpu_batch B)
   if (n == 0) return true;
   StreamScope scope(B->st);
   const int cap = B->cap;
-  const int V = (int)B->g->V;
+  const int V = (int)B->Vs;
   cudaStream_t st = B->st;
   if (!QG_CUDA(cudaEventSynchronize(B->ev))) return false;
   std::vector<double> rr_iter(n), beta_iter(n);
@@ -530,7 +622,8 @@ bool batch_finish(qcdgpu_batch B)
   for (int k = 0; k < n; k++) {
     if (!need[k]) continue;
     BSlot &sl = B->slots[(size_t)k];
-    k_mx_flush<<<(unsigned)((V + 127) / 128), 128, 0, st>>>((double2 *)sl.x->data, sl.x->stride, mx(B), k);
+    qcdgpu_field acc = B->eo ? sl.xe : sl.x;  // the slot's FP64 solution
+    k_mx_flush<<<(unsigned)((V + 127) / 128), 128, 0, st>>>((double2 *)acc->data, acc->stride, mx(B), k);
     if (!QG_LAUNCHED("mrhs_flush_slot")) return false;
     double rel, rr;
     if (!slot_residual(B, k, sl, &rel, &rr)) return false;
@@ -568,7 +661,12 @@ extern "C" {
 
 int qcdgpu_batch_create(qcdgpu_batch *b, qcdgpu_gauge g, int capacity)
 {
-  *b = qg::batch_new(g, capacity);
+  *b = qg::batch_new(g, capacity, false);
+  return *b ? 0 : 1;
+}
+int qcdgpu_batch_create_eo(qcdgpu_batch *b, qcdgpu_gauge g, int capacity)
+{
+  *b = qg::batch_new(g, capacity, true);
   return *b ? 0 : 1;
 }
 int qcdgpu_batch_destroy(qcdgpu_batch b)
@@ -601,7 +699,9 @@ int qcdgpu_batch_poll(qcdgpu_batch b, int *tags, int *status, int *iters, double
 size_t qcdgpu_batch_bytes(qcdgpu_batch b)
 {
   if (!b) return 0;
-  return 4 * b->rs->bytes + (size_t)12 * b->g->V * b->cap * sizeof(float2) + 4 * b->rt->bytes;
+  size_t n = 4 * b->rs->bytes + (size_t)12 * b->Vs * b->cap * sizeof(float2) + 3 * b->rt->bytes + b->bd->bytes;
+  if (b->eo) n += b->u->bytes + b->u64->bytes + 3 * b->r32->bytes + (size_t)3 * b->cap * b->rt->bytes;
+  return n;
 }
 
 }  // extern "C"

@@ -68,12 +68,20 @@ static size_t field_bytes_f64(const int L[4])
   return (size_t)pad_stride((int64_t)L[0] * L[1] * L[2] * L[3]) * 12 * sizeof(double2);
 }
 
+// batches of lattices with an even t extent solve the even/odd system
+static bool use_eo(const int L[4]) { return L[0] % 2 == 0; }
+
 // device bytes of a batch of `slots` slots on lattice L (mirrors batch_new)
 static size_t batch_bytes_est(const int L[4], int slots)
 {
-  const int64_t V = (int64_t)L[0] * L[1] * L[2] * L[3];
-  const size_t mf = (size_t)12 * V * slots * sizeof(__half2) + (size_t)V * slots * sizeof(float);
-  return 4 * mf + (size_t)12 * V * slots * sizeof(float2) + 4 * field_bytes_f64(L);
+  const bool eo = use_eo(L);
+  const int Ls[4] = {eo ? L[0] / 2 : L[0], L[1], L[2], L[3]};
+  const int64_t Vs = (int64_t)Ls[0] * Ls[1] * Ls[2] * Ls[3];
+  const size_t mf = (size_t)12 * Vs * slots * sizeof(__half2) + (size_t)Vs * slots * sizeof(float);
+  const size_t f64 = field_bytes_f64(Ls), f32 = f64 / 2;
+  size_t n = 4 * mf + (size_t)12 * Vs * slots * sizeof(float2) + 3 * f64 + field_bytes_f64(L);
+  if (eo) n += mf + f64 + 3 * f32 + (size_t)3 * slots * f64;
+  return n;
 }
 
 static void free_request_fields(SrvRequest &r)
@@ -102,7 +110,8 @@ static bool admit(qcdgpu_server S, SrvRequest &r)
   if (!G.batch) {
     G.batch = [&]() {
       qcdgpu_batch b = nullptr;
-      return qcdgpu_batch_create(&b, G.g, S->slots) == 0 ? b : nullptr;
+      const int rc = use_eo(G.g->L) ? qcdgpu_batch_create_eo(&b, G.g, S->slots) : qcdgpu_batch_create(&b, G.g, S->slots);
+      return rc == 0 ? b : nullptr;
     }();
     if (!G.batch) return false;
     S->used += qcdgpu_batch_bytes(G.batch);

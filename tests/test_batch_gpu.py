@@ -33,7 +33,12 @@ def _run(batch, pending, max_steps=4000):
     return out
 
 
-def test_batch_mixed_kappa_mu_op_each_converges(gpu, orc):
+@pytest.fixture(params=[False, True], ids=["full", "eo"])
+def eo(request):
+    return request.param
+
+
+def test_batch_mixed_kappa_mu_op_each_converges(gpu, orc, eo):
     u = orc.gauge_synthetic(L, 11, EPS_PLAQ_060)
     g = q.Gauge(L, TH).load(u)
     params = [(0.15, 0.0, q.OP_D, 1e-10), (0.14, 0.02, q.OP_D, 1e-10), (0.155, 0.0, q.OP_D, 1e-8),
@@ -45,9 +50,10 @@ def test_batch_mixed_kappa_mu_op_each_converges(gpu, orc):
         srcs.append(b)
         fields += [fb, fx]
         reqs.append((i, fx, fb, kappa, mu, op, tol))
-    batch = q.Batch(g, 8)
+    batch = q.Batch(g, 8, eo=eo)
     res = _run(batch, reqs)
-    assert q.mrhs_tuned(L, 8) is not None  # the operator variant was tuned before graph capture
+    if not eo:
+        assert q.mrhs_tuned(L, 8) is not None  # the operator variant was tuned before graph capture
     assert sorted(res) == list(range(len(params)))
     for i, (kappa, mu, op, tol) in enumerate(params):
         st, it, tr = res[i]
@@ -61,7 +67,7 @@ def test_batch_mixed_kappa_mu_op_each_converges(gpu, orc):
         f.close()
 
 
-def test_batch_continuous_admission_more_requests_than_slots(gpu, orc):
+def test_batch_continuous_admission_more_requests_than_slots(gpu, orc, eo):
     u = orc.gauge_synthetic(L, 12, EPS_PLAQ_060)
     g = q.Gauge(L, TH).load(u)
     n = 9
@@ -73,7 +79,7 @@ def test_batch_continuous_admission_more_requests_than_slots(gpu, orc):
         fields += [fb, fx]
         kappa = 0.13 + 0.0025 * i
         reqs.append((i, fx, fb, kappa, 0.0, q.OP_D, 1e-10))
-    batch = q.Batch(g, 3)
+    batch = q.Batch(g, 3, eo=eo)
     res = _run(batch, reqs)
     assert sorted(res) == list(range(n))
     for i in range(n):
@@ -85,7 +91,7 @@ def test_batch_continuous_admission_more_requests_than_slots(gpu, orc):
         f.close()
 
 
-def test_batch_result_independent_of_the_mix(gpu, orc):
+def test_batch_result_independent_of_the_mix(gpu, orc, eo):
     """Per-slot reductions sum in a fixed order and the tensor-core product of
     one RHS row does not involve the others, so a request solved alone and in
     a mix (same capacity) gives bit-identical solutions."""
@@ -93,7 +99,7 @@ def test_batch_result_independent_of_the_mix(gpu, orc):
     g = q.Gauge(L, TH).load(u)
     b = orc.gaussian_spinor(L, 500)
     fb, fx_alone = q.Field(L).load(b), q.Field(L)
-    batch = q.Batch(g, 4)
+    batch = q.Batch(g, 4, eo=eo)
     _run(batch, [(0, fx_alone, fb, 0.15, 0.01, q.OP_D, 1e-10)])
     others = []
     reqs = []

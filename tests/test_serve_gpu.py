@@ -50,7 +50,7 @@ def gauges(gpu, orc):
 
 def test_server_stream_of_mixed_requests(gpu, orc, gauges):
     (ua, ga), (ub, gb) = gauges
-    budget = 64 * MB  # both batches plus a few requests: later ones wait for admission
+    budget = 96 * MB  # both batches plus a few requests: later ones wait for admission
     srv = q.Server(budget, slots=8)
     ia, ib = srv.add_gauge(ga), srv.add_gauge(gb)
     reqs = [  # (tag, gauge, L, u, nrhs, kappa, mu, op, tol, gaussian sources?)
