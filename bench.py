@@ -6,19 +6,27 @@ links with mean plaquette 0.60 and a seeded Gaussian spinor): the lattice of
 the plain FP64 single-RHS configuration, timed over K applications.
 
   value  -- device-resident: algorithmic bytes per apply (spinor in + 4
-            links (12 reals) + spinor out = 768 B/site) / kernel time, GB/s.
+            links (18 reals) + spinor out = 960 B/site) / kernel time, GB/s,
+            for the faster FP64-accurate kernel (float-float or native).
   e2e    -- the same apply through the qcd_lib C entry point
             qcd_applyWilsonTMOp on host (page-locked) buffers: each step
             copies the input spinor host->device and the result back; the
             gauge field is uploaded once beforehand (qcdgpu_gauge_upload).
-  solve  -- RHS-solves/s and latency percentiles of point-source solves to a
-            true residual of 1e-10: plain FP64 GPU solve vs mixed precision.
+  solve  -- point-source columns at 24^3 x 48 to a true residual of 1e-10:
+            plain FP64 GPU CGNR (the drop-in) vs mixed precision and even/odd.
+  precision_32x64 -- the same comparison at 32^3 x 64, kappa = 0.155, plus
+            batched multi-RHS solves (full and even/odd).
+  mrhs_operator -- multi-RHS operator at 48^3 x 96 over RHS per block.
+  serving -- a seeded Poisson stream of requests (four resident gauge
+            fields, 8^3 x 16 ... 32^3 x 64, 1-48 RHS each): RHS-solves/s and
+            p50 / p99 latency.
 
 Multi-GPU: the operator keeps the whole lattice on one GPU; N processes run
 N independent replicas (no collective) and value sums their throughput.
 
 --impl reference times the reference's CPU path (the oracle build of the
 reference where it exists, else the C restatement) on all host cores.
+--only X runs one part alone (the profiling targets of profiles/).
 """
 from __future__ import annotations
 
@@ -440,7 +448,9 @@ def run_ours(args, rank, world, local_rank):
         "gflops": V * FLOPS_PER_SITE / (ms_max * 1e-3) / 1e9 * world,
         "roofline": {"bound": "hbm", "achieved": achieved_1, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved_1 / peaks["hbm_gbs"], "peak_source": peaks["src"],
-                     "traffic": profile_traffic("dslash_f64_24x24x24x48.txt")},
+                     "traffic": profile_traffic("dslash_df64_24x24x24x48.md" if arith == "df64" else
+                                                "dslash_f64_24x24x24x48.md"),
+                     "traffic_source": "profiles/ ncu capture of the same kernel and lattice (dram read + write)"},
         "kernels_ms": {"f64": ms_native, "df64": ms_df64},
         "e2e": {"value": V * bps / (ms_e2e * 1e-3) / 1e9 * world, "unit": "GB/s", "ms_per_step": ms_e2e,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -463,6 +473,16 @@ def run_only(args):
 
     import qcd_gb300 as q
 
+    if args.only == "solve":
+        # one point-source column solved to 1e-10 (even/odd CGNR, FP16 inner)
+        g = q.Gauge(L_BENCH, THETA).synthetic(1000, EPS_PLAQ_060)
+        b, x = q.Field(L_BENCH).point((0, 0, 0, 0), 0, 0), q.Field(L_BENCH)
+        q.sync()
+        t0 = time.perf_counter()
+        p = q.solve(x, b, g, KAPPA, 0.0, solver=q.SOLVER_CGNR_EO, inner_prec=q.F16, tol=1e-10, maxiter=args.steps)
+        q.sync()
+        return {"only": "solve", "s": time.perf_counter() - t0, "iters": p.iters, "status": p.status,
+                "true_residual": p.true_residual}
     if args.only == "batch":
         # batched multi-RHS solve of point-source columns on the bench lattice
         g = q.Gauge(L_BENCH, THETA).synthetic(1000, EPS_PLAQ_060)
@@ -545,7 +565,7 @@ def main():
     ap.add_argument("--eo", action="store_true", help="--only batch: even/odd preconditioned batch")
     ap.add_argument("--mrhs-variant", type=int, default=-1,
                     help="--only mrhs: -1 tuned, 1 tensor cores, 64/128/256 SIMT block size")
-    ap.add_argument("--only", choices=["f64", "df64", "f32", "f16", "mrhs", "batch"],
+    ap.add_argument("--only", choices=["f64", "df64", "f32", "f16", "mrhs", "batch", "solve"],
                     help="profiling target: time only this operator variant (a few launches under ncu)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -175,6 +175,19 @@ int qcd_apeSmear3d(qcd_gaugeField *apeu, qcd_gaugeField *u, qcd_real_8 alpha);
 int qcd_gaussIteration3d(qcd_vector *v, qcd_gaugeField *u, qcd_real_8 alpha, qcd_uint_4 t);
 qcd_real_8 qcd_calculatePlaquette(qcd_gaugeField *u);
 
+/* LIME files, include/qcd_io.h:26-43 (lib/src/qcd_io.c:204-540,984-1150,
+ * 1766-1950). ILDG gauge configurations (precision 64 or 32, big-endian,
+ * file order t,z,y,x and link directions x,y,z,t) and ETMC spinor files
+ * ("etmc-propagator-format" / "etmc-source-format" + "scidac-binary-data").
+ * Writers produce FP64 files with qcd_lib's records. Differences: all of a
+ * 32-bit gauge file is byte-swapped (qcd_io.c:377 swaps one time-slice's
+ * worth); getGaugeField knows type qcd_GF_LIME (0) only. Return 0 or 1. */
+int qcd_getGaugeLime(char *fname, qcd_gaugeField *u);
+int qcd_getGaugeField(char *fname, int type, qcd_gaugeField *u);
+int qcd_writeGaugeLime(char *fname, qcd_gaugeField *u, char *message);
+int qcd_getVectorLime(char *fname, qcd_vector *v);
+int qcd_writeVectorLime(char *fname, int type, qcd_vector *v);
+
 /* include/qcd_communication.h:12,21 (lib/src/qcd_communication.c:20,:343).
  * One GPU holds the whole lattice: no halo exists, both are no-ops that keep
  * the reference's "communication already in flight" check. */
@@ -341,6 +354,12 @@ int qcdgpu_dot_noalloc(const double *a, const double *b, int64_t n, double *resu
  * of the 24^3 x 48 workload: a unit point at x (t, x, y, z), spin, colour,
  * Gaussian-smeared gauss_n times with gauss_alpha on links APE-smeared ape_n
  * times with ape_alpha (on time-slice x[0]). Return 0, or 1 on error. */
+/* LIME files straight into / out of device fields (byte order and site
+ * order converted on the GPU); source != 0 writes an ETMC source file */
+int qcdgpu_gauge_load_lime(qcdgpu_gauge g, const char *fname);
+int qcdgpu_gauge_save_lime(qcdgpu_gauge g, const char *fname, const char *message);
+int qcdgpu_field_load_lime(qcdgpu_field f, const char *fname);
+int qcdgpu_field_save_lime(qcdgpu_field f, const char *fname, int source);
 int qcdgpu_gauge_ape3d(qcdgpu_gauge out, qcdgpu_gauge in, double alpha, int n);
 int qcdgpu_field_gauss3d(qcdgpu_field v, qcdgpu_gauge g, double alpha, int t, int n);
 int qcdgpu_smeared_source(qcdgpu_field f, qcdgpu_gauge g, const int x[4], int spin, int colour, double ape_alpha,

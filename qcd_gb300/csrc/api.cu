@@ -533,6 +533,88 @@ qcd_real_8 qcd_calculatePlaquette(qcd_gaugeField *u)
   return plaquette(g);
 }
 
+// ------------------------------------------------------------ LIME files
+// include/qcd_io.h:26 (lib/src/qcd_io.c:204): ILDG configuration into u
+int qcd_getGaugeLime(char *fname, qcd_gaugeField *u)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!u || !u->initialized || !u->D || !u->geo || u->geo->initialized != 1) {
+    set_error("qcd_getGaugeLime: gauge field must be properly initialized");
+    return 1;
+  }
+  int L[4];
+  geo_L(u->geo, L);
+  const size_t bytes = (size_t)u->geo->V * 72 * sizeof(double);
+  void *dev = nullptr;
+  bool ok = QG_CUDA(cudaMalloc(&dev, bytes)) && lime_read_gauge(fname, L, dev) &&
+            QG_CUDA(cudaMemcpy(u->D, dev, bytes, cudaMemcpyDeviceToHost));
+  auto it = g_gauge.find((const void *)u->D);
+  if (ok && it != g_gauge.end() && it->second.g) {
+    gauge_forget(it->second.g);
+    if (it->second.resident) ok = pack_gauge(it->second.g, dev) && QG_CUDA(cudaStreamSynchronize(stream()));
+  }
+  if (dev) cudaFree(dev);
+  return ok ? 0 : 1;
+}
+
+// include/qcd_io.h:27 (lib/src/qcd_io.c:401): type qcd_GF_LIME (0) only
+int qcd_getGaugeField(char *fname, int type, qcd_gaugeField *u)
+{
+  if (type != 0) {
+    set_error("qcd_getGaugeField: unknown type %d (LIME = 0)", type);
+    return 1;
+  }
+  return qcd_getGaugeLime(fname, u);
+}
+
+// include/qcd_io.h:29 (lib/src/qcd_io.c:419): FP64 ILDG file with an xlf-info message
+int qcd_writeGaugeLime(char *fname, qcd_gaugeField *u, char *message)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  qcdgpu_gauge g = gauge_in(u);  // the device copy (uploaded unless resident)
+  if (!g) return 1;
+  const size_t bytes = (size_t)g->V * 72 * sizeof(double);
+  void *dev = nullptr;
+  bool ok = QG_CUDA(cudaMalloc(&dev, bytes)) && gauge_to_aos_dev(g, dev) &&
+            lime_write_gauge(fname, g->L, dev, message);
+  if (dev) cudaFree(dev);
+  return ok ? 0 : 1;
+}
+
+// include/qcd_io.h:36 (lib/src/qcd_io.c:984): ETMC spinor file into v
+int qcd_getVectorLime(char *fname, qcd_vector *v)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  qcdgpu_field f = vec_out(v);
+  if (!f) return 1;
+  const size_t bytes = (size_t)f->V * 24 * sizeof(double);
+  void *dev = nullptr;
+  bool ok = QG_CUDA(cudaMalloc(&dev, bytes)) && lime_read_spinor(fname, f->L, dev) && spinor_from_aos_dev(f, dev);
+  if (dev) {
+    cudaStreamSynchronize(stream());
+    cudaFree(dev);
+  }
+  return ok && vec_done(v) ? 0 : 1;
+}
+
+// include/qcd_io.h:43 (lib/src/qcd_io.c:1766): type qcd_PROP_LIME (3) or qcd_SOURCE_LIME (4)
+int qcd_writeVectorLime(char *fname, int type, qcd_vector *v)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (type != 3 && type != 4) {
+    set_error("qcd_writeVectorLime: type must be qcd_PROP_LIME (3) or qcd_SOURCE_LIME (4)");
+    return 1;
+  }
+  qcdgpu_field f = vec_in(v);
+  if (!f) return 1;
+  const size_t bytes = (size_t)f->V * 24 * sizeof(double);
+  void *dev = nullptr;
+  bool ok = QG_CUDA(cudaMalloc(&dev, bytes)) && spinor_to_aos_dev(f, dev) &&
+            lime_write_spinor(fname, f->L, dev, type == 4);
+  if (dev) cudaFree(dev);
+  return ok ? 0 : 1;
+}
+
 // --------------------------------------------------------------- solvers
 qcd_int_4 gcr(qcd_vector *sol, qcd_vector *src, qcd_gaugeField *u, qcd_real_8 kappa, qcd_real_8 muTM,
               qcd_uint_4 n, qcd_geometry *geo)

@@ -370,24 +370,25 @@ int solve_cgnr_eo(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, do
   if (!bd || !gi || !be || !bo || !to || !ce || !xe || !xo || !ti || !t64 || !tin) return 3;
   // c_e = b_e + H_eo A^{-1} b_o / 2
   if (!eo_split(be, bo, bd) || !eo_diag(to, bo, mp4, tm, true)) return 3;
-  if (!dslash_eo(ce, to, be, g, mp4, tm, false, 0, 0.5, false, 1, nullptr)) return 3;
+  if (!dslash_eo(ce, to, be, g, mp4, tm, false, 0, 0.5, false, 1, nullptr, QCDGPU_ARITH_DF64)) return 3;
   CgOps ops;
   memcpy(ops.L, Lh, sizeof(ops.L));
+  const int ar = QCDGPU_ARITH_DF64;  // FP64 fields: float-float arithmetic
   ops.op = [&](qcdgpu_field o, qcdgpu_field i, double *part) {
-    return dslash_eo(ti, i, nullptr, gi, mp4, tm, false, 1, 1.0, true, 0, nullptr) &&
-           dslash_eo(o, ti, i, gi, mp4, tm, false, 0, -0.25, false, 2, part);
+    return dslash_eo(ti, i, nullptr, gi, mp4, tm, false, 1, 1.0, true, 0, nullptr, ar) &&
+           dslash_eo(o, ti, i, gi, mp4, tm, false, 0, -0.25, false, 2, part, ar);
   };
   ops.opdag = [&](qcdgpu_field o, qcdgpu_field i) {
-    return dslash_eo(ti, i, nullptr, gi, mp4, tm, true, 1, 1.0, true, 0, nullptr) &&
-           dslash_eo(o, ti, i, gi, mp4, tm, true, 0, -0.25, false, 2, nullptr);
+    return dslash_eo(ti, i, nullptr, gi, mp4, tm, true, 1, 1.0, true, 0, nullptr, ar) &&
+           dslash_eo(o, ti, i, gi, mp4, tm, true, 0, -0.25, false, 2, nullptr, ar);
   };
   ops.op64 = [&](qcdgpu_field o, qcdgpu_field i) {
-    return dslash_eo(t64, i, nullptr, g, mp4, tm, false, 1, 1.0, true, 0, nullptr) &&
-           dslash_eo(o, t64, i, g, mp4, tm, false, 0, -0.25, false, 2, nullptr);
+    return dslash_eo(t64, i, nullptr, g, mp4, tm, false, 1, 1.0, true, 0, nullptr, ar) &&
+           dslash_eo(o, t64, i, g, mp4, tm, false, 0, -0.25, false, 2, nullptr, ar);
   };
   ops.opdag64 = [&](qcdgpu_field o, qcdgpu_field i) {
-    return dslash_eo(t64, i, nullptr, g, mp4, tm, true, 1, 1.0, true, 0, nullptr) &&
-           dslash_eo(o, t64, i, g, mp4, tm, true, 0, -0.25, false, 2, nullptr);
+    return dslash_eo(t64, i, nullptr, g, mp4, tm, true, 1, 1.0, true, 0, nullptr, ar) &&
+           dslash_eo(o, t64, i, g, mp4, tm, true, 0, -0.25, false, 2, nullptr, ar);
   };
   if (prec != QCDGPU_F64)
     ops.restart = [&](qcdgpu_field rs, qcdgpu_field rt, double *rr) {
@@ -396,7 +397,7 @@ int solve_cgnr_eo(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, do
   const int st = cgnr_core(xe, ce, sqrt(bn2), ops, p);
   if (st == 3) return 3;
   // x_o = A^{-1} b_o + A^{-1} H_oe x_e / 2, then the full true residual
-  if (!dslash_eo(xo, xe, to, g, mp4, tm, false, 1, 0.5, true, 1, nullptr) || !eo_merge(x, xe, xo)) return 3;
+  if (!dslash_eo(xo, xe, to, g, mp4, tm, false, 1, 0.5, true, 1, nullptr, ar) || !eo_merge(x, xe, xo)) return 3;
   qcdgpu_field rt = w.get(b->L, QCDGPU_F64);
   double r2;
   if (!rt || !dslash(rt, x, g, mp4, tm, QCDGPU_OP_D, QCDGPU_ARITH_DF64) ||

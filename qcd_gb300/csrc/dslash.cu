@@ -19,7 +19,7 @@ using namespace qgd;
 
 
 // float-float kernel for FP64 storage (dslash_df64.cu)
-bool dslash_df64(const DArgs &a, bool dag);
+bool dslash_df64(const DArgs &a, bool dag, bool eo = false);
 
 template <bool DAG>
 static bool launch_native(const DArgs &a, int prec, int recon)
@@ -125,7 +125,7 @@ bool dslash(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4, doubl
 // with A = mp4 + i tm g5 (D^+: tm -> -tm and the hopping term of D^+).
 // in, out, z are fields on the half lattice {L_t / 2, L_x, L_y, L_z}.
 bool dslash_eo(qcdgpu_field out, qcdgpu_field in, qcdgpu_field z, qcdgpu_gauge g, double mp4, double tm, bool dag,
-               int par, double ch, bool ainv, int zmode, double *partials)
+               int par, double ch, bool ainv, int zmode, double *partials, int arith)
 {
   if (!out || !in || !g || out == in || (zmode && (!z || z == out)) || in->prec != out->prec ||
       in->prec != g->prec || (z && z->prec != in->prec) || g->L[0] % 2 != 0 || in->L[0] * 2 != g->L[0] ||
@@ -178,6 +178,14 @@ bool dslash_eo(qcdgpu_field out, qcdgpu_field in, qcdgpu_field z, qcdgpu_gauge g
   split_host(a.ch, &a.ch_h, &a.ch_l);
   split_host(a.ai_r, &a.ai_r_h, &a.ai_r_l);
   split_host(a.ai_i, &a.ai_i_h, &a.ai_i_l);
+  if (in->prec == QCDGPU_F64 && arith == QCDGPU_ARITH_DF64) {
+    // float-pair copy of the links (phases folded in)
+    qcdgpu_gauge gf = gauge_at(g, kGaugeFF);
+    if (!gf) return false;
+    a.gauge = gf->data;
+    a.gstride = gf->stride;
+    return dslash_df64(a, dag, true);
+  }
   const unsigned grid = (unsigned)((a.V + 127) / 128);
   cudaStream_t s = stream();
 #define QG_EO(SP, RECON, R)                                                        \

@@ -190,19 +190,31 @@ __device__ __forceinline__ CF coef(CF z, bool ifl, bool ng)
 // (qcd_wilson.h:17-387).
 constexpr int kFFSites = 128;
 
-template <bool DAG>
+// EO: even/odd kernel on half fields (sites of parity a.eo_par; neighbours
+// read at (full index) >> 1) with the epilogue ch * [A^{-1}] H in + {z | A z}
+template <bool DAG, bool EO>
 __global__ void __launch_bounds__(384, 3) k_wilson_ff(const DArgs a)
 {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int grp = w / 3, col = w - 3 * grp;
-  const int x = blockIdx.x * kFFSites + grp * 32 + lane;
-  const bool act = x < a.V;
+  const int e = blockIdx.x * kFFSites + grp * 32 + lane;  // output index
+  const bool act = e < a.V;
   __shared__ CF hs[4][2][3][32];
   const double2 *sp = (const double2 *)a.in;
   const float4 *gf = (const float4 *)a.gauge;
   constexpr int SF = DAG ? +1 : -1;
   int c[4] = {0, 0, 0, 0};
-  if (act) coords(a.geo, x, c);
+  int x = e;
+  if (act) {
+    if (EO) {  // the site of parity eo_par among full indices 2e, 2e + 1 (even t extent)
+      coords(a.geo, 2 * e, c);
+      const int b = (a.eo_par ^ c[1] ^ c[2] ^ c[3]) & 1;
+      x = 2 * e + b;
+      c[0] += b;
+    } else {
+      coords(a.geo, x, c);
+    }
+  }
   CA acc[4];
 #pragma unroll
   for (int s = 0; s < 4; s++) acc[s] = CA{{0.f, 0.f}, {0.f, 0.f}};
@@ -224,8 +236,9 @@ __global__ void __launch_bounds__(384, 3) k_wilson_ff(const DArgs a)
     const bool neg0 = S > 0, neg1 = mu < 2 ? S > 0 : S < 0;
     CF h0 = {{0.f, 0.f}, {0.f, 0.f}}, h1 = h0;
     if (act) {
-      CF p0 = load_sp(sp, a.stride, y, col), p1 = load_sp(sp, a.stride, y, 3 + col);
-      CF q0 = load_sp(sp, a.stride, y, 3 * b0 + col), q1 = load_sp(sp, a.stride, y, 3 * b1 + col);
+      const int ys = EO ? (y >> 1) : y;
+      CF p0 = load_sp(sp, a.stride, ys, col), p1 = load_sp(sp, a.stride, ys, 3 + col);
+      CF q0 = load_sp(sp, a.stride, ys, 3 * b0 + col), q1 = load_sp(sp, a.stride, ys, 3 * b1 + col);
       h0 = cadd(p0, coef(q0, odd, neg0));
       h1 = cadd(p1, coef(q1, odd, neg1));
     }
@@ -258,7 +271,45 @@ __global__ void __launch_bounds__(384, 3) k_wilson_ff(const DArgs a)
     __syncthreads();  // hs is rewritten by the next hop
   }
   double n2 = 0.0;
-  if (act) {
+  if (EO && act) {
+    double2 *out = (double2 *)a.out;
+    const F2 mp4{a.mp4_h, a.mp4_l}, tm{a.tm_h, a.tm_l}, ch{a.ch_h, a.ch_l};
+    const F2 air{a.ai_r_h, a.ai_r_l}, aii{a.ai_i_h, a.ai_i_l};
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+      const int k = 3 * s + col;
+      F2 hr = fin(acc[s].re), hi = fin(acc[s].im);
+      if (a.ainv) {  // (ai_r + i ai_i g5) H in
+        const F2 gi = s < 2 ? aii : neg(aii);
+        FA re{0.f, 0.f}, im{0.f, 0.f};
+        mac(re, air, hr);
+        mac(re, neg(gi), hi);
+        mac(im, air, hi);
+        mac(im, gi, hr);
+        hr = fin(re);
+        hi = fin(im);
+      }
+      FA re{0.f, 0.f}, im{0.f, 0.f};
+      mac(re, ch, hr);
+      mac(im, ch, hi);
+      if (a.zmode) {
+        const CF zv = load_sp((const double2 *)a.z, a.stride, e, k);
+        if (a.zmode == 2) {  // + (m+4) z + i tm g5 z
+          const F2 g5tm = s < 2 ? tm : neg(tm);
+          mac(re, mp4, zv.re);
+          mac(re, neg(g5tm), zv.im);
+          mac(im, mp4, zv.im);
+          mac(im, g5tm, zv.re);
+        } else {
+          acc_add(re, zv.re);
+          acc_add(im, zv.im);
+        }
+      }
+      const double vr = join_d(fin(re)), vi = join_d(fin(im));
+      out[(int64_t)k * a.stride + e] = make_double2(vr, vi);
+      n2 += vr * vr + vi * vi;
+    }
+  } else if (act) {
     double2 *out = (double2 *)a.out;
     const F2 mp4{a.mp4_h, a.mp4_l}, tm{a.tm_h, a.tm_l};
 #pragma unroll
@@ -341,11 +392,16 @@ bool gauge_to_ff(qcdgpu_gauge d, qcdgpu_gauge s)
   return QG_LAUNCHED("gauge_to_ff");
 }
 
-bool dslash_df64(const DArgs &a, bool dag)
+bool dslash_df64(const DArgs &a, bool dag, bool eo)
 {
   unsigned grid = (unsigned)((a.V + kFFSites - 1) / kFFSites);
-  if (dag) k_wilson_ff<true><<<grid, 384, 0, stream()>>>(a);
-  else k_wilson_ff<false><<<grid, 384, 0, stream()>>>(a);
+  if (eo) {
+    if (dag) k_wilson_ff<true, true><<<grid, 384, 0, stream()>>>(a);
+    else k_wilson_ff<false, true><<<grid, 384, 0, stream()>>>(a);
+  } else {
+    if (dag) k_wilson_ff<true, false><<<grid, 384, 0, stream()>>>(a);
+    else k_wilson_ff<false, false><<<grid, 384, 0, stream()>>>(a);
+  }
   return QG_LAUNCHED("wilson_df64");
 }
 

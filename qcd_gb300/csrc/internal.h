@@ -117,14 +117,26 @@ bool convert_gauge(qcdgpu_gauge dst, qcdgpu_gauge src, int force_recon = 0);
 // SU(3)-check + packing of a gauge field held there in the host layout
 void *stage_buffer(size_t bytes);
 bool pack_gauge(qcdgpu_gauge g, const void *dev_aos);
+// the same conversions from / to the host layout held in device memory
+bool spinor_from_aos_dev(qcdgpu_field f, const void *dev_aos);
+bool spinor_to_aos_dev(qcdgpu_field f, void *dev_aos);
+bool gauge_to_aos_dev(qcdgpu_gauge g, void *dev_aos);
+
+// lime.cu: LIME files (ILDG gauge fields, ETMC spinors) <-> the host layout
+// [V][4][3][3] / [V][4][3] complex double in device memory
+bool lime_read_gauge(const char *fname, const int L[4], void *dev_aos);
+bool lime_write_gauge(const char *fname, const int L[4], const void *dev_aos, const char *message);
+bool lime_read_spinor(const char *fname, const int L[4], void *dev_aos);
+bool lime_write_spinor(const char *fname, const int L[4], const void *dev_aos, bool source);
 
 // dslash.cu: out = op(in) with diagonal mp4 = m + 4 and twisted mass tm
 bool dslash(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4, double tm, int op,
             int arith);
 // even/odd kernel on half fields {L_t/2, L_x, L_y, L_z} (native arithmetic):
 // out (parity par) = ch * [A^{-1}] H in + {0 | z | A z}, A = mp4 + i tm g5
+// arith: QCDGPU_ARITH_DF64 runs FP64 fields in float-float arithmetic
 bool dslash_eo(qcdgpu_field out, qcdgpu_field in, qcdgpu_field z, qcdgpu_gauge g, double mp4, double tm, bool dag,
-               int par, double ch, bool ainv, int zmode, double *partials);
+               int par, double ch, bool ainv, int zmode, double *partials, int arith = QCDGPU_ARITH_F64);
 
 // cg.cu: even/odd helpers -- full FP64 field <-> its two half fields, and
 // out = A in or A^{-1} in on a half field (A = mp4 + i tm g5)

@@ -282,6 +282,43 @@ bool pack_gauge(qcdgpu_gauge g, const void *dev_aos)
 
 void *stage_buffer(size_t bytes) { return stage(bytes); }
 
+// spinor field <-> the host layout [V][4][3] complex double held in device memory
+bool spinor_from_aos_dev(qcdgpu_field f, const void *dev_aos)
+{
+  unsigned g = grid_for(f->V, 128);
+  const double2 *a = (const double2 *)dev_aos;
+  switch (f->prec) {
+  case QCDGPU_F64: k_spinor_aos_to_soa<QCDGPU_F64><<<g, 128, 0, stream()>>>(f->data, f->norm, f->stride, a, f->V); break;
+  case QCDGPU_F32: k_spinor_aos_to_soa<QCDGPU_F32><<<g, 128, 0, stream()>>>(f->data, f->norm, f->stride, a, f->V); break;
+  default: k_spinor_aos_to_soa<QCDGPU_F16><<<g, 128, 0, stream()>>>(f->data, f->norm, f->stride, a, f->V);
+  }
+  return QG_LAUNCHED("spinor_aos_to_soa");
+}
+
+bool spinor_to_aos_dev(qcdgpu_field f, void *dev_aos)
+{
+  unsigned g = grid_for(f->V, 128);
+  double2 *a = (double2 *)dev_aos;
+  switch (f->prec) {
+  case QCDGPU_F64: k_spinor_soa_to_aos<QCDGPU_F64><<<g, 128, 0, stream()>>>(a, f->data, f->norm, f->stride, f->V); break;
+  case QCDGPU_F32: k_spinor_soa_to_aos<QCDGPU_F32><<<g, 128, 0, stream()>>>(a, f->data, f->norm, f->stride, f->V); break;
+  default: k_spinor_soa_to_aos<QCDGPU_F16><<<g, 128, 0, stream()>>>(a, f->data, f->norm, f->stride, f->V);
+  }
+  return QG_LAUNCHED("spinor_soa_to_aos");
+}
+
+// gauge field -> the host layout [V][4][3][3] complex double in device memory
+bool gauge_to_aos_dev(qcdgpu_gauge g, void *dev_aos)
+{
+  unsigned gr = grid_for(g->V * 4, 128);
+  double2 *d = (double2 *)dev_aos;
+  if (g->prec == QCDGPU_F64) k_gauge_soa_to_aos<QCDGPU_F64, 18><<<gr, 128, 0, stream()>>>(d, g->data, g->stride, g->V);
+  else if (g->prec == QCDGPU_F32 && g->recon == 12) k_gauge_soa_to_aos<QCDGPU_F32, 12><<<gr, 128, 0, stream()>>>(d, g->data, g->stride, g->V);
+  else if (g->prec == QCDGPU_F32) k_gauge_soa_to_aos<QCDGPU_F32, 18><<<gr, 128, 0, stream()>>>(d, g->data, g->stride, g->V);
+  else k_gauge_soa_to_aos<QCDGPU_F16, 12><<<gr, 128, 0, stream()>>>(d, g->data, g->stride, g->V);
+  return QG_LAUNCHED("gauge_soa_to_aos");
+}
+
 bool upload_gauge_aos(qcdgpu_gauge g, const double *host)
 {
   std::lock_guard<std::mutex> lk(g_stage_mu);

@@ -291,9 +291,13 @@ __device__ __forceinline__ void mhop_pair(const MArgs &a, int x, const int c[4],
   }
 }
 
-template <bool DAG, int RP, bool EO>
+// MODE 0: full lattice, out = A in - H in / 2. Even/odd (half fields): MODE 1
+// out = A^{-1} H in; MODE 2 out = A z - H in / 4 (the two halves of the Schur
+// complement). The epilogue is fixed at compile time for each mode.
+template <bool DAG, int RP, int MODE>
 __global__ void __launch_bounds__(256) k_wilson_mrhs_simt(const MArgs a, double *partials)
 {
+  constexpr bool EO = MODE != 0;
   const int r0 = threadIdx.x * RP;
   const int e = blockIdx.x * blockDim.y + threadIdx.y;  // output index
   double n2[RP];
@@ -318,16 +322,19 @@ __global__ void __launch_bounds__(256) k_wilson_mrhs_simt(const MArgs a, double 
     mhop_pair<1, DAG, RP, EO>(a, x, c, r0, acc);
     mhop_pair<2, DAG, RP, EO>(a, x, c, r0, acc);
     mhop_pair<3, DAG, RP, EO>(a, x, c, r0, acc);
+    constexpr int zmode = MODE == 1 ? 0 : 2;
+    constexpr bool ainv = MODE == 1;
+    constexpr float ch = MODE == 0 ? -0.5f : MODE == 1 ? 1.0f : -0.25f;
     C<float> s[RP][12];
     float nrm[RP];
-    if (a.zmode) mload_rp<RP>(a, a.z, a.z_norm, e, r0, s, nrm);
+    if (zmode) mload_rp<RP>(a, EO ? a.z : a.in, EO ? a.z_norm : a.in_norm, e, r0, s, nrm);
 #pragma unroll
     for (int q = 0; q < RP; q++) {
       const int r = r0 + q;
       // slots past nact hold zeros; their results are not stored
       const float mp4r = a.mp4s ? a.mp4s[r] : a.mp4;
       const float tmr = a.tms ? (DAG ? -a.tms[r] : a.tms[r]) : a.tm;
-      if (a.ainv) {  // A^{-1} = (mp4 - i tm g5) / (mp4^2 + tm^2)
+      if (ainv) {  // A^{-1} = (mp4 - i tm g5) / (mp4^2 + tm^2)
         const float den = 1.0f / (mp4r * mp4r + tmr * tmr), ar = mp4r * den, ai = -tmr * den;
 #pragma unroll
         for (int k = 0; k < 12; k++) {
@@ -335,15 +342,15 @@ __global__ void __launch_bounds__(256) k_wilson_mrhs_simt(const MArgs a, double 
           acc[q][k] = C<float>{ar * acc[q][k].re - g5ai * acc[q][k].im, ar * acc[q][k].im + g5ai * acc[q][k].re};
         }
       }
-      const float zs = a.zmode ? nrm[q] : 0.f;
-      const float zm = a.zmode == 2 ? mp4r * zs : zs, zt = a.zmode == 2 ? tmr * zs : 0.f;
+      const float zs = zmode ? nrm[q] : 0.f;
+      const float zm = zmode == 2 ? mp4r * zs : zs, zt = zmode == 2 ? tmr * zs : 0.f;
       float mx = 0.f;
 #pragma unroll
       for (int k = 0; k < 12; k++) {
         const float g5tm = k < 6 ? zt : -zt;
-        const C<float> zk = a.zmode ? s[q][k] : C<float>{0.f, 0.f};
-        acc[q][k] = C<float>{zm * zk.re - g5tm * zk.im + a.ch * acc[q][k].re,
-                             zm * zk.im + g5tm * zk.re + a.ch * acc[q][k].im};
+        const C<float> zk = zmode ? s[q][k] : C<float>{0.f, 0.f};
+        acc[q][k] = C<float>{zm * zk.re - g5tm * zk.im + ch * acc[q][k].re,
+                             zm * zk.im + g5tm * zk.re + ch * acc[q][k].im};
         mx = fmaxf(mx, fmaxf(fabsf(acc[q][k].re), fabsf(acc[q][k].im)));
       }
       if (!(mx >= 1.17549435e-38f)) mx = 0.f;
@@ -542,18 +549,27 @@ static bool launch_mrhs(const MArgs &a, bool dag, MrhsTune t, double *partials, 
   const size_t shm = sizeof(double) * a.N * blk.y;
   if (simt) {
     const size_t sm = partials ? shm : 0;
-    const bool eo = a.eo_par >= 0;
-#define QG_SIMT(RP, EO)                                                             \
-  if (dag) k_wilson_mrhs_simt<true, RP, EO><<<nb, blk, sm, s>>>(a, partials);       \
-  else k_wilson_mrhs_simt<false, RP, EO><<<nb, blk, sm, s>>>(a, partials);
-    if (t.rp == 2 && eo) {
-      QG_SIMT(2, true)
-    } else if (t.rp == 2) {
-      QG_SIMT(2, false)
-    } else if (eo) {
-      QG_SIMT(1, true)
+    // kernel mode from the epilogue (see k_wilson_mrhs_simt)
+    const int mode = a.eo_par < 0 ? 0 : a.ainv ? 1 : 2;
+#define QG_SIMT(RP, MODE)                                                           \
+  if (dag) k_wilson_mrhs_simt<true, RP, MODE><<<nb, blk, sm, s>>>(a, partials);     \
+  else k_wilson_mrhs_simt<false, RP, MODE><<<nb, blk, sm, s>>>(a, partials);
+    if (t.rp == 2) {
+      if (mode == 0) {
+        QG_SIMT(2, 0)
+      } else if (mode == 1) {
+        QG_SIMT(2, 1)
+      } else {
+        QG_SIMT(2, 2)
+      }
     } else {
-      QG_SIMT(1, false)
+      if (mode == 0) {
+        QG_SIMT(1, 0)
+      } else if (mode == 1) {
+        QG_SIMT(1, 1)
+      } else {
+        QG_SIMT(1, 2)
+      }
     }
 #undef QG_SIMT
     if (!QG_LAUNCHED("wilson_mrhs_simt")) return false;
@@ -584,16 +600,15 @@ static bool launch_mrhs(const MArgs &a, bool dag, MrhsTune t, double *partials, 
 // three times on the caller's fields (the output is overwritten with the
 // same result). Not while the stream is being captured: then the SIMT
 // variant with 256-thread blocks runs until a tuned choice exists.
-static MrhsTune mrhs_tune(const MArgs &a, bool dag, qcdgpu_mfield out, qcdgpu_mfield in)
+static MrhsTune mrhs_tune(const MArgs &a, bool dag)
 {
-  (void)out;
-  (void)in;
   if (g_mrhs_variant == MRHS_MMA) return MrhsTune{MRHS_MMA, 256, 1};
   if (g_mrhs_variant >= 64) {  // forced block size; +1: two slots per thread
     const int rp = (g_mrhs_variant & 1) && a.N % 2 == 0 ? 2 : 1;
     return MrhsTune{MRHS_SIMT, g_mrhs_variant & ~1, rp};
   }
-  const auto key = std::make_pair((int64_t)a.V, a.N);
+  // even/odd kernels are tuned separately (key: minus the half volume)
+  const auto key = std::make_pair(a.eo_par < 0 ? (int64_t)a.V : -(int64_t)a.V, a.N);
   auto it = g_mrhs_tuned.find(key);
   if (it != g_mrhs_tuned.end()) return it->second;
   const MrhsTune fallback{MRHS_SIMT, 128, 1};
@@ -602,6 +617,7 @@ static MrhsTune mrhs_tune(const MArgs &a, bool dag, qcdgpu_mfield out, qcdgpu_mf
   if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return fallback;
   const MrhsTune cands[] = {{MRHS_SIMT, 64, 1}, {MRHS_SIMT, 128, 1}, {MRHS_SIMT, 256, 1}, {MRHS_SIMT, 64, 2},
                             {MRHS_SIMT, 128, 2}, {MRHS_SIMT, 256, 2}, {MRHS_MMA, 256, 1}};
+  const int ncand = a.eo_par < 0 ? 7 : 6;  // no tensor-core even/odd kernel
   cudaEvent_t e0, e1;
   if (cudaEventCreate(&e0) != cudaSuccess) return fallback;
   if (cudaEventCreate(&e1) != cudaSuccess) {
@@ -610,7 +626,8 @@ static MrhsTune mrhs_tune(const MArgs &a, bool dag, qcdgpu_mfield out, qcdgpu_mf
   }
   MrhsTune best = fallback;
   float best_ms = 1e30f;
-  for (const MrhsTune &c : cands) {
+  for (int ic = 0; ic < ncand; ic++) {
+    const MrhsTune &c = cands[ic];
     if (c.variant == MRHS_SIMT && (c.threads < a.N || (c.rp == 2 && a.N % 2 != 0))) continue;
     if (!launch_mrhs(a, dag, c, nullptr, nullptr)) break;  // warm-up
     cudaEventRecord(e0, s);
@@ -688,7 +705,7 @@ bool dslash_mrhs(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_gauge g, double mp4
     if (nblocks) *nblocks = 0;
     return true;
   }
-  const MrhsTune tune = mrhs_tune(a, dag, out, in);
+  const MrhsTune tune = mrhs_tune(a, dag);
   if (!launch_mrhs(a, dag, tune, partials, nblocks)) return false;
   return true;
 }
@@ -745,12 +762,16 @@ bool dslash_mrhs_eo(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_mfield z, qcdgpu
   a.ainv = ainv ? 1 : 0;
   a.ch = (float)ch;
   a.eo_par = par;
+  // the kernels implement the two halves of the Schur complement
+  if (!((ainv && zmode == 0 && ch == 1.0) || (!ainv && zmode == 2 && ch == -0.25))) {
+    set_error("even/odd multi-RHS operator: epilogue A^{-1} H in or A z - H in / 4 only");
+    return false;
+  }
   if (nact == 0) {
     if (nblocks) *nblocks = 0;
     return true;
   }
-  const MrhsTune t{MRHS_SIMT, 128, in->N % 2 == 0 ? 2 : 1};
-  return launch_mrhs(a, dag, t, partials, nblocks);
+  return launch_mrhs(a, dag, mrhs_tune(a, dag), partials, nblocks);
 }
 
 }  // namespace qg

@@ -350,8 +350,9 @@ static bool slot_residual(qcdgpu_batch B, int k, const BSlot &sl, double *rel, d
   if (B->eo) {
     qcdgpu_gauge g32 = gauge_at(B->g, QCDGPU_F32);
     double n2;
-    if (!g32 || !dslash_eo(B->u64, sl.xe, nullptr, B->g, sl.mp4, sl.tm, false, 1, 1.0, true, 0, nullptr) ||
-        !dslash_eo(B->rt, B->u64, sl.xe, B->g, sl.mp4, sl.tm, false, 0, -0.25, false, 2, nullptr) ||
+    const int ar = QCDGPU_ARITH_DF64;
+    if (!g32 || !dslash_eo(B->u64, sl.xe, nullptr, B->g, sl.mp4, sl.tm, false, 1, 1.0, true, 0, nullptr, ar) ||
+        !dslash_eo(B->rt, B->u64, sl.xe, B->g, sl.mp4, sl.tm, false, 0, -0.25, false, 2, nullptr, ar) ||
         !blas_axpby(B->rt, 1.0, 0.0, sl.ce, -1.0, 0.0, B->rt) || !blas_norm2(B->rt, &n2))
       return false;
     *rel = sl.bn > 0 ? sqrt(n2) / sl.bn : 0.0;
@@ -430,7 +431,8 @@ int batch_add(qcdgpu_batch B, qcdgpu_field x, qcdgpu_field b, double kappa, doub
     sl.to = set[1];
     sl.xe = set[2];
     const bool ok = slot_bd(B, sl) && eo_split(B->rt, B->r, B->bd) && eo_diag(sl.to, B->r, sl.mp4, mu, true) &&
-                    dslash_eo(sl.ce, sl.to, B->rt, B->g, sl.mp4, mu, false, 0, 0.5, false, 1, nullptr) &&
+                    dslash_eo(sl.ce, sl.to, B->rt, B->g, sl.mp4, mu, false, 0, 0.5, false, 1, nullptr,
+                              QCDGPU_ARITH_DF64) &&
                     blas_zero(sl.xe);
     if (!ok) {
       B->spare.push_back(set);
@@ -475,7 +477,7 @@ static bool retire(qcdgpu_batch B, int k, int status)
   BSlot &sl = B->slots[(size_t)k];
   if (B->eo) {
     // x_o = A^{-1} b_o + A^{-1} H_oe x_e / 2, then x = (x_e, x_o)
-    if (!dslash_eo(B->r, sl.xe, sl.to, B->g, sl.mp4, sl.tm, false, 1, 0.5, true, 1, nullptr) ||
+    if (!dslash_eo(B->r, sl.xe, sl.to, B->g, sl.mp4, sl.tm, false, 1, 0.5, true, 1, nullptr, QCDGPU_ARITH_DF64) ||
         !eo_merge(sl.x, sl.xe, B->r))
       return false;
     B->spare.push_back({sl.ce, sl.to, sl.xe});
@@ -550,10 +552,15 @@ bool batch_launch(qcdgpu_batch B)
   StreamScope scope(B->st);
   const int n = B->nchunk;
   if (!gauge_at(B->g, kGaugeF32Full)) return false;  // resident before any capture
-  if (!B->tuned && !B->eo) {
-    // the operator's tuner times its variants outside stream capture; t is
-    // scratch (recomputed by every iteration)
-    if (!dslash_mrhs(B->t, B->ps, B->g, 4.0, 0.0, false, n, B->mp4s, B->tms)) return false;
+  if (!B->tuned) {
+    // the operator's tuner times its variants outside stream capture; t and
+    // u are scratch (recomputed by every iteration)
+    const bool ok = B->eo ? dslash_mrhs_eo(B->u, B->ps, nullptr, B->g, false, n, B->mp4s, B->tms, 1, 1.0, true, 0,
+                                           nullptr, nullptr) &&
+                                dslash_mrhs_eo(B->t, B->u, B->ps, B->g, false, n, B->mp4s, B->tms, 0, -0.25, false, 2,
+                                               nullptr, nullptr)
+                          : dslash_mrhs(B->t, B->ps, B->g, 4.0, 0.0, false, n, B->mp4s, B->tms);
+    if (!ok) return false;
     B->tuned = true;
   }
   if (B->use_graphs) {
