@@ -365,6 +365,16 @@ int qcdgpu_field_gauss3d(qcdgpu_field v, qcdgpu_gauge g, double alpha, int t, in
 int qcdgpu_smeared_source(qcdgpu_field f, qcdgpu_gauge g, const int x[4], int spin, int colour, double ape_alpha,
                           int ape_n, double gauss_alpha, int gauss_n);
 
+/* Proton two-point function of twop.c (no qcd_lib library counterpart: the
+ * driver twop.c:219-399 computes it inline) on GPU-resident propagators: up
+ * and down each 12 FP64 fields, column nu * 3 + c2 = source spin nu, source
+ * colour c2 (qcd_lib's D[v][mu][nu][c1][c2]). Source at xsrc (t, x, y, z),
+ * theta_t = pi; time-slices t0..t1 relative to the source; mom: nmom
+ * momenta (px, py, pz) in units of 2 pi / L. corr[((t - t0) * nmom + j) * 2
+ * + {0, 1}] = re, im of the correlator twop.c writes. Returns 0 or 1. */
+int qcdgpu_twop_proton(const qcdgpu_field *up, const qcdgpu_field *dn, const int xsrc[4], int t0, int t1,
+                       const int *mom, int nmom, double *corr);
+
 /* ---------------------------------------------------------------------- */
 /* Multi-RHS (no reference counterpart: qcd_lib solves one column at a time,
  * invert.c:255). A multi-RHS field holds up to 64 spinors in FP16 with one

@@ -100,6 +100,8 @@ class Oracle:
         lib.orc_z4_spinor.argtypes = [_dp, C.c_size_t, C.c_uint64]
         lib.orc_gauge_synthetic.argtypes = [_dp, _ip, C.c_uint64, C.c_double]
         lib.orc_gauge_unit.argtypes = [_dp, C.c_size_t]
+        lib.orc_twop_proton.argtypes = [_dp, _dp, _ip, _ip, C.c_int, C.c_int, _ip, C.c_int, _dp]
+        lib.orc_twop_tables.argtypes = [_dp, _dp, _dp]
 
     # --- operator -------------------------------------------------------
     def dslash(self, v, u, L, theta, kappa=None, m=None, tm=0.0, op="D"):
@@ -159,6 +161,23 @@ class Oracle:
     def true_residual(self, x, b, u, L, theta, kappa, mu=0.0, op="D"):
         return self.lib.orc_true_residual(np.ascontiguousarray(x), np.ascontiguousarray(b), u,
                                           _L(L), _th(theta), kappa, mu, {"D": 0, "Q": 1}[op])
+
+    # --- contractions ---------------------------------------------------------
+    def twop_proton(self, up, dn, L, xsrc, t0, t1, moms):
+        """proton two-point function of twop.c: corr[t - t0, j] (complex). The
+        propagators (V, 4, 4, 3, 3, 2) are copied (the oracle phases them in place)."""
+        up = np.array(up, dtype=np.float64, copy=True, order="C")
+        dn = np.array(dn, dtype=np.float64, copy=True, order="C")
+        moms = np.ascontiguousarray(moms, dtype=np.int32).reshape(-1, 3)
+        corr = np.zeros((t1 - t0 + 1, len(moms), 2))
+        self.lib.orc_twop_proton(up, dn, _L(L), np.ascontiguousarray(xsrc, dtype=np.int32), t0, t1, moms,
+                                 len(moms), corr)
+        return corr[..., 0] + 1j * corr[..., 1]
+
+    def twop_tables(self):
+        cg5, bcg5, p13 = np.zeros((4, 4)), np.zeros((4, 4)), np.zeros((4, 4, 2))
+        self.lib.orc_twop_tables(cg5, bcg5, p13)
+        return cg5, bcg5, p13[..., 0] + 1j * p13[..., 1]
 
     # --- setup ----------------------------------------------------------------
     def exp_iM(self, M):
@@ -236,6 +255,9 @@ class Reference:
         lib.ref_project_su3.argtypes = [_dp]
         for n in ("ref_sizeof_geometry", "ref_sizeof_vector", "ref_sizeof_gauge"):
             getattr(lib, n).restype = C.c_size_t
+        lib.ref_io_set.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.ref_twop.argtypes = [C.c_char_p]
+        lib.ref_twop.restype = C.c_int
 
     def dslash(self, v, u, L, theta, kappa=None, m=None, tm=0.0, variant="TMOp", reps=1):
         if m is None:
@@ -279,6 +301,43 @@ class Reference:
         g = np.array(g, dtype=np.float64, copy=True).reshape(3, 3, 2)
         self.lib.ref_project_su3(g)
         return g
+
+    def twop(self, u, up, dn, L, xsrc, t0, t1, moms, nsmear=0, alpha=4.0, nape=0, alpha_ape=0.5):
+        """runs the reference's twop.c main() on in-memory inputs (propagators
+        (V, 4, 4, 3, 3, 2), links (V, 4, 3, 3, 2)); returns corr[t - t0, j]"""
+        import tempfile
+
+        moms = np.asarray(moms, dtype=int).reshape(-1, 3)
+        with tempfile.TemporaryDirectory() as d:
+            mfile, cfile = os.path.join(d, "mom.txt"), os.path.join(d, "corr.dat")
+            with open(mfile, "w") as f:
+                f.write(f"{len(moms)}\n" + "".join(f"{a} {b} {c}\n" for a, b, c in moms))
+            params = (f"<processors_txyz>1 1 1 1</processors_txyz><lattice_txyz>{L[0]} {L[1]} {L[2]} {L[3]}"
+                      f"</lattice_txyz><t>{t0} {t1}</t><source_pos_txyz>{xsrc[0]} {xsrc[1]} {xsrc[2]} {xsrc[3]}"
+                      f"</source_pos_txyz><propagator_u>up</propagator_u><propagator_d>down</propagator_d>"
+                      f"<cfg_name>conf</cfg_name><corr_name>{cfile}</corr_name><momenta_list>{mfile}"
+                      f"</momenta_list><alpha_gauss>{alpha!r}</alpha_gauss><nsmear_gauss>{nsmear}</nsmear_gauss>"
+                      f"<alpha_APE>{alpha_ape!r}</alpha_APE><nsmear_APE>{nape}</nsmear_APE>").encode()
+            keep = [np.ascontiguousarray(u, dtype=np.float64), np.ascontiguousarray(up, dtype=np.float64),
+                    np.ascontiguousarray(dn, dtype=np.float64)]
+            self.lib.ref_io_set(params, *[a.ctypes.data for a in keep])
+            assert self.lib.ref_twop(b"params.txt") == 0
+            self.lib.ref_io_set(None, None, None, None)
+            rows = np.loadtxt(cfile, ndmin=2)
+        corr = np.zeros((t1 - t0 + 1, len(moms)), dtype=complex)
+        for k, row in enumerate(rows):
+            corr[k // len(moms), k % len(moms)] = row[4] + 1j * row[5]
+        return corr
+
+    def twop_tables(self):
+        """qcd_CGAMMA[5], qcd_BAR_CGAMMA[5] and PROJECTOR[13] as compiled"""
+        c16 = C.c_double * (6 * 4 * 4 * 2)
+        cg = np.frombuffer(c16.in_dll(self.lib, "qcd_CGAMMA"), dtype=np.float64).reshape(6, 4, 4, 2)
+        bcg = np.frombuffer(c16.in_dll(self.lib, "qcd_BAR_CGAMMA"), dtype=np.float64).reshape(6, 4, 4, 2)
+        pr = np.frombuffer((C.c_double * (25 * 16 * 2)).in_dll(self.lib, "PROJECTOR"), dtype=np.float64)
+        pr = pr.reshape(25, 4, 4, 2)
+        return (cg[5, ..., 0] + 1j * cg[5, ..., 1], bcg[5, ..., 0] + 1j * bcg[5, ..., 1],
+                pr[13, ..., 0] + 1j * pr[13, ..., 1])
 
     def geometry(self, L, theta=(0, 0, 0, 0)):
         """neighbour tables, even/odd list and edge lists of qcd_initGeometry"""

@@ -760,3 +760,100 @@ void orc_gauge_unit(double *u, size_t V)
   memset(u, 0, V * 4 * 18 * 8);
   for (size_t l = 0; l < V * 4; l++) { u[l * 18 + 0] = 1; u[l * 18 + 8] = 1; u[l * 18 + 16] = 1; }
 }
+
+/* ------------------------------------------------------- contractions */
+
+/* Tables of the proton two-point function (kept identical to the
+ * reference's): the antisymmetric colour permutations qcd_EPS / qcd_SGN_EPS
+ * (lib/src/qcd_gamma.c:13-26), C gamma_5 and its bar (qcd_CGAMMA[5],
+ * qcd_BAR_CGAMMA[5], lib/src/qcd_gamma.c:105-195) and the parity projector
+ * PROJECTOR[13] (projectors.h). */
+static const int TP_EPS[6][3] = {{0, 1, 2}, {2, 0, 1}, {1, 2, 0}, {2, 1, 0}, {0, 2, 1}, {1, 0, 2}};
+static const int TP_SGN[6] = {+1, +1, +1, -1, -1, -1};
+static const double TP_CG5[4][4] = {{0, 1, 0, 0}, {-1, 0, 0, 0}, {0, 0, 0, 1}, {0, 0, -1, 0}};
+static const double TP_BCG5[4][4] = {{0, -1, 0, 0}, {1, 0, 0, 0}, {0, 0, 0, -1}, {0, 0, 1, 0}};
+static const double TP_P13[4][4][2] = {{{0, .5}, {0, 0}, {-.5, 0}, {0, 0}},
+                                       {{0, 0}, {0, .5}, {0, 0}, {-.5, 0}},
+                                       {{-.5, 0}, {0, 0}, {0, -.5}, {0, 0}},
+                                       {{0, 0}, {-.5, 0}, {0, 0}, {0, -.5}}};
+
+void orc_twop_tables(double *cg5, double *bcg5, double *p13)
+{
+  memcpy(cg5, TP_CG5, sizeof(TP_CG5));
+  memcpy(bcg5, TP_BCG5, sizeof(TP_BCG5));
+  memcpy(p13, TP_P13, sizeof(TP_P13));
+}
+
+/* Proton two-point function of twop.c (twop.c:219-226 phases, :264-282
+ * C g5 x bar C g5 entries, :324-399 block and Fourier sum): up and down
+ * propagators D[v][mu][nu][c1][c2] (sink spin, source spin, sink colour,
+ * source colour), source at xsrc (t, x, y, z), theta_t = pi. The
+ * propagators are phased in place: time-slice (t + xsrc_t) % L_t times
+ * exp(i pi t / L_t). corr[(t - t0) * nmom + j] (re, im) for t = t0..t1. */
+void orc_twop_proton(double *up, double *dn, const int L[4], const int xsrc[4], int t0, int t1, const int *mom,
+                     int nmom, double *corr)
+{
+  const size_t V = vol(L), V3 = V / (size_t)L[0];
+  for (int t = 0; t < L[0]; t++) {
+    const double ph = M_PI * t / L[0];
+    const cx f = cmk(cos(ph), sin(ph));
+    const int lt = (t + xsrc[0]) % L[0];
+    for (size_t s = 0; s < V3; s++) {
+      const size_t v = (size_t)lt + (size_t)L[0] * s;
+      cx *pu = (cx *)(up + v * 288), *pd = (cx *)(dn + v * 288);
+      for (int k = 0; k < 144; k++) {
+        pu[k] = cmul(pu[k], f);
+        pd[k] = cmul(pd[k], f);
+      }
+    }
+  }
+  cx *block = malloc(V3 * sizeof(cx));
+  for (int t = t0; t <= t1; t++) {
+    const int lt = (t + xsrc[0]) % L[0];
+    for (size_t s = 0; s < V3; s++) block[s] = cmk(0, 0);
+    for (int al = 0; al < 4; al++)
+      for (int be = 0; be < 4; be++) {
+        const cx P = cmk(TP_P13[al][be][0], TP_P13[al][be][1]);
+        if (P.re * P.re + P.im * P.im <= 1e-8) continue;
+        for (int mu = 0; mu < 4; mu++)
+          for (int nu = 0; nu < 4; nu++)
+            for (int ku = 0; ku < 4; ku++)
+              for (int lu = 0; lu < 4; lu++) {
+                const double C = TP_CG5[mu][nu] * TP_BCG5[ku][lu];
+                if (fabs(C) <= 1e-3) continue;
+                for (int e1 = 0; e1 < 6; e1++)
+                  for (int e2 = 0; e2 < 6; e2++) {
+                    const int c1 = TP_EPS[e1][0], c2 = TP_EPS[e1][1], c3 = TP_EPS[e1][2];
+                    const int d1 = TP_EPS[e2][0], d2 = TP_EPS[e2][1], d3 = TP_EPS[e2][2];
+                    const double sg = (double)(TP_SGN[e1] * TP_SGN[e2]);
+                    for (size_t s = 0; s < V3; s++) {
+                      const size_t v = (size_t)lt + (size_t)L[0] * s;
+#define PR(p, a, b, c, d) (((const cx *)((p) + v * 288))[(((a) * 4 + (b)) * 3 + (c)) * 3 + (d)])
+                      cx term = cmul(cmul(cmul(cmk(C, 0), PR(up, mu, ku, c1, d1)), PR(dn, nu, lu, c2, d2)),
+                                     PR(up, be, al, c3, d3));
+                      block[s] = csub(block[s], cmul(P, cscale(term, sg)));
+                      term = cmul(cmul(cmul(cmk(C, 0), PR(up, mu, al, c1, d1)), PR(dn, nu, lu, c2, d2)),
+                                  PR(up, be, ku, c3, d3));
+                      block[s] = csub(block[s], cmul(P, cscale(term, sg)));
+#undef PR
+                    }
+                  }
+              }
+      }
+    for (int j = 0; j < nmom; j++) {
+      cx c = cmk(0, 0);
+      for (size_t s = 0; s < V3; s++) {
+        /* spatial site s = x + Lx (y + Ly z) of the time-slice */
+        const int x = (int)(s % (size_t)L[1]), y = (int)((s / (size_t)L[1]) % (size_t)L[2]),
+                  z = (int)(s / ((size_t)L[1] * L[2]));
+        const double a = 2 * M_PI * ((double)mom[3 * j] * (x - xsrc[1]) / L[1] +
+                                     (double)mom[3 * j + 1] * (y - xsrc[2]) / L[2] +
+                                     (double)mom[3 * j + 2] * (z - xsrc[3]) / L[3]);
+        c = cadd(c, cmul(block[s], cmk(cos(a), -sin(a))));
+      }
+      corr[2 * ((size_t)(t - t0) * nmom + j)] = 0.5 * c.re;
+      corr[2 * ((size_t)(t - t0) * nmom + j) + 1] = 0.5 * c.im;
+    }
+  }
+  free(block);
+}

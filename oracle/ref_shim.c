@@ -19,14 +19,78 @@ qcd_int_4 gcr(qcd_vector *sol, qcd_vector *src, qcd_gaugeField *u, qcd_real_8 ka
               qcd_real_8 muTM, qcd_uint_4 n, qcd_geometry *geo);
 void Exp(qcd_complex_16 M[][3]);
 
-/* invert.c's main() also references the file-I/O layer (qcd_io.c needs
- * MPI-IO and c-lime and is not built); these stand-ins keep the shared object
- * loadable. main() itself is never called. */
-char *qcd_getParams(char *fname, int *len) { (void)fname; (void)len; return NULL; }
-char *qcd_getParam(char token[], char *params, int len) { (void)token; (void)params; (void)len; return (char *)""; }
-int qcd_getGaugeField(char *fname, int type, qcd_gaugeField *u) { (void)fname; (void)type; (void)u; return 1; }
+/* The drivers' file-I/O layer (qcd_io.c needs MPI-IO and c-lime and is not
+ * built) is replaced by in-memory stand-ins: the parameter text, gauge field
+ * and propagators come from arrays the test harness registers with
+ * ref_io_set(). invert.c's main() is never called; twop.c's main() runs as
+ * ref_twop_main() on those arrays. */
+static const char *io_params;
+static const double *io_gauge, *io_uprop, *io_dprop;
+
+void ref_io_set(const char *params, const double *gauge, const double *uprop, const double *dprop)
+{
+  io_params = params;
+  io_gauge = gauge;
+  io_uprop = uprop;
+  io_dprop = dprop;
+}
+
+char *qcd_getParams(char *fname, int *len)
+{
+  (void)fname;
+  if (!io_params) return NULL;
+  *len = (int)strlen(io_params) + 1;
+  char *p = malloc((size_t)*len);
+  memcpy(p, io_params, (size_t)*len);
+  return p;
+}
+
+/* the text between `token` (an opening tag) and the next '<' */
+char *qcd_getParam(char token[], char *params, int len)
+{
+  static char val[16][256];
+  static int slot;
+  char *out = val[slot++ % 16];
+  out[0] = 0;
+  const char *p = strstr(params, token);
+  if (!p || p >= params + len) return out;
+  p += strlen(token);
+  int n = 0;
+  while (p[n] && p[n] != '<' && n < 255) n++;
+  memcpy(out, p, (size_t)n);
+  out[n] = 0;
+  return out;
+}
+
+int qcd_getGaugeField(char *fname, int type, qcd_gaugeField *u)
+{
+  (void)fname;
+  (void)type;
+  if (!io_gauge) return 1;
+  memcpy(u->D, io_gauge, sizeof(qcd_complex_16) * 36 * u->geo->lV);
+  return 0;
+}
+
+/* propagator file names "up..." / "down..." select the registered arrays */
+int qcd_getPropagator(char *fname, int type, qcd_propagator *p)
+{
+  (void)type;
+  const double *src = strstr(fname, "up") ? io_uprop : strstr(fname, "down") ? io_dprop : NULL;
+  if (!src) return 1;
+  memcpy(p->D, src, sizeof(qcd_complex_16) * 144 * p->geo->lV);
+  return 0;
+}
+
 int qcd_getVector(char *fname, int type, qcd_uint_2 nu, qcd_uint_2 c2, qcd_vector *vec)
 { (void)fname; (void)type; (void)nu; (void)c2; (void)vec; return 1; }
+
+/* twop.c (proton two-point function), main renamed */
+int ref_twop_main(int argc, char *argv[]);
+int ref_twop(const char *param_file)
+{
+  char *argv[3] = {(char *)"twop", (char *)param_file, NULL};
+  return ref_twop_main(2, argv);
+}
 
 static int geo_make(qcd_geometry *geo, const int L[4], const double theta[4])
 {

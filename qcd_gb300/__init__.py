@@ -171,6 +171,7 @@ def lib() -> C.CDLL:
     L.qcdgpu_mfield_set.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
     L.qcdgpu_mfield_get.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
     L.qcdgpu_dslash_mrhs.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_int]
+    L.qcdgpu_twop_proton.argtypes = [C.c_void_p, C.c_void_p, _ip, C.c_int, C.c_int, _ip, C.c_int, _dp]
     L.qcd_apeSmear3d.argtypes = [up, up, C.c_double]
     L.qcd_gaussIteration3d.argtypes = [vp, up, C.c_double, C.c_uint32]
     L.qcd_calculatePlaquette.argtypes = [up]
@@ -455,6 +456,20 @@ def smeared_source(f: "Field", g: "Gauge", x, spin: int, colour: int, ape_alpha:
     _check(lib().qcdgpu_smeared_source(f.h, g.h, np.ascontiguousarray(x, dtype=np.int32), spin, colour, ape_alpha,
                                        ape_n, gauss_alpha, gauss_n), "qcdgpu_smeared_source")
     return f
+
+
+def twop_proton(up, dn, xsrc, t0: int, t1: int, moms) -> np.ndarray:
+    """proton two-point function of twop.c on 12 + 12 FP64 propagator columns
+    (Field, column nu * 3 + c2); returns corr[t - t0, j] (complex)."""
+    moms = np.ascontiguousarray(moms, dtype=np.int32).reshape(-1, 3)
+    cu = (C.c_void_p * 12)(*[f.h.value for f in up])
+    cd = (C.c_void_p * 12)(*[f.h.value for f in dn])
+    out = np.zeros((t1 - t0 + 1) * len(moms) * 2)
+    _check(lib().qcdgpu_twop_proton(C.cast(cu, C.c_void_p), C.cast(cd, C.c_void_p),
+                                    np.ascontiguousarray(xsrc, dtype=np.int32), t0, t1, moms, len(moms), out),
+           "qcdgpu_twop_proton")
+    out = out.reshape(t1 - t0 + 1, len(moms), 2)
+    return out[..., 0] + 1j * out[..., 1]
 
 
 def set_mrhs_variant(v: int) -> None:

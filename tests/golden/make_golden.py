@@ -57,5 +57,39 @@ def main():
         print("wrote", name)
 
 
+# proton two-point function (twop.c run on in-memory inputs): propagator
+# column k of up / down = oracle Gaussian spinor of seed TWOP_SEED + k / + 100 + k
+TWOP = {
+    "twop_L8442": dict(L=(8, 4, 4, 2), xsrc=(3, 1, 2, 0), t0=0, t1=7, nsmear=0, nape=0, seed=21),
+    "twop_L8442_smeared": dict(L=(8, 4, 4, 2), xsrc=(5, 0, 3, 1), t0=1, t1=6, nsmear=2, nape=1, seed=22),
+}
+TWOP_MOMS = [(0, 0, 0), (1, 0, 0), (0, -1, 1), (2, 1, 0)]
+
+
+def twop_inputs(orc, L, seed):
+    u = orc.gauge_synthetic(L, seed, EPS_PLAQ_060)
+    V = int(np.prod(L))
+    cols = lambda off: [orc.gaussian_spinor(L, 1000 * seed + off + k) for k in range(12)]  # noqa: E731
+    # D[v][mu][nu][c1][c2]: column k = nu * 3 + c2 holds [v][mu][c1]
+    prop = lambda cs: np.stack(cs, axis=0).reshape(4, 3, V, 4, 3, 2).transpose(2, 3, 0, 4, 1, 5)  # noqa: E731
+    return u, cols(0), cols(100), prop
+
+
+def main_twop():
+    orc, ref = Oracle(), Reference()
+    out_dir = os.path.dirname(os.path.abspath(__file__))
+    for name, c in TWOP.items():
+        L = c["L"]
+        u, cu, cd, prop = twop_inputs(orc, L, c["seed"])
+        corr = ref.twop(u, np.ascontiguousarray(prop(cu)), np.ascontiguousarray(prop(cd)), L, c["xsrc"], c["t0"],
+                        c["t1"], TWOP_MOMS, nsmear=c["nsmear"], alpha=4.0, nape=c["nape"], alpha_ape=0.5)
+        np.savez_compressed(os.path.join(out_dir, name + ".npz"), corr=corr, moms=np.array(TWOP_MOMS),
+                            **{k: np.array(v) for k, v in c.items()})
+        print("wrote", name)
+
+
 if __name__ == "__main__":
+    if len(sys.argv) > 1 and sys.argv[1] == "twop":
+        main_twop()
+        sys.exit(0)
     main()

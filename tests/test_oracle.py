@@ -142,3 +142,43 @@ def test_rng_counter_stream(orc):
     assert set(np.unique(vals)).issubset({1, -1, 1j, -1j})
     counts = [np.sum(vals == c) for c in (1, -1, 1j, -1j)]
     assert min(counts) > 0.15 * vals.size
+
+
+def test_twop_tables_match_reference(orc, ref):
+    for mine, theirs in zip(orc.twop_tables(), ref.twop_tables()):
+        assert np.array_equal(mine, theirs)
+
+
+def test_twop_oracle_matches_reference_run(orc, ref):
+    """twop.c itself (main() on in-memory inputs) against the restatement; the
+    reference prints 7 significant digits (%+e), which bounds the agreement."""
+    L, xsrc = (8, 4, 2, 4), (6, 3, 1, 2)
+    V = int(np.prod(L))
+    rng = np.random.default_rng(5)
+    up, dn = rng.normal(size=(V, 4, 4, 3, 3, 2)), rng.normal(size=(V, 4, 4, 3, 3, 2))
+    u = orc.gauge_synthetic(L, 6, 0.43374)
+    moms = [(0, 0, 0), (1, 1, 0), (-1, 0, 2)]
+    c_ref = ref.twop(u, up, dn, L, xsrc, 0, 7, moms)
+    c_orc = orc.twop_proton(up, dn, L, xsrc, 0, 7, moms)
+    assert np.max(np.abs(c_orc - c_ref)) <= 2e-6 * np.max(np.abs(c_ref))
+
+
+@pytest.mark.parametrize("case", ["twop_L8442", "twop_L8442_smeared"])
+def test_twop_oracle_matches_golden(orc, golden, case):
+    from tests.golden.make_golden import TWOP_MOMS, twop_inputs
+
+    g = golden[case]
+    L = tuple(int(x) for x in g["L"])
+    u, cu, cd, prop = twop_inputs(orc, L, int(g["seed"]))
+    if int(g["nsmear"]):
+        ua = u
+        for _ in range(int(g["nape"])):
+            ua = orc.ape3d(ua, L, 0.5)
+        for cols in (cu, cd):
+            for k in range(12):
+                for _ in range(int(g["nsmear"])):
+                    for t in range(L[0]):
+                        cols[k] = orc.gauss3d(cols[k], ua, L, 4.0, t)
+    corr = orc.twop_proton(prop(cu), prop(cd), L, tuple(int(x) for x in g["xsrc"]), int(g["t0"]), int(g["t1"]),
+                           TWOP_MOMS)
+    assert np.max(np.abs(corr - g["corr"])) <= 2e-6 * np.max(np.abs(g["corr"]))
