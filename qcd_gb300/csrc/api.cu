@@ -13,6 +13,7 @@
 #include <mutex>
 #include <unordered_map>
 #include <unordered_set>
+#include <vector>
 
 #include "internal.h"
 
@@ -164,6 +165,80 @@ static bool check_op_args(qcd_vector *Dv, qcd_vector *v, qcd_gaugeField *u)
   return true;
 }
 
+// Pipelined apply for page-locked host vectors: the lattice is cut into S
+// slabs of whole z-planes; slab k is copied in over the host link (by a
+// kernel reading host memory, on s_in), applied as soon as slabs k-1..k+1
+// are in (on the library stream), and written back (on s_out) while later
+// slabs are still arriving. Slabs 0 and S-1 need each other (periodic z),
+// so the order of application is 1 .. S-2, S-1, 0.
+static cudaStream_t g_s_in, g_s_out;
+static std::vector<cudaEvent_t> g_ev_in, g_ev_op;
+static cudaEvent_t g_ev_start, g_ev_done;
+
+static int pipeline_slabs(const qcdgpu_field f)
+{
+  for (int S : {8, 6, 4, 3})
+    if (f->L[3] % S == 0) return S;
+  return 0;
+}
+
+static bool pipeline_ready(int S)
+{
+  if (!g_s_in) {
+    if (!QG_CUDA(cudaStreamCreateWithFlags(&g_s_in, cudaStreamNonBlocking)) ||
+        !QG_CUDA(cudaStreamCreateWithFlags(&g_s_out, cudaStreamNonBlocking)) ||
+        !QG_CUDA(cudaEventCreateWithFlags(&g_ev_start, cudaEventDisableTiming)) ||
+        !QG_CUDA(cudaEventCreateWithFlags(&g_ev_done, cudaEventDisableTiming)))
+      return false;
+  }
+  while ((int)g_ev_in.size() < S) {
+    cudaEvent_t a, b;
+    if (!QG_CUDA(cudaEventCreateWithFlags(&a, cudaEventDisableTiming)) ||
+        !QG_CUDA(cudaEventCreateWithFlags(&b, cudaEventDisableTiming)))
+      return false;
+    g_ev_in.push_back(a);
+    g_ev_op.push_back(b);
+  }
+  return true;
+}
+
+static bool apply_pipelined(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, const double *vin, double *vout,
+                            double mp4, double tm, int op, int S)
+{
+  if (!pipeline_ready(S)) return false;
+  const int64_t V = in->V, slab = V / S;
+  cudaStream_t st = stream();
+  if (!QG_CUDA(cudaEventRecord(g_ev_start, st)) || !QG_CUDA(cudaStreamWaitEvent(g_s_in, g_ev_start, 0)) ||
+      !QG_CUDA(cudaStreamWaitEvent(g_s_out, g_ev_start, 0)))
+    return false;
+  {
+    StreamScope scope(g_s_in);
+    for (int k = 0; k < S; k++)
+      if (!spinor_from_host_sites(in, vin, k * slab, (k + 1) * slab) || !QG_CUDA(cudaEventRecord(g_ev_in[k], g_s_in)))
+        return false;
+  }
+  std::vector<int> order;
+  for (int k = 1; k < S - 1; k++) order.push_back(k);
+  order.push_back(S - 1);
+  order.push_back(0);
+  for (int k : order) {
+    const int need = (k == 0 || k == S - 1) ? S - 1 : k + 1;
+    if (!QG_CUDA(cudaStreamWaitEvent(st, g_ev_in[need], 0)) ||
+        !dslash_sites(out, in, g, mp4, tm, op, -1, (int)(k * slab), (int)((k + 1) * slab)) ||
+        !QG_CUDA(cudaEventRecord(g_ev_op[k], st)))
+      return false;
+  }
+  {
+    StreamScope scope(g_s_out);
+    for (int k : order)
+      if (!QG_CUDA(cudaStreamWaitEvent(g_s_out, g_ev_op[k], 0)) ||
+          !spinor_to_host_sites(out, vout, k * slab, (k + 1) * slab))
+        return false;
+  }
+  return QG_CUDA(cudaEventRecord(g_ev_done, g_s_out)) && QG_CUDA(cudaStreamWaitEvent(st, g_ev_done, 0)) &&
+         QG_CUDA(cudaStreamSynchronize(st));
+}
+
 static int apply_op(qcd_vector *Dv, qcd_vector *v, qcd_gaugeField *u, double m, double tm, int op)
 {
   std::lock_guard<std::mutex> lk(g_mu);
@@ -175,6 +250,12 @@ static int apply_op(qcd_vector *Dv, qcd_vector *v, qcd_gaugeField *u, double m, 
   }
   qcdgpu_gauge g = gauge_in(u);
   if (!g) return 1;
+  VecMirror *mi = vec_mirror(v), *mo = vec_mirror(Dv);
+  if (!mi || !mo) return 1;
+  const int S = pipeline_slabs(mi->f);
+  if (!mi->resident && !mo->resident && S && g_pinned.count((const void *)v->D) &&
+      g_pinned.count((const void *)Dv->D) && (op == QCDGPU_OP_D || op == QCDGPU_OP_Q))
+    return apply_pipelined(mo->f, mi->f, g, (const double *)v->D, (double *)Dv->D, 4.0 + m, tm, op, S) ? 0 : 1;
   qcdgpu_field in = vec_in(v);
   qcdgpu_field out = vec_out(Dv);
   if (!in || !out) return 1;

@@ -24,7 +24,7 @@ bool dslash_df64(const DArgs &a, bool dag, bool eo = false);
 template <bool DAG>
 static bool launch_native(const DArgs &a, int prec, int recon)
 {
-  unsigned grid = (unsigned)((a.V + 127) / 128);
+  unsigned grid = (unsigned)((a.V - a.x0 + 127) / 128);
   cudaStream_t s = stream();
   // FP64 arithmetic is the bottleneck of the native FP64 kernel (GB300 runs
   // DFMA at ~1/60 of the FP32 rate): read all 18 link reals, no rebuild
@@ -36,10 +36,11 @@ static bool launch_native(const DArgs &a, int prec, int recon)
 }
 
 static bool dslash_once(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4, double tm,
-                        bool dag, bool q, int arith, double *partials = nullptr)
+                        bool dag, bool q, int arith, double *partials = nullptr, int x0 = 0, int x1 = -1)
 {
   DArgs a;
   a.partials = partials;
+  a.x0 = x0;
   a.out = out->data;
   a.out_norm = out->norm;
   a.in = in->data;
@@ -50,7 +51,7 @@ static bool dslash_once(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, doubl
   a.geo.st[1] = in->L[0];
   a.geo.st[2] = in->L[0] * in->L[1];
   a.geo.st[3] = in->L[0] * in->L[1] * in->L[2];
-  a.V = (int)in->V;
+  a.V = x1 < 0 ? (int)in->V : x1;
   a.stride = in->stride;
   a.gstride = g->stride;
   a.twist_mask = 0;
@@ -136,6 +137,7 @@ bool dslash_eo(qcdgpu_field out, qcdgpu_field in, qcdgpu_field z, qcdgpu_gauge g
   }
   DArgs a;
   a.partials = partials;
+  a.x0 = 0;
   a.out = out->data;
   a.out_norm = out->norm;
   a.in = in->data;
@@ -202,6 +204,20 @@ bool dslash_eo(qcdgpu_field out, qcdgpu_field in, qcdgpu_field z, qcdgpu_gauge g
   }
 #undef QG_EO
   return QG_LAUNCHED("wilson_eo");
+}
+
+// out = op(in) (op D or Q) on sites x0 .. x1-1 only: the pieces of a
+// pipelined apply. The neighbours' values must be in place.
+bool dslash_sites(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4, double tm, int op, int arith,
+                  int x0, int x1)
+{
+  if (!out || !in || !g || out == in || in->prec != out->prec || in->prec != g->prec || in->V != g->V ||
+      !same_shape(out, in) || (op != QCDGPU_OP_D && op != QCDGPU_OP_Q) || x0 < 0 || x1 > in->V || x0 >= x1) {
+    set_error("dslash over a site range: fields of one shape, op D or Q, 0 <= x0 < x1 <= V");
+    return false;
+  }
+  if (arith < 0) arith = g_f64_arith;
+  return dslash_once(out, in, g, mp4, tm, false, op == QCDGPU_OP_Q, arith, nullptr, x0, x1);
 }
 
 // out = D in (dag: D^+ in) on fields checked by the caller; when partials is

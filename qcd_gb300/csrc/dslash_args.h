@@ -12,6 +12,7 @@ struct DArgs {
   const float *in_norm;
   const void *gauge;
   qgd::Geom geo;
+  int x0;  // sites x0 .. V-1 (a range of a full-lattice launch; 0 otherwise)
   int V;
   int64_t stride;   // spinor block stride
   int64_t gstride;  // gauge block stride

@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(384, 3) k_wilson_ff(const DArgs a)
 {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int grp = w / 3, col = w - 3 * grp;
-  const int e = blockIdx.x * kFFSites + grp * 32 + lane;  // output index
+  const int e = a.x0 + blockIdx.x * kFFSites + grp * 32 + lane;  // output index
   const bool act = e < a.V;
   __shared__ CF hs[4][2][3][32];
   const double2 *sp = (const double2 *)a.in;
@@ -394,7 +394,7 @@ bool gauge_to_ff(qcdgpu_gauge d, qcdgpu_gauge s)
 
 bool dslash_df64(const DArgs &a, bool dag, bool eo)
 {
-  unsigned grid = (unsigned)((a.V + kFFSites - 1) / kFFSites);
+  unsigned grid = (unsigned)((a.V - a.x0 + kFFSites - 1) / kFFSites);
   if (eo) {
     if (dag) k_wilson_ff<true, true><<<grid, 384, 0, stream()>>>(a);
     else k_wilson_ff<false, true><<<grid, 384, 0, stream()>>>(a);

@@ -39,9 +39,9 @@ static inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + b
 // ------------------------------------------------------------ spinors
 template <int P>
 __global__ void k_spinor_aos_to_soa(void *dst, float *norm, int64_t stride, const double2 *src,
-                                    int64_t V)
+                                    int64_t V, int64_t x0 = 0)
 {
-  int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t x = x0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= V) return;
   C<double> s[12];
   const double2 *p = src + x * 12;
@@ -55,9 +55,9 @@ __global__ void k_spinor_aos_to_soa(void *dst, float *norm, int64_t stride, cons
 
 template <int P>
 __global__ void k_spinor_soa_to_aos(double2 *dst, const void *src, const float *norm,
-                                    int64_t stride, int64_t V)
+                                    int64_t stride, int64_t V, int64_t x0 = 0)
 {
-  int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t x = x0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= V) return;
   C<double> s[12];
   Spinor<P, double>::load(src, norm, stride, x, s);
@@ -305,6 +305,26 @@ bool spinor_to_aos_dev(qcdgpu_field f, void *dev_aos)
   default: k_spinor_soa_to_aos<QCDGPU_F16><<<g, 128, 0, stream()>>>(a, f->data, f->norm, f->stride, f->V);
   }
   return QG_LAUNCHED("spinor_soa_to_aos");
+}
+
+// sites x0 .. x1-1 of an FP64 field from / to a page-locked host array in the
+// host layout, read and written by the kernel over the host link (no staging)
+bool spinor_from_host_sites(qcdgpu_field f, const double *host, int64_t x0, int64_t x1)
+{
+  double2 *src = nullptr;
+  if (f->prec != QCDGPU_F64 || !QG_CUDA(cudaHostGetDevicePointer((void **)&src, (void *)host, 0))) return false;
+  k_spinor_aos_to_soa<QCDGPU_F64><<<grid_for(x1 - x0, 128), 128, 0, stream()>>>(f->data, f->norm, f->stride, src, x1,
+                                                                                 x0);
+  return QG_LAUNCHED("spinor_host_to_soa");
+}
+
+bool spinor_to_host_sites(qcdgpu_field f, double *host, int64_t x0, int64_t x1)
+{
+  double2 *dst = nullptr;
+  if (f->prec != QCDGPU_F64 || !QG_CUDA(cudaHostGetDevicePointer((void **)&dst, host, 0))) return false;
+  k_spinor_soa_to_aos<QCDGPU_F64><<<grid_for(x1 - x0, 128), 128, 0, stream()>>>(dst, f->data, f->norm, f->stride, x1,
+                                                                                 x0);
+  return QG_LAUNCHED("spinor_soa_to_host");
 }
 
 // gauge field -> the host layout [V][4][3][3] complex double in device memory

@@ -109,7 +109,7 @@ __device__ __forceinline__ void hop_pair(const DArgs &a, int x, const int c[4], 
 template <bool DAG, int SP, int GP, int RECON, typename R>
 __global__ void __launch_bounds__(128) k_wilson(const DArgs a)
 {
-  int x = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  int x = a.x0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
   double n2 = 0.0;
   if (x < a.V) {
     int c[4];
