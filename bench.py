@@ -454,7 +454,8 @@ def run_ours(args, rank, world, local_rank):
         "kernels_ms": {"f64": ms_native, "df64": ms_df64},
         "e2e": {"value": V * bps / (ms_e2e * 1e-3) / 1e9 * world, "unit": "GB/s", "ms_per_step": ms_e2e,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "path": "qcd_applyWilsonTMOp on page-locked host qcd_vector buffers, resident gauge"},
+                "path": "qcd_applyWilsonTMOp on page-locked host qcd_vector buffers, resident gauge; slab-wise "
+                        "copies in and out overlapped with the operator"},
         "gpu_launches": launches,
         "clocks": clocks,
         "solve": solve,

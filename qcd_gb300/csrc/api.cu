@@ -166,18 +166,21 @@ static bool check_op_args(qcd_vector *Dv, qcd_vector *v, qcd_gaugeField *u)
 }
 
 // Pipelined apply for page-locked host vectors: the lattice is cut into S
-// slabs of whole z-planes; slab k is copied in over the host link (by a
-// kernel reading host memory, on s_in), applied as soon as slabs k-1..k+1
-// are in (on the library stream), and written back (on s_out) while later
-// slabs are still arriving. Slabs 0 and S-1 need each other (periodic z),
-// so the order of application is 1 .. S-2, S-1, 0.
+// slabs of whole z-planes; slab k is copied in by the copy engine and
+// reordered on s_in, applied as soon as slabs k-1..k+1 are in (on the
+// library stream), and reordered and copied back on s_out while later slabs
+// are still arriving, so the two copy directions and the operator overlap.
+// Slabs 0 and S-1 need each other (periodic z), so the order of application
+// is 1 .. S-2, S-1, 0.
 static cudaStream_t g_s_in, g_s_out;
 static std::vector<cudaEvent_t> g_ev_in, g_ev_op;
 static cudaEvent_t g_ev_start, g_ev_done;
+static void *g_stage_in, *g_stage_out;  // device copies of the host layout
+static size_t g_stage_bytes;
 
 static int pipeline_slabs(const qcdgpu_field f)
 {
-  for (int S : {8, 6, 4, 3})
+  for (int S : {12, 8, 6, 4, 3})
     if (f->L[3] % S == 0) return S;
   return 0;
 }
@@ -207,15 +210,28 @@ static bool apply_pipelined(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, c
 {
   if (!pipeline_ready(S)) return false;
   const int64_t V = in->V, slab = V / S;
+  const size_t bytes = (size_t)V * 24 * sizeof(double), sbytes = bytes / S;
+  if (bytes > g_stage_bytes) {
+    cudaFree(g_stage_in);
+    cudaFree(g_stage_out);
+    g_stage_in = g_stage_out = nullptr;
+    g_stage_bytes = 0;
+    if (!QG_CUDA(cudaMalloc(&g_stage_in, bytes)) || !QG_CUDA(cudaMalloc(&g_stage_out, bytes))) return false;
+    g_stage_bytes = bytes;
+  }
   cudaStream_t st = stream();
   if (!QG_CUDA(cudaEventRecord(g_ev_start, st)) || !QG_CUDA(cudaStreamWaitEvent(g_s_in, g_ev_start, 0)) ||
       !QG_CUDA(cudaStreamWaitEvent(g_s_out, g_ev_start, 0)))
     return false;
   {
     StreamScope scope(g_s_in);
-    for (int k = 0; k < S; k++)
-      if (!spinor_from_host_sites(in, vin, k * slab, (k + 1) * slab) || !QG_CUDA(cudaEventRecord(g_ev_in[k], g_s_in)))
+    for (int k = 0; k < S; k++) {
+      char *dst = (char *)g_stage_in + k * sbytes;
+      if (!QG_CUDA(cudaMemcpyAsync(dst, (const char *)vin + k * sbytes, sbytes, cudaMemcpyHostToDevice, g_s_in)) ||
+          !spinor_from_aos_sites(in, g_stage_in, k * slab, (k + 1) * slab) ||
+          !QG_CUDA(cudaEventRecord(g_ev_in[k], g_s_in)))
         return false;
+    }
   }
   std::vector<int> order;
   for (int k = 1; k < S - 1; k++) order.push_back(k);
@@ -232,7 +248,9 @@ static bool apply_pipelined(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, c
     StreamScope scope(g_s_out);
     for (int k : order)
       if (!QG_CUDA(cudaStreamWaitEvent(g_s_out, g_ev_op[k], 0)) ||
-          !spinor_to_host_sites(out, vout, k * slab, (k + 1) * slab))
+          !spinor_to_aos_sites(out, g_stage_out, k * slab, (k + 1) * slab) ||
+          !QG_CUDA(cudaMemcpyAsync((char *)vout + k * sbytes, (const char *)g_stage_out + k * sbytes, sbytes,
+                                   cudaMemcpyDeviceToHost, g_s_out)))
         return false;
   }
   return QG_CUDA(cudaEventRecord(g_ev_done, g_s_out)) && QG_CUDA(cudaStreamWaitEvent(st, g_ev_done, 0)) &&

@@ -121,10 +121,10 @@ bool pack_gauge(qcdgpu_gauge g, const void *dev_aos);
 bool spinor_from_aos_dev(qcdgpu_field f, const void *dev_aos);
 bool spinor_to_aos_dev(qcdgpu_field f, void *dev_aos);
 bool gauge_to_aos_dev(qcdgpu_gauge g, void *dev_aos);
-// sites x0 .. x1-1 of an FP64 field from / to a page-locked host array in the
-// host layout, accessed by the kernel over the host link
-bool spinor_from_host_sites(qcdgpu_field f, const double *host, int64_t x0, int64_t x1);
-bool spinor_to_host_sites(qcdgpu_field f, double *host, int64_t x0, int64_t x1);
+// sites x0 .. x1-1 of an FP64 field from / to the host layout held in device
+// memory (the whole field's array; only the range is touched)
+bool spinor_from_aos_sites(qcdgpu_field f, const void *dev_aos, int64_t x0, int64_t x1);
+bool spinor_to_aos_sites(qcdgpu_field f, void *dev_aos, int64_t x0, int64_t x1);
 // dslash.cu: op D or Q on sites x0 .. x1-1 only
 bool dslash_sites(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4, double tm, int op, int arith,
                   int x0, int x1);

@@ -307,24 +307,22 @@ bool spinor_to_aos_dev(qcdgpu_field f, void *dev_aos)
   return QG_LAUNCHED("spinor_soa_to_aos");
 }
 
-// sites x0 .. x1-1 of an FP64 field from / to a page-locked host array in the
-// host layout, read and written by the kernel over the host link (no staging)
-bool spinor_from_host_sites(qcdgpu_field f, const double *host, int64_t x0, int64_t x1)
+// sites x0 .. x1-1 of an FP64 field from / to the host layout held in device
+// memory (the whole field's array; only the range is touched)
+bool spinor_from_aos_sites(qcdgpu_field f, const void *dev_aos, int64_t x0, int64_t x1)
 {
-  double2 *src = nullptr;
-  if (f->prec != QCDGPU_F64 || !QG_CUDA(cudaHostGetDevicePointer((void **)&src, (void *)host, 0))) return false;
-  k_spinor_aos_to_soa<QCDGPU_F64><<<grid_for(x1 - x0, 128), 128, 0, stream()>>>(f->data, f->norm, f->stride, src, x1,
-                                                                                 x0);
-  return QG_LAUNCHED("spinor_host_to_soa");
+  if (f->prec != QCDGPU_F64) return false;
+  k_spinor_aos_to_soa<QCDGPU_F64><<<grid_for(x1 - x0, 128), 128, 0, stream()>>>(f->data, f->norm, f->stride,
+                                                                                 (const double2 *)dev_aos, x1, x0);
+  return QG_LAUNCHED("spinor_aos_to_soa");
 }
 
-bool spinor_to_host_sites(qcdgpu_field f, double *host, int64_t x0, int64_t x1)
+bool spinor_to_aos_sites(qcdgpu_field f, void *dev_aos, int64_t x0, int64_t x1)
 {
-  double2 *dst = nullptr;
-  if (f->prec != QCDGPU_F64 || !QG_CUDA(cudaHostGetDevicePointer((void **)&dst, host, 0))) return false;
-  k_spinor_soa_to_aos<QCDGPU_F64><<<grid_for(x1 - x0, 128), 128, 0, stream()>>>(dst, f->data, f->norm, f->stride, x1,
-                                                                                 x0);
-  return QG_LAUNCHED("spinor_soa_to_host");
+  if (f->prec != QCDGPU_F64) return false;
+  k_spinor_soa_to_aos<QCDGPU_F64><<<grid_for(x1 - x0, 128), 128, 0, stream()>>>((double2 *)dev_aos, f->data, f->norm,
+                                                                                 f->stride, x1, x0);
+  return QG_LAUNCHED("spinor_soa_to_aos");
 }
 
 // gauge field -> the host layout [V][4][3][3] complex double in device memory
