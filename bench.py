@@ -364,6 +364,51 @@ def precision_bench(q, L, kappa, n_batch, cap):
     return out
 
 
+def batching_bench(q, L, kappa, nrhs):
+    """the batching configuration: nrhs point-source columns at L solved to
+    1e-10 by one even/odd batch of nrhs slots, beside one even/odd FP16 solve
+    and one plain FP64 solve of the first column"""
+    g = q.Gauge(L, THETA).synthetic(4, EPS_PLAQ_060)
+    out = {"lattice_txyz": list(L), "kappa": kappa, "rhs": nrhs, "tol": 1e-10}
+    b, x = q.Field(L), q.Field(L)
+    for name, solver, prec in (("fp64_cgnr", q.SOLVER_CGNR, q.F64), ("eo_cgnr_f16", q.SOLVER_CGNR_EO, q.F16)):
+        b.point((0, 0, 0, 0), 0, 0)
+        q.sync()
+        t0 = time.perf_counter()
+        p = q.solve(x, b, g, kappa, 0.0, solver=solver, inner_prec=prec, tol=1e-10, maxiter=40000)
+        q.sync()
+        dt = time.perf_counter() - t0
+        out[name] = {"rhs_solves_per_s": 1.0 / dt if p.status == 0 else None, "s_per_solve": dt, "iters": p.iters,
+                     "true_residual": p.true_residual, "status": p.status}
+    b.close()
+    x.close()
+    srcs = [q.Field(L).point(((c // 12) * L[0] // 2, 0, 0, 0), c % 12 // 3, c % 3) for c in range(nrhs)]
+    xs = [q.Field(L) for _ in range(nrhs)]
+    batch = q.Batch(g, nrhs, eo=True)
+    q.sync()
+    t0 = time.perf_counter()
+    for c in range(nrhs):
+        batch.add(xs[c], srcs[c], kappa, 0.0, q.OP_D, tol=1e-10, maxiter=40000, tag=c)
+    done = []
+    while batch.active:
+        batch.step(16)
+        done += batch.poll()
+    done += batch.poll()
+    q.sync()
+    dt = time.perf_counter() - t0
+    ok = len(done) == nrhs and all(d[1] == 0 for d in done)
+    out["batched_mrhs_eo"] = {"rhs_solves_per_s": nrhs / dt if ok else None, "wall_s": dt,
+                              "iters_max": max(d[2] for d in done), "max_true_residual": max(d[3] for d in done),
+                              "status": sorted({d[1] for d in done}), "bytes": batch.nbytes()}
+    base = out["fp64_cgnr"]["rhs_solves_per_s"]
+    if base and out["batched_mrhs_eo"]["rhs_solves_per_s"]:
+        out["speedup_batched_mrhs_eo_vs_fp64"] = out["batched_mrhs_eo"]["rhs_solves_per_s"] / base
+    batch.close()
+    for f in srcs + xs + [g]:
+        f.close()
+    return out
+
+
 def serving_bench(q, seconds, rate, slots, budget_gb):
     """Poisson stream over four resident gauge fields (one per volume)"""
     from qcd_gb300 import serving
@@ -425,9 +470,13 @@ def run_ours(args, rank, world, local_rank):
         solve = solve_bench(q, None, g, L_BENCH, args.solve_rhs)
     for f in (g, fin, fout):
         f.close()
-    mrhs = precision = serving = None
+    mrhs = precision = serving = batching = None
     if rank == 0 and not args.no_mrhs:
         mrhs = mrhs_bench(q, torch, stream, L_MRHS, (4, 8, 16, 32, 48, 64), 10)
+    if rank == 0 and not args.no_mrhs and not args.no_solve:
+        q.release_work()
+        batching = batching_bench(q, L_MRHS, KAPPA, args.big_batch_rhs)
+        q.release_work()
     if rank == 0 and not args.no_solve:
         precision = precision_bench(q, L_PREC, KAPPA_PREC, args.batch_rhs, args.batch_slots)
     if rank == 0 and not args.no_serve:
@@ -461,6 +510,7 @@ def run_ours(args, rank, world, local_rank):
         "solve": solve,
         "precision_32x64": precision,
         "mrhs_operator": mrhs,
+        "batching_48x96": batching,
         "serving": serving,
     }
     if not args.no_cpu:
@@ -474,6 +524,11 @@ def run_only(args):
 
     import qcd_gb300 as q
 
+    if args.only == "serve":
+        # arrival-rate sweep of the serving stream (one line per rate)
+        rates = [float(r) for r in args.serve_sweep.split(",")]
+        return {"only": "serve", "sweep": [serving_bench(q, args.serve_seconds, r, args.serve_slots,
+                                                         args.serve_budget_gb) for r in rates]}
     if args.only == "solve":
         # one point-source column solved to 1e-10 (even/odd CGNR, FP16 inner)
         g = q.Gauge(L_BENCH, THETA).synthetic(1000, EPS_PLAQ_060)
@@ -556,6 +611,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--batch-rhs", type=int, default=48, help="point-source columns of the batched 32^3x64 solve")
     ap.add_argument("--batch-slots", type=int, default=48)
+    ap.add_argument("--big-batch-rhs", type=int, default=16, help="point-source columns of the 48^3x96 batch")
     ap.add_argument("--serve-seconds", type=float, default=30.0)
     ap.add_argument("--serve-rate", type=float, default=2.0, help="request arrivals per second")
     ap.add_argument("--serve-slots", type=int, default=32)
@@ -566,7 +622,8 @@ def main():
     ap.add_argument("--eo", action="store_true", help="--only batch: even/odd preconditioned batch")
     ap.add_argument("--mrhs-variant", type=int, default=-1,
                     help="--only mrhs: -1 tuned, 1 tensor cores, 64/128/256 SIMT block size")
-    ap.add_argument("--only", choices=["f64", "df64", "f32", "f16", "mrhs", "batch", "solve"],
+    ap.add_argument("--serve-sweep", default="0.5,1,2,4", help="--only serve: arrival rates (requests/s)")
+    ap.add_argument("--only", choices=["f64", "df64", "f32", "f16", "mrhs", "batch", "solve", "serve"],
                     help="profiling target: time only this operator variant (a few launches under ncu)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -347,6 +347,10 @@ int qcdgpu_solve(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double kappa, d
  * message), and calls that overlap on the GPU race on that array. The first
  * call on each device looks the array's address up; make it before any
  * stream capture. Returns 0, or 1 on error (qcdgpu_last_error). */
+/* Solvers keep their work fields in a pool between calls; this frees the
+ * pool's device memory (the next solve allocates again). Returns 0. */
+int qcdgpu_release_work(void);
+
 int qcdgpu_dot_noalloc(const double *a, const double *b, int64_t n, double *result, void *stream);
 
 /* Source construction on device fields (FP64): n APE steps out <- in (out

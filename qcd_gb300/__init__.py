@@ -402,6 +402,11 @@ def solve(x: Field, b: Field, g: Gauge, kappa: float, mu: float = 0.0, solver=SO
     return p
 
 
+def release_work() -> None:
+    """free the solvers' pooled work fields"""
+    lib().qcdgpu_release_work()
+
+
 def set_stream(stream_ptr: int | None):
     _check(lib().qcdgpu_set_stream(C.c_void_p(stream_ptr or 0)), "set_stream")
 

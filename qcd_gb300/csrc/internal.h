@@ -99,6 +99,7 @@ bool same_shape(qcdgpu_field a, qcdgpu_field b);
 // pooled work fields (runtime.cu): returned fields are zero-free garbage
 qcdgpu_field work_get(const int L[4], int prec);
 void work_put(qcdgpu_field f);
+void work_trim();  // frees the pooled fields
 
 // scratch for reductions: 2 * kMaxPartials doubles + result slots
 constexpr int kMaxPartials = 2048;

@@ -161,7 +161,12 @@ qcdgpu_field work_get(const int L[4], int prec)
       }
     }
   }
-  return field_new(L, prec);
+  qcdgpu_field f = field_new(L, prec);
+  if (!f) {  // out of device memory: give back the pooled fields and retry once
+    work_trim();
+    f = field_new(L, prec);
+  }
+  return f;
 }
 
 void work_put(qcdgpu_field f)
@@ -169,6 +174,14 @@ void work_put(qcdgpu_field f)
   if (!f) return;
   std::lock_guard<std::mutex> lk(g_pool_mu);
   g_pool.push_back(f);
+}
+
+void work_trim()
+{
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  if (!g_pool.empty()) cudaStreamSynchronize(g_stream);
+  for (qcdgpu_field f : g_pool) field_free(f);
+  g_pool.clear();
 }
 
 // ------------------------------------------------------- reduction scratch
@@ -225,6 +238,12 @@ int qcdgpu_set_stream(void *s)
 }
 
 int qcdgpu_sync(void) { return QG_CUDA(cudaStreamSynchronize(qg::g_stream)) ? 0 : 1; }
+
+int qcdgpu_release_work(void)
+{
+  qg::work_trim();
+  return 0;
+}
 
 uint64_t qcdgpu_kernel_launches(void) { return qg::g_launches.load(); }
 
