@@ -5,7 +5,7 @@
 // (measured: 0.60 T DFMA/s against 35 T FFMA/s), so the FP64 operator
 // computed natively is bound by the FP64 pipe, not by HBM. This kernel keeps
 // FP64 storage for the spinors (read and written as doubles) and computes on
-// the FP32 pipes with unevaluated float pairs (hi + lo, ~48 significant bits):
+// the FP32 pipes with unevaluated float pairs (hi + lo, ~47 significant bits):
 //   * products: Dekker's exact product of the high words via FMA plus the two
 //     cross terms (T. J. Dekker, Numer. Math. 18 (1971) 224);
 //   * sums: Knuth's TwoSum (TAOCP vol. 2) into lazy accumulators (s, e) whose
@@ -18,7 +18,7 @@
 // float pairs, made once per field, with the boundary phase e^{i th/L}
 // multiplied into the links of twisted directions (U' h for the forward hop,
 // U'^+ h = e^{-i th/L} U^+ h for the backward one, as qcd_wilson.c applies it).
-// The result differs from FP64 by a few 2^-47 relative, within the 1e-13
+// The result differs from FP64 by a few 2^-46 relative, within the 1e-13
 // per-site parity bar. Spinor values must lie in [2^-74, 2^127) in magnitude
 // for the fast conversion; other values take an exact slower path, and
 // doubles below 2^-1022 (denormals) count as zero.
@@ -41,7 +41,7 @@ struct CA {
   FA re, im;
 };
 
-// out of line so the common path carries no FP64 instructions
+// out of line, so the common path does not carry its FP64 conversions
 __device__ __noinline__ F2 split_slow(double d)
 {
   F2 r;
@@ -50,21 +50,20 @@ __device__ __noinline__ F2 split_slow(double d)
   return r;
 }
 
+// double -> float pair. In range (|d| in [2^-74, 2^127)) with integer bit
+// operations: hi takes the leading 24 significand bits and lo the next 23
+// (both truncated; the pair keeps 47 bits, relative error below 2^-46).
 __device__ __forceinline__ F2 split_d(double d)
 {
-  unsigned lo32 = (unsigned)__double2loint(d), hi32 = (unsigned)__double2hiint(d);
-  unsigned e = (hi32 >> 20) & 0x7ffu;
-  unsigned sign = hi32 & 0x80000000u;
+  const unsigned lo32 = (unsigned)__double2loint(d), hi32 = (unsigned)__double2hiint(d);
+  const unsigned e = (hi32 >> 20) & 0x7ffu;
+  const unsigned sign = hi32 & 0x80000000u;
   F2 r;
   if (e >= 949u && e <= 1150u) {
-    // hi: the leading 24 significand bits (truncated); lo: the next 29 bits
-    // rounded to 24 -- built from two exact 23-bit pieces and one FMA
     r.h = __uint_as_float(sign | ((e - 896u) << 23) | ((hi32 & 0xfffffu) << 3) | (lo32 >> 29));
-    unsigned rem = lo32 & 0x1fffffffu;  // value rem * 2^(e - 1075)
-    float f1 = __fsub_rn(__uint_as_float(0x4B000000u | (rem >> 6)), 8388608.0f);
-    float f2 = __fsub_rn(__uint_as_float(0x4B000000u | (rem & 63u)), 8388608.0f);
-    float lo = __fmul_rn(__fmaf_rn(f1, 64.0f, f2), __uint_as_float((e - 948u) << 23));
-    r.l = __uint_as_float(__float_as_uint(lo) ^ sign);
+    // the 23 bits below hi as an exact integer-valued float, scaled by 2^(e - 1069)
+    const float f1 = __fsub_rn(__uint_as_float(0x4B000000u | ((lo32 >> 6) & 0x7fffffu)), 8388608.0f);
+    r.l = __fmul_rn(f1, __uint_as_float(sign | ((e - 942u) << 23)));
   } else if (e == 0u) {
     r.h = __uint_as_float(sign);
     r.l = 0.0f;
@@ -179,7 +178,8 @@ __device__ __forceinline__ CF coef(CF z, bool ifl, bool ng)
 // the four accumulators (spins 0..3) of that colour. Per hop each warp
 // projects the neighbour spinor of its colour, the three warps share the
 // half spinors through shared memory, and each warp multiplies its link row.
-// The hops run as a loop with one compiled body; with S the projector sign,
+// The eight hops are unrolled (directions and signs compile-time); with S
+// the projector sign,
 // (1 + S g_mu) in the chiral basis is
 //   h0 = p0 + c0 p_b0, h1 = p1 + c1 p_b1            (upper half)
 //   b0 = 2 (mu 0,3) or 3 (mu 1,2), b1 = 5 - b0, c = +-1 (mu even) or +-i (odd)
@@ -188,63 +188,95 @@ __device__ __forceinline__ CF coef(CF z, bool ifl, bool ng)
 //   r2 = cA v_jA, r3 = cB v_jB ; jA = 1 for mu 1,2 else 0, jB = 1 - jA
 //   cA = -S (mu 0) else +S ; cB = +S (mu 1) else -S ; times i for odd mu
 // (qcd_wilson.h:17-387).
+//
+// Each group of three warps synchronises on its own named barrier (ids 1..4,
+// 96 threads), so the four groups of a block never wait for one another.
+//
+// The spin projections (adds of two spinor components) run in native FP64
+// straight after the loads, and only the half spinor is split into float
+// pairs: two double -> pair conversions per half-spinor component instead of
+// four, for four FP64 adds per hop and warp. The FP64 pipe is far too slow
+// for the operator's multiply-adds, but it is otherwise idle here, and the
+// conversions it saves are integer work on the issue-bound FP32 side.
+// (Measured on GB300, 24^3x48: 0.505 -> 0.440 ms per apply; unrolled hops
+// and the 47-bit split: 0.425 ms. Moving more --
+// the epilogue, whole hops, or whole site groups -- onto the FP64 pipe was
+// slower.)
 constexpr int kFFSites = 128;
 
-// EO: even/odd kernel on half fields (sites of parity a.eo_par; neighbours
-// read at (full index) >> 1) with the epilogue ch * [A^{-1}] H in + {z | A z}
-template <bool DAG, bool EO>
-__global__ void __launch_bounds__(384, 3) k_wilson_ff(const DArgs a)
+__device__ __forceinline__ void group_bar(int grp) { asm volatile("bar.sync %0, 96;" ::"r"(grp + 1) : "memory"); }
+
+// site of output index e; EO: the site of parity eo_par among full indices
+// 2e, 2e + 1 (even t extent)
+template <bool EO>
+__device__ __forceinline__ int ff_site(const DArgs &a, int e, bool act, int c[4])
 {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int grp = w / 3, col = w - 3 * grp;
-  const int e = a.x0 + blockIdx.x * kFFSites + grp * 32 + lane;  // output index
-  const bool act = e < a.V;
-  __shared__ CF hs[4][2][3][32];
+  c[0] = c[1] = c[2] = c[3] = 0;
+  if (!act) return e;
+  if (EO) {
+    coords(a.geo, 2 * e, c);
+    const int b = (a.eo_par ^ c[1] ^ c[2] ^ c[3]) & 1;
+    c[0] += b;
+    return 2 * e + b;
+  }
+  coords(a.geo, e, c);
+  return e;
+}
+
+// neighbour of x across direction mu (backwards if back), periodic
+__device__ __forceinline__ int ff_nb(const DArgs &a, int x, const int c[4], int mu, bool back)
+{
+  const int cm = mu == 0 ? c[0] : mu == 1 ? c[1] : mu == 2 ? c[2] : c[3];
+  const int Lm = a.geo.L[mu], st = a.geo.st[mu];
+  if (back) return cm == 0 ? x + (Lm - 1) * st : x - st;
+  return cm == Lm - 1 ? x - (Lm - 1) * st : x + st;
+}
+
+// sign flip by integer operation (keeps the FP64 pipe for arithmetic)
+__device__ __forceinline__ double dflip(double v, bool ng)
+{
+  return __longlong_as_double(__double_as_longlong(v) ^ ((long long)ng << 63));
+}
+// z -> (i z if ifl) then negated if ng
+__device__ __forceinline__ double2 dcoef(double2 z, bool ifl, bool ng)
+{
+  return make_double2(dflip(ifl ? z.y : z.x, ng ^ ifl), dflip(ifl ? z.x : z.y, ng));
+}
+__device__ __forceinline__ double2 dadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+
+// the float-float operator for one group's 32 sites; returns the thread's |out|^2
+template <bool DAG, bool EO>
+__device__ __forceinline__ double group_ff(const DArgs &a, int grp, int col, int lane, int e, bool act, int x,
+                                           const int c[4], CF (*hs)[2][3][32])
+{
   const double2 *sp = (const double2 *)a.in;
   const float4 *gf = (const float4 *)a.gauge;
   constexpr int SF = DAG ? +1 : -1;
-  int c[4] = {0, 0, 0, 0};
-  int x = e;
-  if (act) {
-    if (EO) {  // the site of parity eo_par among full indices 2e, 2e + 1 (even t extent)
-      coords(a.geo, 2 * e, c);
-      const int b = (a.eo_par ^ c[1] ^ c[2] ^ c[3]) & 1;
-      x = 2 * e + b;
-      c[0] += b;
-    } else {
-      coords(a.geo, x, c);
-    }
-  }
   CA acc[4];
 #pragma unroll
   for (int s = 0; s < 4; s++) acc[s] = CA{{0.f, 0.f}, {0.f, 0.f}};
-#pragma unroll 1
+#pragma unroll
   for (int d = 0; d < 8; d++) {
     const int mu = d >> 1;
     const bool back = d & 1;
     const int S = back ? -SF : SF;
-    const int cm = mu == 0 ? c[0] : mu == 1 ? c[1] : mu == 2 ? c[2] : c[3];
-    const int Lm = a.geo.L[mu], st = a.geo.st[mu];
-    int y = x;
-    if (act) {
-      if (back) y = cm == 0 ? x + (Lm - 1) * st : x - st;
-      else y = cm == Lm - 1 ? x - (Lm - 1) * st : x + st;
-    }
+    const int y = act ? ff_nb(a, x, c, mu, back) : x;
     const int ly = back ? y : x;
     const bool odd = mu & 1;
     const int b0 = (mu == 0 || mu == 3) ? 2 : 3, b1 = 5 - b0;
     const bool neg0 = S > 0, neg1 = mu < 2 ? S > 0 : S < 0;
-    CF h0 = {{0.f, 0.f}, {0.f, 0.f}}, h1 = h0;
+    double2 d0 = make_double2(0.0, 0.0), d1 = d0;
     if (act) {
       const int ys = EO ? (y >> 1) : y;
-      CF p0 = load_sp(sp, a.stride, ys, col), p1 = load_sp(sp, a.stride, ys, 3 + col);
-      CF q0 = load_sp(sp, a.stride, ys, 3 * b0 + col), q1 = load_sp(sp, a.stride, ys, 3 * b1 + col);
-      h0 = cadd(p0, coef(q0, odd, neg0));
-      h1 = cadd(p1, coef(q1, odd, neg1));
+      const double2 p0 = __ldg(sp + (int64_t)col * a.stride + ys), p1 = __ldg(sp + (int64_t)(3 + col) * a.stride + ys);
+      const double2 q0 = __ldg(sp + (int64_t)(3 * b0 + col) * a.stride + ys);
+      const double2 q1 = __ldg(sp + (int64_t)(3 * b1 + col) * a.stride + ys);
+      d0 = dadd(p0, dcoef(q0, odd, neg0));
+      d1 = dadd(p1, dcoef(q1, odd, neg1));
     }
-    hs[grp][0][col][lane] = h0;
-    hs[grp][1][col][lane] = h1;
-    __syncthreads();
+    hs[grp][0][col][lane] = CF{split_d(d0.x), split_d(d0.y)};
+    hs[grp][1][col][lane] = CF{split_d(d1.x), split_d(d1.y)};
+    group_bar(grp);
     CA u0 = {{0.f, 0.f}, {0.f, 0.f}}, u1 = u0;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
@@ -261,17 +293,18 @@ __global__ void __launch_bounds__(384, 3) k_wilson_ff(const DArgs a)
       mac(u1.im, wr, g1.im);
       mac(u1.im, wi, g1.re);
     }
-    CF v0{fin(u0.re), fin(u0.im)}, v1{fin(u1.re), fin(u1.im)};
+    const CF v0{fin(u0.re), fin(u0.im)}, v1{fin(u1.re), fin(u1.im)};
     const bool jA = (mu == 1 || mu == 2);
     const bool negA = mu == 0 ? S > 0 : S < 0, negB = mu == 1 ? S < 0 : S > 0;
     cacc(acc[0], v0);
     cacc(acc[1], v1);
     cacc(acc[2], coef(jA ? v1 : v0, odd, negA));
     cacc(acc[3], coef(jA ? v0 : v1, odd, negB));
-    __syncthreads();  // hs is rewritten by the next hop
+    group_bar(grp);  // hs is rewritten by the next hop
   }
+  if (!act) return 0.0;
   double n2 = 0.0;
-  if (EO && act) {
+  if (EO) {
     double2 *out = (double2 *)a.out;
     const F2 mp4{a.mp4_h, a.mp4_l}, tm{a.tm_h, a.tm_l}, ch{a.ch_h, a.ch_l};
     const F2 air{a.ai_r_h, a.ai_r_l}, aii{a.ai_i_h, a.ai_i_l};
@@ -309,7 +342,7 @@ __global__ void __launch_bounds__(384, 3) k_wilson_ff(const DArgs a)
       out[(int64_t)k * a.stride + e] = make_double2(vr, vi);
       n2 += vr * vr + vi * vi;
     }
-  } else if (act) {
+  } else {
     double2 *out = (double2 *)a.out;
     const F2 mp4{a.mp4_h, a.mp4_l}, tm{a.tm_h, a.tm_l};
 #pragma unroll
@@ -341,6 +374,22 @@ __global__ void __launch_bounds__(384, 3) k_wilson_ff(const DArgs a)
       n2 += vr * vr + vi * vi;
     }
   }
+  return n2;
+}
+
+// EO: even/odd kernel on half fields (sites of parity a.eo_par; neighbours
+// read at (full index) >> 1) with the epilogue ch * [A^{-1}] H in + {z | A z}
+template <bool DAG, bool EO>
+__global__ void __launch_bounds__(384, 3) k_wilson_ff(const DArgs a)
+{
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int grp = w / 3, col = w - 3 * grp;
+  const int e = a.x0 + blockIdx.x * kFFSites + grp * 32 + lane;  // output index
+  const bool act = e < a.V;
+  __shared__ CF hs[4][2][3][32];
+  int c[4];
+  const int x = ff_site<EO>(a, e, act, c);
+  const double n2 = group_ff<DAG, EO>(a, grp, col, lane, e, act, x, c, hs);
   if (a.partials) block_partial(n2, a.partials);
 }
 
