@@ -32,6 +32,28 @@ __global__ void k_axpby(void *out, float *onorm, R ar, R ai, const void *x, cons
   Spinor<P, R>::store(out, onorm, stride, s, vx);
 }
 
+// out = a x + b y with real a, b: b y + x (a = 1: exact for b = +-1) or
+// b y + (a x); one or two FP64 operations per real instead of the complex
+// form's six (GB300's FP64 pipe, not HBM, bounds the complex form)
+template <int P, typename R>
+__global__ void k_axpby_real(void *out, float *onorm, R a, const void *x, const float *xn, R b, const void *y,
+                             const float *yn, int64_t stride, int64_t V)
+{
+  int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= V) return;
+  C<R> vx[12], vy[12];
+  Spinor<P, R>::load(x, xn, stride, s, vx);
+  Spinor<P, R>::load(y, yn, stride, s, vy);
+  const bool unit = a == (R)1;
+#pragma unroll
+  for (int k = 0; k < 12; k++) {
+    const R xr = unit ? vx[k].re : a * vx[k].re, xi = unit ? vx[k].im : a * vx[k].im;
+    vx[k].re = qfma(b, vy[k].re, xr);
+    vx[k].im = qfma(b, vy[k].im, xi);
+  }
+  Spinor<P, R>::store(out, onorm, stride, s, vx);
+}
+
 // y = a x + y with real a: one fused multiply-add per real
 template <int P, typename R>
 __global__ void k_axpy_real(void *y, float *yn, R a, const void *x, const float *xn, int64_t stride,
@@ -120,25 +142,50 @@ __global__ void __launch_bounds__(256) k_reduce(const void *a, const float *an, 
        s += (int64_t)gridDim.x * blockDim.x) {
     C<R> va[12];
     Spinor<P, R>::load(a, an, stride, s, va);
+    // FP64 fields: FP64 products and sums; FP32 / FP16 fields: the site's
+    // twelve terms in FP32 (their own precision), the sum over sites in FP64
+    // (FP64 arithmetic per component would make these kernels FP64-pipe bound)
+    constexpr bool F = sizeof(R) == 4;
     if (KIND == 0) {
+      if (F) {
+        R t = (R)0;
 #pragma unroll
-      for (int k = 0; k < 12; k++) s0 += (double)va[k].re * va[k].re + (double)va[k].im * va[k].im;
+        for (int k = 0; k < 12; k++) t += va[k].re * va[k].re + va[k].im * va[k].im;
+        s0 += (double)t;
+      } else {
+#pragma unroll
+        for (int k = 0; k < 12; k++) s0 += (double)va[k].re * va[k].re + (double)va[k].im * va[k].im;
+      }
     } else if (KIND == 1) {
       C<R> vb[12];
       Spinor<P, R>::load(b, bn, stride, s, vb);
+      if (F) {
+        R t0 = (R)0, t1 = (R)0;
 #pragma unroll
-      for (int k = 0; k < 12; k++) {
-        s0 += (double)va[k].re * vb[k].re + (double)va[k].im * vb[k].im;
-        s1 += (double)va[k].re * vb[k].im - (double)va[k].im * vb[k].re;
+        for (int k = 0; k < 12; k++) {
+          t0 += va[k].re * vb[k].re + va[k].im * vb[k].im;
+          t1 += va[k].re * vb[k].im - va[k].im * vb[k].re;
+        }
+        s0 += (double)t0;
+        s1 += (double)t1;
+      } else {
+#pragma unroll
+        for (int k = 0; k < 12; k++) {
+          s0 += (double)va[k].re * vb[k].re + (double)va[k].im * vb[k].im;
+          s1 += (double)va[k].re * vb[k].im - (double)va[k].im * vb[k].re;
+        }
       }
     } else {
       C<R> vb[12], c{ar, ai};
       Spinor<P, R>::load(b, bn, stride, s, vb);
+      R t = (R)0;
 #pragma unroll
       for (int k = 0; k < 12; k++) {
         vb[k] = vb[k] + c * va[k];
-        s0 += (double)vb[k].re * vb[k].re + (double)vb[k].im * vb[k].im;
+        if (F) t += vb[k].re * vb[k].re + vb[k].im * vb[k].im;
+        else s0 += (double)vb[k].re * vb[k].re + (double)vb[k].im * vb[k].im;
       }
+      if (F) s0 += (double)t;
       Spinor<P, R>::store(b, bn, stride, s, vb);
     }
   }
@@ -213,6 +260,13 @@ bool blas_axpby(qcdgpu_field out, double ar, double ai, qcdgpu_field x, double b
                 (k_axpy_real<QCDGPU_F32, float><<<g, 128, 0, st>>>(y->data, y->norm, (float)ar, x->data, x->norm, out->stride, out->V)),
                 (k_axpy_real<QCDGPU_F16, float><<<g, 128, 0, st>>>(y->data, y->norm, (float)ar, x->data, x->norm, out->stride, out->V)));
     return QG_LAUNCHED("axpy_real");
+  }
+  if (ai == 0.0 && bi == 0.0) {
+    QG_DISPATCH(out->prec,
+                (k_axpby_real<QCDGPU_F64, double><<<g, 128, 0, st>>>(out->data, out->norm, ar, x->data, x->norm, br, y->data, y->norm, out->stride, out->V)),
+                (k_axpby_real<QCDGPU_F32, float><<<g, 128, 0, st>>>(out->data, out->norm, (float)ar, x->data, x->norm, (float)br, y->data, y->norm, out->stride, out->V)),
+                (k_axpby_real<QCDGPU_F16, float><<<g, 128, 0, st>>>(out->data, out->norm, (float)ar, x->data, x->norm, (float)br, y->data, y->norm, out->stride, out->V)));
+    return QG_LAUNCHED("axpby_real");
   }
   QG_DISPATCH(out->prec,
               (k_axpby<QCDGPU_F64, double><<<g, 128, 0, st>>>(out->data, out->norm, ar, ai, x->data, x->norm, br, bi, y->data, y->norm, out->stride, out->V)),

@@ -41,10 +41,59 @@ double *big_partials(int64_t n);
 enum { S_RR = 0, S_PAP = 1, S_RRNEW = 2, S_ALPHA = 3, S_BETA = 4, S_HIST = 8 };
 constexpr int kChunk = 16;
 
+// the CG scalars from a reduced total: mode 0 t = p^+ A p -> alpha;
+// mode 1 t = |r|^2 -> beta and the residual history
+__device__ __forceinline__ void cg_scalars_from(double t, double *s, int mode, int hist)
+{
+  if (mode == 0) {
+    s[S_PAP] = t;
+    s[S_ALPHA] = t > 0.0 ? s[S_RR] / t : nan("");  // p^+ A p <= 0: breakdown
+  } else {
+    s[S_RRNEW] = t;
+    s[S_BETA] = t / s[S_RR];
+    s[S_RR] = t;
+    s[S_HIST + hist] = t;
+  }
+}
+
+// Called by every thread of a 128-thread block after block_partial wrote the
+// block's partial: the block that finishes last sums all gridDim.x partials
+// in index order (the same order whichever block is last), updates the
+// scalars and re-arms the counter. No block waits for another.
+__device__ __forceinline__ void cg_last_block(const double *partials, unsigned *done, double *s, int mode, int hist)
+{
+  __shared__ unsigned last;
+  __shared__ double sh[4];
+  if (threadIdx.x == 0) {
+    __threadfence();  // this block's partial before its count
+    last = atomicAdd(done, 1u) == gridDim.x - 1 ? 1u : 0u;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // eight independent loads in flight per thread, summed in a fixed order
+  const int n = (int)gridDim.x;
+  double v = 0.0;
+  for (int i0 = threadIdx.x; i0 < n; i0 += 8 * 128) {
+    double w[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) w[k] = i0 + k * 128 < n ? __ldcg(partials + i0 + k * 128) : 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) v += w[k];
+  }
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    cg_scalars_from(sh[0] + sh[1] + sh[2] + sh[3], s, mode, hist);
+    *done = 0u;
+  }
+}
+
 template <int P, typename R>
 __global__ void __launch_bounds__(128) k_cg_update(void *xs, float *xsn, const void *ps, const float *psn, void *rs,
                                                    float *rsn, const void *aps, const float *apsn, int64_t stride,
-                                                   int V, const double *s, double *partials)
+                                                   int V, double *s, double *partials, unsigned *done, int hist)
 {
   int x = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   double n2 = 0.0;
@@ -75,6 +124,7 @@ __global__ void __launch_bounds__(128) k_cg_update(void *xs, float *xsn, const v
     Spinor<P, R>::store(rs, rsn, stride, x, vx);
   }
   block_partial(n2, partials);
+  cg_last_block(partials, done, s, 1, hist);
 }
 
 template <int P, typename R>
@@ -99,7 +149,8 @@ __global__ void __launch_bounds__(128) k_cg_p(void *ps, float *psn, const void *
 // FP16 fields A p = D^+ round(D p), and |D p|^2 would not match it)
 template <int P, typename R>
 __global__ void __launch_bounds__(128) k_dot_re(const void *a, const float *an, const void *b, const float *bn,
-                                                int64_t stride, int V, double *partials)
+                                                int64_t stride, int V, double *partials, double *s,
+                                                unsigned *done, int hist)
 {
   int x = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   double d = 0.0;
@@ -107,10 +158,13 @@ __global__ void __launch_bounds__(128) k_dot_re(const void *a, const float *an, 
     C<R> va[12], vb[12];
     Spinor<P, R>::load(a, an, stride, x, va);
     Spinor<P, R>::load(b, bn, stride, x, vb);
+    R t = (R)0;
 #pragma unroll
-    for (int k = 0; k < 12; k++) d += (double)(va[k].re * vb[k].re + va[k].im * vb[k].im);
+    for (int k = 0; k < 12; k++) t += va[k].re * vb[k].re + va[k].im * vb[k].im;
+    d = (double)t;  // per-site sum in the working precision, block sum in double
   }
   block_partial(d, partials);
+  cg_last_block(partials, done, s, 0, hist);
 }
 
 // one block: sum n partials in a fixed order and update the scalars
@@ -125,15 +179,7 @@ __global__ void k_cg_scalars(const double *partials, int n, double *s, int mode,
   if (threadIdx.x == 0) {
     double t = 0.0;
     for (int i = 0; i < (int)(blockDim.x >> 5); i++) t += sh[i];
-    if (mode == 0) {
-      s[S_PAP] = t;
-      s[S_ALPHA] = t > 0.0 ? s[S_RR] / t : nan("");  // p^+ A p <= 0: breakdown
-    } else {
-      s[S_RRNEW] = t;
-      s[S_BETA] = t / s[S_RR];
-      s[S_RR] = t;
-      s[S_HIST + hist] = t;
-    }
+    cg_scalars_from(t, s, mode, hist);
   }
 }
 
@@ -173,6 +219,55 @@ struct Held {
   }
 };
 
+// A chunk of solver iterations recorded once and replayed. Recording runs
+// on a library-owned stream (the caller's stream may be the legacy default
+// stream, which cannot be captured); the replay goes to the caller's stream.
+// If recording fails the solver keeps launching the chunk directly.
+struct ChunkGraph {
+  cudaGraphExec_t exec = nullptr;
+  uint64_t launches = 0;
+  bool usable = true;
+  ~ChunkGraph()
+  {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+  template <typename F>
+  bool run(cudaStream_t st, F &&enqueue)
+  {
+    if (!exec) {
+      static cudaStream_t cs = nullptr;
+      if (!cs && cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) cs = nullptr;
+      if (!cs) {
+        usable = false;
+        cudaGetLastError();
+        return enqueue();
+      }
+      cudaGraph_t graph = nullptr;
+      const uint64_t counted = g_launches.load();
+      bool ok = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+      if (ok) {
+        const cudaStream_t prev = swap_stream(cs);
+        ok = enqueue();
+        swap_stream(prev);
+        ok = cudaStreamEndCapture(cs, &graph) == cudaSuccess && ok;
+      }
+      launches = g_launches.load() - counted;
+      g_launches.store(counted);  // recorded, not launched
+      ok = ok && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+      if (graph) cudaGraphDestroy(graph);
+      if (!ok) {
+        exec = nullptr;
+        usable = false;
+        cudaGetLastError();
+        return enqueue();
+      }
+    }
+    if (!QG_CUDA(cudaGraphLaunch(exec, st))) return false;
+    count_launches(launches);
+    return true;
+  }
+};
+
 // CG on A^+ A y = A^+ c, x0 = 0, chunked with reliable updates; convergence
 // on the true residual |c - A y| / cn (cn: the norm the residual is relative
 // to). Returns 0 converged, 1 maxiter, 2 breakdown, 3 CUDA error.
@@ -192,7 +287,9 @@ static int cgnr_core(qcdgpu_field y, qcdgpu_field c, double cn, const CgOps &ops
   double *h = host_result();
   if (!part || !s || !h) return 3;
   s += 2 * kMaxPartials + 16;  // 16 + kChunk slots past the blas result words
+  unsigned *done = (unsigned *)(s + S_HIST + kChunk);  // block counters of the fused reductions
   cudaStream_t st = stream();
+  if (!QG_CUDA(cudaMemsetAsync(done, 0, 2 * sizeof(unsigned), st))) return 3;
   if (!blas_zero(y)) return 3;
   // true residual rt = c - A y (FP64), returns |rt| / cn
   auto true_res = [&](double *rel) -> bool {
@@ -224,35 +321,46 @@ static int cgnr_core(qcdgpu_field y, qcdgpu_field c, double cn, const CgOps &ops
   bool first = true;
   const double delta = p->delta > 0 ? p->delta : 0.1;
   int since_update = 0;
-  while (true) {
-    int chunk = kChunk;
-    if (p->maxiter - p->iters < chunk) chunk = p->maxiter - p->iters;
+  // one chunk of iterations; every chunk after the first launches the same
+  // kernels with the same arguments, so it is captured once as a CUDA graph
+  // and replayed (the captured launches are counted at each replay)
+  auto enqueue_chunk = [&](int chunk) -> bool {
+    const cudaStream_t st = stream();  // the capture stream while a graph is recorded
     for (int j = 0; j < chunk; j++) {
       // p = r + beta p opens each iteration (not the first), so a reliable
       // update between chunks enters the next direction through beta
       if (!first) {
         QG_PREC_DISPATCH(prec, k_cg_p, ps->data, ps->norm, rs->data, rs->norm, ps->stride, V, s);
-        if (!QG_LAUNCHED("cg_p")) return 3;
+        if (!QG_LAUNCHED("cg_p")) return false;
       }
       first = false;
       if (prec != QCDGPU_F16) {
         // p^+ A^+ A p = |A p|^2 summed in the epilogue of the first operator
-        if (!ops.op(t, ps, part)) return 3;
+        if (!ops.op(t, ps, part)) return false;
         k_cg_scalars<<<1, 256, 0, st>>>(part, (int)nb, s, 0, j);
-        if (!QG_LAUNCHED("cg_scalars")) return 3;
-        if (!ops.opdag(aps, t)) return 3;
+        if (!QG_LAUNCHED("cg_scalars")) return false;
+        if (!ops.opdag(aps, t)) return false;
       } else {
-        if (!ops.op(t, ps, nullptr) || !ops.opdag(aps, t)) return 3;
-        k_dot_re<QCDGPU_F16, float><<<nb, 128, 0, st>>>(ps->data, ps->norm, aps->data, aps->norm, ps->stride, V, part);
-        if (!QG_LAUNCHED("cg_dot")) return 3;
-        k_cg_scalars<<<1, 256, 0, st>>>(part, (int)nb, s, 0, j);
-        if (!QG_LAUNCHED("cg_scalars")) return 3;
+        if (!ops.op(t, ps, nullptr) || !ops.opdag(aps, t)) return false;
+        // p^+ A p and alpha in one launch
+        k_dot_re<QCDGPU_F16, float><<<nb, 128, 0, st>>>(ps->data, ps->norm, aps->data, aps->norm, ps->stride, V, part,
+                                                         s, done, j);
+        if (!QG_LAUNCHED("cg_dot")) return false;
       }
       QG_PREC_DISPATCH(prec, k_cg_update, xs->data, xs->norm, ps->data, ps->norm, rs->data, rs->norm, aps->data,
-                       aps->norm, xs->stride, V, s, part);
-      if (!QG_LAUNCHED("cg_update")) return 3;
-      k_cg_scalars<<<1, 256, 0, st>>>(part, (int)nb, s, 1, j);
-      if (!QG_LAUNCHED("cg_scalars")) return 3;
+                       aps->norm, xs->stride, V, s, part, done + 1, j);  // with |r|^2 and beta
+      if (!QG_LAUNCHED("cg_update")) return false;
+    }
+    return true;
+  };
+  ChunkGraph graph;
+  while (true) {
+    int chunk = kChunk;
+    if (p->maxiter - p->iters < chunk) chunk = p->maxiter - p->iters;
+    if (!first && chunk == kChunk && graph.usable) {
+      if (!graph.run(st, [&] { return enqueue_chunk(chunk); })) return 3;
+    } else {
+      if (!enqueue_chunk(chunk)) return 3;
     }
     // history, and rr / beta of the last iteration (slots 0..S_HIST+kChunk)
     if (!QG_CUDA(cudaMemcpyAsync(h, s, sizeof(double) * (S_HIST + chunk), cudaMemcpyDeviceToHost, st)) ||

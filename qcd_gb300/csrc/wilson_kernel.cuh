@@ -63,6 +63,58 @@ __device__ __forceinline__ void accumulate(C<R> acc[12], const C<R> h[6])
   }
 }
 
+// h = upper half of (1 + S g_mu) s for the spinor s at index y: any storage
+// loads the twelve components, then projects
+template <int MU, int S, int SP, typename R>
+struct LoadProject {
+  __device__ __forceinline__ static void run(const void *base, const float *norm, int64_t stride, int64_t y,
+                                             C<R> h[6])
+  {
+    C<R> s[12];
+    Spinor<SP, R>::load(base, norm, stride, y, s);
+    project<MU, S>(s, h);
+  }
+};
+
+// a + sg b (IM: a + sg i b) on packed (re, im) half pairs
+template <bool IM>
+__device__ __forceinline__ __half2 hcomb(__half2 a, __half2 b, int sg)
+{
+  if (IM) return __hfma2(__lowhigh2highlow(b), sg > 0 ? __floats2half2_rn(-1.f, 1.f) : __floats2half2_rn(1.f, -1.f), a);
+  return sg > 0 ? __hadd2(a, b) : __hsub2(a, b);
+}
+
+// FP16 storage (component k = 3 spin + colour is the k-th (re, im) half pair
+// of the site's three 16-byte words): the projection adds the stored half
+// pairs directly (one FP16 rounding per projected component, below the
+// storage's own 2^-11), and only the six projected components are converted
+// and scaled by the site norm -- half the conversions and multiplies of
+// decoding all twelve (measured: 57.4 -> 54.0 us per 24^3x48 apply)
+template <int MU, int S>
+struct LoadProject<MU, S, QCDGPU_F16, float> {
+  __device__ __forceinline__ static void run(const void *base, const float *norm, int64_t stride, int64_t y,
+                                             C<float> h[6])
+  {
+    const uint4 *p = (const uint4 *)base + y;
+    const float nrm = __ldg(norm + y);
+    uint4 w[3];
+#pragma unroll
+    for (int j = 0; j < 3; j++) w[j] = __ldg(p + j * stride);
+    const __half2 *hv = reinterpret_cast<const __half2 *>(w);
+    constexpr bool IM = MU & 1;
+    // partner spins and signs of the two projected halves (as in project())
+    constexpr int B0 = (MU == 0 || MU == 3) ? 2 : 3, B1 = 5 - B0;
+    constexpr int SG0 = S > 0 ? -1 : 1, SG1 = MU < 2 ? SG0 : -SG0;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const float2 f0 = __half22float2(hcomb<IM>(hv[c], hv[3 * B0 + c], SG0));
+      const float2 f1 = __half22float2(hcomb<IM>(hv[3 + c], hv[3 * B1 + c], SG1));
+      h[c] = C<float>{nrm * f0.x, nrm * f0.y};
+      h[3 + c] = C<float>{nrm * f1.x, nrm * f1.y};
+    }
+  }
+};
+
 template <int MU, bool DAG, int SP, int GP, int RECON, typename R, bool EO = false>
 __device__ __forceinline__ void hop_pair(const DArgs &a, int x, const int c[4], C<R> acc[12])
 {
@@ -70,9 +122,8 @@ __device__ __forceinline__ void hop_pair(const DArgs &a, int x, const int c[4], 
   const bool twisted = (a.twist_mask >> MU) & 1;
   {
     int y = fwd(a.geo, x, c, MU);
-    C<R> s[12], h[6], uh[6], U[9];
-    Spinor<SP, R>::load(a.in, a.in_norm, a.stride, EO ? (y >> 1) : y, s);
-    project<MU, SF>(s, h);
+    C<R> h[6], uh[6], U[9];
+    LoadProject<MU, SF, SP, R>::run(a.in, a.in_norm, a.stride, EO ? (y >> 1) : y, h);
     Link<GP, RECON, R>::load(a.gauge, a.gstride, x, MU, U);
 #pragma unroll
     for (int j = 0; j < 2; j++)
@@ -88,9 +139,8 @@ __device__ __forceinline__ void hop_pair(const DArgs &a, int x, const int c[4], 
   }
   {
     int y = bwd(a.geo, x, c, MU);
-    C<R> s[12], h[6], uh[6], U[9];
-    Spinor<SP, R>::load(a.in, a.in_norm, a.stride, EO ? (y >> 1) : y, s);
-    project<MU, -SF>(s, h);
+    C<R> h[6], uh[6], U[9];
+    LoadProject<MU, -SF, SP, R>::run(a.in, a.in_norm, a.stride, EO ? (y >> 1) : y, h);
     Link<GP, RECON, R>::load(a.gauge, a.gstride, y, MU, U);
 #pragma unroll
     for (int j = 0; j < 2; j++)
