@@ -249,6 +249,10 @@ int qcdgpu_sync(void);
 void qcdgpu_set_gcr_compat(int shipped);
 /* arithmetic of the FP64 operator used by the Part-2 entry points */
 int qcdgpu_set_f64_arith(int arith);
+/* slabs of the pipelined host-buffer operator apply (0: automatic, the largest
+ * of 24, 16, 12, 8, 6, 4, 3 dividing L_z; otherwise a divisor of L_z, >= 3);
+ * a tuning knob with no reference counterpart */
+int qcdgpu_set_pipeline_slabs(int S);
 /* number of kernels this library launched since the process started */
 uint64_t qcdgpu_kernel_launches(void);
 

@@ -166,21 +166,27 @@ static bool check_op_args(qcd_vector *Dv, qcd_vector *v, qcd_gaugeField *u)
 }
 
 // Pipelined apply for page-locked host vectors: the lattice is cut into S
-// slabs of whole z-planes; slab k is copied in by the copy engine and
-// reordered on s_in, applied as soon as slabs k-1..k+1 are in (on the
-// library stream), and reordered and copied back on s_out while later slabs
-// are still arriving, so the two copy directions and the operator overlap.
-// Slabs 0 and S-1 need each other (periodic z), so the order of application
-// is 1 .. S-2, S-1, 0.
-static cudaStream_t g_s_in, g_s_out;
-static std::vector<cudaEvent_t> g_ev_in, g_ev_op;
-static cudaEvent_t g_ev_start, g_ev_done;
+// slabs of whole z-planes (up to 24). Each stage runs on its own stream,
+// chained per slab by events, so the copy engines stream their slabs back
+// to back: c_in copies slab k in, s_in reorders it to the field layout, the
+// operator runs as soon as slabs k-1..k+1 are in (consecutive slabs
+// alternating between the library stream and op2, so thin slabs share the
+// GPU), s_out reorders the result and c_out copies it out. Slabs 0 and S-1
+// need each other (periodic z), so the order of application is
+// 1 .. S-2, S-1, 0. The host link bounds it: 254 MB per 24^3x48 apply at
+// the 340 GB/s both directions reach together is 0.75 ms.
+static cudaStream_t g_c_in, g_s_in, g_s_out, g_c_out, g_s_op2;
+static std::vector<cudaEvent_t> g_ev_cin, g_ev_in, g_ev_op, g_ev_rout;
+static cudaEvent_t g_ev_start, g_ev_done, g_ev_op2;
 static void *g_stage_in, *g_stage_out;  // device copies of the host layout
 static size_t g_stage_bytes;
 
+static int g_pipe_slabs = 0;  // 0: the largest of 24, 16, 12, 8, 6, 4, 3 dividing L_z
+
 static int pipeline_slabs(const qcdgpu_field f)
 {
-  for (int S : {12, 8, 6, 4, 3})
+  if (g_pipe_slabs > 0) return f->L[3] % g_pipe_slabs == 0 && g_pipe_slabs >= 3 ? g_pipe_slabs : 0;
+  for (int S : {24, 16, 12, 8, 6, 4, 3})
     if (f->L[3] % S == 0) return S;
   return 0;
 }
@@ -188,20 +194,82 @@ static int pipeline_slabs(const qcdgpu_field f)
 static bool pipeline_ready(int S)
 {
   if (!g_s_in) {
-    if (!QG_CUDA(cudaStreamCreateWithFlags(&g_s_in, cudaStreamNonBlocking)) ||
-        !QG_CUDA(cudaStreamCreateWithFlags(&g_s_out, cudaStreamNonBlocking)) ||
-        !QG_CUDA(cudaEventCreateWithFlags(&g_ev_start, cudaEventDisableTiming)) ||
-        !QG_CUDA(cudaEventCreateWithFlags(&g_ev_done, cudaEventDisableTiming)))
+    for (cudaStream_t *q : {&g_c_in, &g_s_in, &g_s_out, &g_c_out, &g_s_op2})
+      if (!QG_CUDA(cudaStreamCreateWithFlags(q, cudaStreamNonBlocking))) return false;
+    if (!QG_CUDA(cudaEventCreateWithFlags(&g_ev_start, cudaEventDisableTiming)) ||
+        !QG_CUDA(cudaEventCreateWithFlags(&g_ev_done, cudaEventDisableTiming)) ||
+        !QG_CUDA(cudaEventCreateWithFlags(&g_ev_op2, cudaEventDisableTiming)))
       return false;
   }
   while ((int)g_ev_in.size() < S) {
-    cudaEvent_t a, b;
-    if (!QG_CUDA(cudaEventCreateWithFlags(&a, cudaEventDisableTiming)) ||
-        !QG_CUDA(cudaEventCreateWithFlags(&b, cudaEventDisableTiming)))
-      return false;
-    g_ev_in.push_back(a);
-    g_ev_op.push_back(b);
+    cudaEvent_t e[4];
+    for (auto &x : e)
+      if (!QG_CUDA(cudaEventCreateWithFlags(&x, cudaEventDisableTiming))) return false;
+    g_ev_cin.push_back(e[0]);
+    g_ev_in.push_back(e[1]);
+    g_ev_op.push_back(e[2]);
+    g_ev_rout.push_back(e[3]);
   }
+  return true;
+}
+
+// the whole pipeline enqueued behind stream `origin` (which it joins again)
+static bool enqueue_pipeline(cudaStream_t origin, qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g,
+                             const double *vin, double *vout, double mp4, double tm, int op, int S)
+{
+  const int64_t V = in->V, slab = V / S;
+  const size_t sbytes = (size_t)V * 24 * sizeof(double) / S;
+  if (!QG_CUDA(cudaEventRecord(g_ev_start, origin))) return false;
+  for (cudaStream_t q : {g_c_in, g_s_in, g_s_out, g_c_out, g_s_op2})
+    if (!QG_CUDA(cudaStreamWaitEvent(q, g_ev_start, 0))) return false;
+  // host -> device copies, back to back
+  for (int k = 0; k < S; k++)
+    if (!QG_CUDA(cudaMemcpyAsync((char *)g_stage_in + k * sbytes, (const char *)vin + k * sbytes, sbytes,
+                                 cudaMemcpyHostToDevice, g_c_in)) ||
+        !QG_CUDA(cudaEventRecord(g_ev_cin[k], g_c_in)))
+      return false;
+  {
+    StreamScope scope(g_s_in);
+    for (int k = 0; k < S; k++)
+      if (!QG_CUDA(cudaStreamWaitEvent(g_s_in, g_ev_cin[k], 0)) ||
+          !spinor_from_aos_sites(in, g_stage_in, k * slab, (k + 1) * slab) ||
+          !QG_CUDA(cudaEventRecord(g_ev_in[k], g_s_in)))
+        return false;
+  }
+  std::vector<int> order;
+  for (int k = 1; k < S - 1; k++) order.push_back(k);
+  order.push_back(S - 1);
+  order.push_back(0);
+  // consecutive slabs alternate between two streams, so a thin slab's
+  // launch shares the GPU with the next one
+  for (size_t i = 0; i < order.size(); i++) {
+    const int k = order[i];
+    const int need = (k == 0 || k == S - 1) ? S - 1 : k + 1;
+    const cudaStream_t q = i % 2 ? g_s_op2 : origin;
+    StreamScope scope(q);
+    if (!QG_CUDA(cudaStreamWaitEvent(q, g_ev_in[need], 0)) ||
+        !dslash_sites(out, in, g, mp4, tm, op, -1, (int)(k * slab), (int)((k + 1) * slab)) ||
+        !QG_CUDA(cudaEventRecord(g_ev_op[k], q)))
+      return false;
+  }
+  {
+    StreamScope scope(g_s_out);
+    for (int k : order)
+      if (!QG_CUDA(cudaStreamWaitEvent(g_s_out, g_ev_op[k], 0)) ||
+          !spinor_to_aos_sites(out, g_stage_out, k * slab, (k + 1) * slab) ||
+          !QG_CUDA(cudaEventRecord(g_ev_rout[k], g_s_out)))
+        return false;
+  }
+  // device -> host copies, back to back as the slabs are ready
+  for (int k : order)
+    if (!QG_CUDA(cudaStreamWaitEvent(g_c_out, g_ev_rout[k], 0)) ||
+        !QG_CUDA(cudaMemcpyAsync((char *)vout + k * sbytes, (const char *)g_stage_out + k * sbytes, sbytes,
+                                 cudaMemcpyDeviceToHost, g_c_out)))
+      return false;
+  // join every side stream back into the origin
+  if (!QG_CUDA(cudaEventRecord(g_ev_done, g_c_out)) || !QG_CUDA(cudaStreamWaitEvent(origin, g_ev_done, 0)) ||
+      !QG_CUDA(cudaEventRecord(g_ev_op2, g_s_op2)) || !QG_CUDA(cudaStreamWaitEvent(origin, g_ev_op2, 0)))
+    return false;
   return true;
 }
 
@@ -209,8 +277,7 @@ static bool apply_pipelined(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, c
                             double mp4, double tm, int op, int S)
 {
   if (!pipeline_ready(S)) return false;
-  const int64_t V = in->V, slab = V / S;
-  const size_t bytes = (size_t)V * 24 * sizeof(double), sbytes = bytes / S;
+  const size_t bytes = (size_t)in->V * 24 * sizeof(double);
   if (bytes > g_stage_bytes) {
     cudaFree(g_stage_in);
     cudaFree(g_stage_out);
@@ -220,41 +287,7 @@ static bool apply_pipelined(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, c
     g_stage_bytes = bytes;
   }
   cudaStream_t st = stream();
-  if (!QG_CUDA(cudaEventRecord(g_ev_start, st)) || !QG_CUDA(cudaStreamWaitEvent(g_s_in, g_ev_start, 0)) ||
-      !QG_CUDA(cudaStreamWaitEvent(g_s_out, g_ev_start, 0)))
-    return false;
-  {
-    StreamScope scope(g_s_in);
-    for (int k = 0; k < S; k++) {
-      char *dst = (char *)g_stage_in + k * sbytes;
-      if (!QG_CUDA(cudaMemcpyAsync(dst, (const char *)vin + k * sbytes, sbytes, cudaMemcpyHostToDevice, g_s_in)) ||
-          !spinor_from_aos_sites(in, g_stage_in, k * slab, (k + 1) * slab) ||
-          !QG_CUDA(cudaEventRecord(g_ev_in[k], g_s_in)))
-        return false;
-    }
-  }
-  std::vector<int> order;
-  for (int k = 1; k < S - 1; k++) order.push_back(k);
-  order.push_back(S - 1);
-  order.push_back(0);
-  for (int k : order) {
-    const int need = (k == 0 || k == S - 1) ? S - 1 : k + 1;
-    if (!QG_CUDA(cudaStreamWaitEvent(st, g_ev_in[need], 0)) ||
-        !dslash_sites(out, in, g, mp4, tm, op, -1, (int)(k * slab), (int)((k + 1) * slab)) ||
-        !QG_CUDA(cudaEventRecord(g_ev_op[k], st)))
-      return false;
-  }
-  {
-    StreamScope scope(g_s_out);
-    for (int k : order)
-      if (!QG_CUDA(cudaStreamWaitEvent(g_s_out, g_ev_op[k], 0)) ||
-          !spinor_to_aos_sites(out, g_stage_out, k * slab, (k + 1) * slab) ||
-          !QG_CUDA(cudaMemcpyAsync((char *)vout + k * sbytes, (const char *)g_stage_out + k * sbytes, sbytes,
-                                   cudaMemcpyDeviceToHost, g_s_out)))
-        return false;
-  }
-  return QG_CUDA(cudaEventRecord(g_ev_done, g_s_out)) && QG_CUDA(cudaStreamWaitEvent(st, g_ev_done, 0)) &&
-         QG_CUDA(cudaStreamSynchronize(st));
+  return enqueue_pipeline(st, out, in, g, vin, vout, mp4, tm, op, S) && QG_CUDA(cudaStreamSynchronize(st));
 }
 
 static int apply_op(qcd_vector *Dv, qcd_vector *v, qcd_gaugeField *u, double m, double tm, int op)
@@ -823,3 +856,13 @@ int qcdgpu_gauge_release(qcd_gaugeField *u)
 }
 
 }  // extern "C"
+
+extern "C" int qcdgpu_set_pipeline_slabs(int S)
+{
+  if (S < 0 || S == 1 || S == 2) {
+    qg::set_error("pipeline slabs: 0 (automatic) or at least 3 (got %d)", S);
+    return 1;
+  }
+  qg::g_pipe_slabs = S;
+  return 0;
+}
