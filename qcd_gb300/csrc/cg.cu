@@ -63,7 +63,7 @@ __device__ __forceinline__ void cg_scalars_from(double t, double *s, int mode, i
 __device__ __forceinline__ void cg_last_block(const double *partials, unsigned *done, double *s, int mode, int hist)
 {
   __shared__ unsigned last;
-  __shared__ double sh[4];
+  __shared__ double sh[32];
   if (threadIdx.x == 0) {
     __threadfence();  // this block's partial before its count
     last = atomicAdd(done, 1u) == gridDim.x - 1 ? 1u : 0u;
@@ -74,10 +74,11 @@ __device__ __forceinline__ void cg_last_block(const double *partials, unsigned *
   // eight independent loads in flight per thread, summed in a fixed order
   const int n = (int)gridDim.x;
   double v = 0.0;
-  for (int i0 = threadIdx.x; i0 < n; i0 += 8 * 128) {
+  const int nt = (int)blockDim.x;
+  for (int i0 = threadIdx.x; i0 < n; i0 += 8 * nt) {
     double w[8];
 #pragma unroll
-    for (int k = 0; k < 8; k++) w[k] = i0 + k * 128 < n ? __ldcg(partials + i0 + k * 128) : 0.0;
+    for (int k = 0; k < 8; k++) w[k] = i0 + k * nt < n ? __ldcg(partials + i0 + k * nt) : 0.0;
 #pragma unroll
     for (int k = 0; k < 8; k++) v += w[k];
   }
@@ -85,18 +86,27 @@ __device__ __forceinline__ void cg_last_block(const double *partials, unsigned *
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
   __syncthreads();
   if (threadIdx.x == 0) {
-    cg_scalars_from(sh[0] + sh[1] + sh[2] + sh[3], s, mode, hist);
+    double t = 0.0;
+    for (int i = 0; i < nt >> 5; i++) t += sh[i];
+    cg_scalars_from(t, s, mode, hist);
     *done = 0u;
   }
 }
 
+// The two fused reductions run kCgSpt sites per thread in blocks of
+// kCgThreads: fewer blocks, so the last block sums fewer partials.
+constexpr int kCgThreads = 256, kCgSpt = 2, kCgSites = kCgThreads * kCgSpt;
+
 template <int P, typename R>
-__global__ void __launch_bounds__(128) k_cg_update(void *xs, float *xsn, const void *ps, const float *psn, void *rs,
-                                                   float *rsn, const void *aps, const float *apsn, int64_t stride,
-                                                   int V, double *s, double *partials, unsigned *done, int hist)
+__global__ void __launch_bounds__(kCgThreads) k_cg_update(void *xs, float *xsn, const void *ps, const float *psn,
+                                                          void *rs, float *rsn, const void *aps, const float *apsn,
+                                                          int64_t stride, int V, double *s, double *partials,
+                                                          unsigned *done, int hist)
 {
-  int x = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   double n2 = 0.0;
+#pragma unroll
+  for (int i = 0; i < kCgSpt; i++) {
+  const int x = (int)(blockIdx.x * kCgSites + i * kCgThreads + threadIdx.x);
   if (x < V) {
     // FP16 iterations keep the solution increment in FP32: rounding every
     // increment to 11 bits would cost iterations
@@ -120,8 +130,9 @@ __global__ void __launch_bounds__(128) k_cg_update(void *xs, float *xsn, const v
       vx[k].im = qfma(-alpha, vp[k].im, vx[k].im);
       s2 = s2 + vx[k].re * vx[k].re + vx[k].im * vx[k].im;
     }
-    n2 = (double)s2;
+    n2 += (double)s2;
     Spinor<P, R>::store(rs, rsn, stride, x, vx);
+  }
   }
   block_partial(n2, partials);
   cg_last_block(partials, done, s, 1, hist);
@@ -148,12 +159,14 @@ __global__ void __launch_bounds__(128) k_cg_p(void *ps, float *psn, const void *
 // per-block Re <a, b> (used for p^+ A p when the storage rounds D p: with
 // FP16 fields A p = D^+ round(D p), and |D p|^2 would not match it)
 template <int P, typename R>
-__global__ void __launch_bounds__(128) k_dot_re(const void *a, const float *an, const void *b, const float *bn,
-                                                int64_t stride, int V, double *partials, double *s,
-                                                unsigned *done, int hist)
+__global__ void __launch_bounds__(kCgThreads) k_dot_re(const void *a, const float *an, const void *b, const float *bn,
+                                                       int64_t stride, int V, double *partials, double *s,
+                                                       unsigned *done, int hist)
 {
-  int x = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   double d = 0.0;
+#pragma unroll
+  for (int i = 0; i < kCgSpt; i++) {
+  const int x = (int)(blockIdx.x * kCgSites + i * kCgThreads + threadIdx.x);
   if (x < V) {
     C<R> va[12], vb[12];
     Spinor<P, R>::load(a, an, stride, x, va);
@@ -161,7 +174,8 @@ __global__ void __launch_bounds__(128) k_dot_re(const void *a, const float *an, 
     R t = (R)0;
 #pragma unroll
     for (int k = 0; k < 12; k++) t += va[k].re * vb[k].re + va[k].im * vb[k].im;
-    d = (double)t;  // per-site sum in the working precision, block sum in double
+    d += (double)t;  // per-site sum in the working precision, block sum in double
+  }
   }
   block_partial(d, partials);
   cg_last_block(partials, done, s, 0, hist);
@@ -281,7 +295,8 @@ static int cgnr_core(qcdgpu_field y, qcdgpu_field c, double cn, const CgOps &ops
   qcdgpu_field t = w.get(ops.L, prec), aps = w.get(ops.L, prec);
   if (!rt || !r || !up || !rs || !xs || !ps || !t || !aps) return 3;
   const int V = (int)rt->V;
-  const unsigned nb = (unsigned)((V + 127) / 128);
+  const unsigned nb = (unsigned)((V + 127) / 128);            // operator launches: 128 sites per block
+  const unsigned nbr = (unsigned)((V + kCgSites - 1) / kCgSites);  // the fused reductions
   double *part = big_partials(nb);
   double *s = reduce_scratch();
   double *h = host_result();
@@ -343,12 +358,18 @@ static int cgnr_core(qcdgpu_field y, qcdgpu_field c, double cn, const CgOps &ops
       } else {
         if (!ops.op(t, ps, nullptr) || !ops.opdag(aps, t)) return false;
         // p^+ A p and alpha in one launch
-        k_dot_re<QCDGPU_F16, float><<<nb, 128, 0, st>>>(ps->data, ps->norm, aps->data, aps->norm, ps->stride, V, part,
-                                                         s, done, j);
+        k_dot_re<QCDGPU_F16, float><<<nbr, kCgThreads, 0, st>>>(ps->data, ps->norm, aps->data, aps->norm, ps->stride, V,
+                                                                 part, s, done, j);
         if (!QG_LAUNCHED("cg_dot")) return false;
       }
-      QG_PREC_DISPATCH(prec, k_cg_update, xs->data, xs->norm, ps->data, ps->norm, rs->data, rs->norm, aps->data,
-                       aps->norm, xs->stride, V, s, part, done + 1, j);  // with |r|^2 and beta
+#define QG_CG_UPD(P, R)                                                                                           \
+  k_cg_update<P, R><<<nbr, kCgThreads, 0, st>>>(xs->data, xs->norm, ps->data, ps->norm, rs->data, rs->norm, aps->data, \
+                                                aps->norm, xs->stride, V, s, part, done + 1, j)
+      // x += alpha p, r -= alpha A p, with |r|^2 and beta
+      if (prec == QCDGPU_F64) QG_CG_UPD(QCDGPU_F64, double);
+      else if (prec == QCDGPU_F32) QG_CG_UPD(QCDGPU_F32, float);
+      else QG_CG_UPD(QCDGPU_F16, float);
+#undef QG_CG_UPD
       if (!QG_LAUNCHED("cg_update")) return false;
     }
     return true;

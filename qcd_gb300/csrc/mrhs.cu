@@ -254,6 +254,29 @@ __device__ __forceinline__ void mload_rp(const MArgs &a, const __half2 *d, const
   }
 }
 
+// h = upper half of (1 + S g_mu) s for slot r of the multi-RHS spinor at y,
+// projected on packed half pairs (as the single-RHS FP16 kernel does)
+template <int MU, int S>
+__device__ __forceinline__ void mload_project(const __half2 *d, int64_t V, int N, int y, int r, float nrm,
+                                              C<float> h[6])
+{
+  const uint4 *p = (const uint4 *)d;
+  uint4 w[3];
+#pragma unroll
+  for (int j = 0; j < 3; j++) w[j] = p[((int64_t)j * V + y) * N + r];
+  const __half2 *hv = reinterpret_cast<const __half2 *>(w);
+  constexpr bool IM = MU & 1;
+  constexpr int B0 = (MU == 0 || MU == 3) ? 2 : 3, B1 = 5 - B0;
+  constexpr int SG0 = S > 0 ? -1 : 1, SG1 = MU < 2 ? SG0 : -SG0;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const float2 f0 = __half22float2(hcomb<IM>(hv[c], hv[3 * B0 + c], SG0));
+    const float2 f1 = __half22float2(hcomb<IM>(hv[3 + c], hv[3 * B1 + c], SG1));
+    h[c] = C<float>{nrm * f0.x, nrm * f0.y};
+    h[3 + c] = C<float>{nrm * f1.x, nrm * f1.y};
+  }
+}
+
 template <int MU, bool DAG, int RP, bool EO>
 __device__ __forceinline__ void mhop_pair(const MArgs &a, int x, const int c[4], int r0, C<float> acc[RP][12])
 {
@@ -263,17 +286,24 @@ __device__ __forceinline__ void mhop_pair(const MArgs &a, int x, const int c[4],
   for (int dir = 0; dir < 2; dir++) {
     const bool back = dir == 1;
     const int y = back ? bwd(a.geo, x, c, MU) : fwd(a.geo, x, c, MU);
-    C<float> s[RP][12], U[9];
+    C<float> U[9];
+    const int ys = EO ? (y >> 1) : y;
     float nrm[RP];
-    mload_rp<RP>(a, a.in, a.in_norm, EO ? (y >> 1) : y, r0, s, nrm);
+    if (RP == 2) {
+      const float2 n2 = *(const float2 *)(a.in_norm + (int64_t)ys * a.N + r0);
+      nrm[0] = n2.x;
+      nrm[RP - 1] = n2.y;
+    } else {
+      nrm[0] = a.in_norm[(int64_t)ys * a.N + r0];
+    }
     Link<QCDGPU_F32, 18, float>::load(a.gauge, a.gstride, back ? y : x, MU, U);
 #pragma unroll
     for (int q = 0; q < RP; q++) {
       C<float> h[6], uh[6];
-      if (back) project<MU, -SF>(s[q], h);
-      else project<MU, SF>(s[q], h);
-#pragma unroll
-      for (int k = 0; k < 6; k++) h[k] = C<float>{h[k].re * nrm[q], h[k].im * nrm[q]};
+      // the projection adds the stored half pairs, then the six projected
+      // components are converted and scaled by the slot's site norm
+      if (back) mload_project<MU, -SF>(a.in, a.V, a.N, ys, r0 + q, nrm[q], h);
+      else mload_project<MU, SF>(a.in, a.V, a.N, ys, r0 + q, nrm[q], h);
 #pragma unroll
       for (int j = 0; j < 2; j++)
 #pragma unroll
