@@ -172,28 +172,65 @@ __global__ void k_mcopy(MV m, int from, int to, int zero)
 enum { M_RR = 0, M_PAP = 1, M_ALPHA = 2, M_BETA = 3, M_HIST = 4 };
 constexpr int kMChunk = 16;
 
-// block r sums the partials of slot r over nb blocks in a fixed order
-__global__ void k_mscalars(const double *partials, int nb, int N, double *s, int mode, int hist)
+// Per-slot sums of the nb block partials, in two levels: block g of kMSGroups sums a contiguous
+// range of the nb block partials for every slot (consecutive threads read
+// consecutive slots: coalesced), and the block that finishes last sums the
+// kMSGroups group sums per slot, both in a fixed order, and updates the
+// scalars of the nact occupied slots. No block waits for another.
+constexpr int kMSGroups = 128;
+__global__ void __launch_bounds__(256) k_mscalars2(const double *partials, int nb, int N, int nact, double *s,
+                                                   int mode, int hist, double *l1, unsigned *done)
 {
-  const int r = blockIdx.x;
+  const int K = (int)blockDim.x / N;  // thread groups per slot (N <= 64)
+  const int r = (int)threadIdx.x % N, k = (int)threadIdx.x / N;
+  const int per = (nb + (int)gridDim.x - 1) / (int)gridDim.x;
+  const int b0 = (int)blockIdx.x * per, b1 = min(nb, b0 + per);
   double v = 0.0;
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) v += partials[(int64_t)b * N + r];
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  __shared__ double sh[32];
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  if (k < K)
+    for (int b = b0 + k; b < b1; b += K) v += partials[(int64_t)b * N + r];
+  __shared__ double sh[256];
+  __shared__ unsigned last;
+  sh[threadIdx.x] = v;
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if ((int)threadIdx.x < N) {
     double t = 0.0;
-    for (int i = 0; i < (int)(blockDim.x >> 5); i++) t += sh[i];
+    for (int kk = 0; kk < K; kk++) t += sh[kk * N + threadIdx.x];
+    l1[(int64_t)blockIdx.x * N + threadIdx.x] = t;
+  }
+  __threadfence();  // the group sums before the count
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1 ? 1u : 0u;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // slot r's group sums split over the K thread groups, eight loads in flight
+  const int G = (int)gridDim.x;
+  double w = 0.0;
+  if (k < K)
+    for (int g0 = k; g0 < G; g0 += 8 * K) {
+      double q[8];
+#pragma unroll
+      for (int i = 0; i < 8; i++) q[i] = g0 + i * K < G ? __ldcg(l1 + (int64_t)(g0 + i * K) * N + r) : 0.0;
+#pragma unroll
+      for (int i = 0; i < 8; i++) w += q[i];
+    }
+  __syncthreads();
+  sh[threadIdx.x] = w;
+  __syncthreads();
+  if ((int)threadIdx.x < nact) {
+    const int rr = threadIdx.x;
+    double t = 0.0;
+    for (int kk = 0; kk < K; kk++) t += sh[kk * N + rr];
     if (mode == 0) {
-      s[M_PAP * N + r] = t;
-      s[M_ALPHA * N + r] = t > 0.0 ? s[M_RR * N + r] / t : nan("");
+      s[M_PAP * N + rr] = t;
+      s[M_ALPHA * N + rr] = t > 0.0 ? s[M_RR * N + rr] / t : nan("");
     } else {
-      s[M_BETA * N + r] = t / s[M_RR * N + r];
-      s[M_RR * N + r] = t;
-      s[(M_HIST + hist) * N + r] = t;
+      s[M_BETA * N + rr] = t / s[M_RR * N + rr];
+      s[M_RR * N + rr] = t;
+      s[(M_HIST + hist) * N + rr] = t;
     }
   }
+  if (threadIdx.x == 0) *done = 0u;
 }
 
 }  // namespace qg
@@ -235,6 +272,8 @@ struct qcdgpu_batch_s {
   double *s;                   // device scalars, (M_HIST + kMChunk) * cap
   float *mp4s, *tms;           // device per-slot diagonal
   double *part;                // device partials
+  double *l1;                  // group sums of the two-level reduction, kMSGroups * cap
+  unsigned *msdone;            // its block counter
   double *hs;                  // pinned host copy of the scalars
   std::vector<qg::BSlot> slots;
   std::vector<qg::BDone> done;
@@ -266,6 +305,7 @@ static void batch_free(qcdgpu_batch b)
   cudaFree(b->mp4s);
   cudaFree(b->tms);
   cudaFree(b->part);
+  cudaFree(b->l1);
   cudaFreeHost(b->hs);
   for (auto e : b->graphs)
     if (e) cudaGraphExecDestroy(e);
@@ -324,10 +364,14 @@ static qcdgpu_batch batch_new(qcdgpu_gauge g, int cap, bool eo)
             QG_CUDA(cudaMalloc(&b->s, ns * sizeof(double))) && QG_CUDA(cudaMalloc(&b->mp4s, cap * sizeof(float))) &&
             QG_CUDA(cudaMalloc(&b->tms, cap * sizeof(float))) &&
             QG_CUDA(cudaMalloc(&b->part, (size_t)nb * cap * sizeof(double))) &&
+            QG_CUDA(cudaMalloc(&b->l1, (size_t)kMSGroups * cap * sizeof(double) + 256)) &&
             QG_CUDA(cudaMallocHost(&b->hs, ns * sizeof(double))) &&
             QG_CUDA(cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming)) &&
             QG_CUDA(cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming)) &&
             QG_CUDA(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
+  // the reduction's counter starts at zero, on the batch's own stream
+  ok = ok && QG_CUDA(cudaMemsetAsync(b->l1, 0, (size_t)kMSGroups * cap * sizeof(double) + 256, b->st));
+  if (ok) b->msdone = (unsigned *)(b->l1 + (size_t)kMSGroups * cap);
   if (!ok) {
     batch_free(b);
     return nullptr;
@@ -528,7 +572,7 @@ static bool chunk_enqueue(qcdgpu_batch B, int n)
     } else if (!dslash_mrhs(B->t, B->ps, B->g, 4.0, 0.0, false, n, B->mp4s, B->tms, B->part, &nbo)) {
       return false;
     }
-    k_mscalars<<<n, 256, 0, st>>>(B->part, (int)nbo, cap, B->s, 0, j);
+    k_mscalars2<<<kMSGroups, 256, 0, st>>>(B->part, (int)nbo, cap, n, B->s, 0, j, B->l1, B->msdone);
     if (!QG_LAUNCHED("mrhs_scalars")) return false;
     if (B->eo) {
       if (!dslash_mrhs_eo(B->u, B->t, nullptr, B->g, true, n, B->mp4s, B->tms, 1, 1.0, true, 0, nullptr, nullptr) ||
@@ -539,7 +583,7 @@ static bool chunk_enqueue(qcdgpu_batch B, int n)
     }
     k_mupdate<<<nb, blk, shm, st>>>(mx(B), mv(B->ps), mv(B->rs), mv(B->aps), n, B->s + M_ALPHA * cap, B->part);
     if (!QG_LAUNCHED("mrhs_update")) return false;
-    k_mscalars<<<n, 256, 0, st>>>(B->part, (int)nb, cap, B->s, 1, j);
+    k_mscalars2<<<kMSGroups, 256, 0, st>>>(B->part, (int)nb, cap, n, B->s, 1, j, B->l1, B->msdone);
     if (!QG_LAUNCHED("mrhs_scalars")) return false;
   }
   return QG_CUDA(cudaMemcpyAsync(B->hs, B->s, sizeof(double) * (M_HIST + kMChunk) * cap, cudaMemcpyDeviceToHost, st));
