@@ -473,8 +473,11 @@ int qcdgpu_server_add_gauge(qcdgpu_server s, qcdgpu_gauge g);
  * Returns 0, or 1 on error. */
 int qcdgpu_server_submit(qcdgpu_server s, int gauge_id, int nrhs, const qcdgpu_field *sources, uint64_t seed,
                          double kappa, double mu, int op, double tol, int maxiter, int tag);
-/* one scheduling round: admission, slot filling, one chunk of iterations
- * on every busy batch, retirement. Returns 0, or 3 on a CUDA error. */
+/* one scheduling step: admission, slot filling; batches (one per gauge
+ * field, each on its own stream) run chunks of iterations independently:
+ * idle batches with work start a chunk, and the call returns once at least
+ * one running chunk has ended (its batch then finished, refilled and
+ * relaunched) or at once if none runs. Returns 0, or 3 on a CUDA error. */
 int qcdgpu_server_progress(qcdgpu_server s);
 /* completed requests, oldest first; returns the count */
 int qcdgpu_server_poll(qcdgpu_server s, qcdgpu_server_result *out, int max);

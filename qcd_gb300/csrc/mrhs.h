@@ -90,5 +90,10 @@ namespace qg {
 // wait for it and apply reliable updates / retirement
 bool batch_launch(qcdgpu_batch B);
 bool batch_finish(qcdgpu_batch B);
+// a chunk is launched and not yet finished
+bool batch_in_flight(qcdgpu_batch B);
+// the launched chunk's work has completed on the device (batch_finish will
+// not wait)
+bool batch_chunk_done(qcdgpu_batch B);
 
 }  // namespace qg

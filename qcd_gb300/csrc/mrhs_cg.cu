@@ -275,6 +275,7 @@ struct qcdgpu_batch_s {
   double *l1;                  // group sums of the two-level reduction, kMSGroups * cap
   unsigned *msdone;            // its block counter
   double *hs;                  // pinned host copy of the scalars
+  double *rudev, *ruhost;      // reliable updates' norms, 4 per slot (device, pinned host)
   std::vector<qg::BSlot> slots;
   std::vector<qg::BDone> done;
   cudaStream_t st;             // the stream the batch's work runs on
@@ -294,6 +295,7 @@ static MX mx(qcdgpu_batch B) { return MX{B->xs, (int)B->Vs, B->cap}; }
 static void batch_free(qcdgpu_batch b)
 {
   if (!b) return;
+  if (b->st) cudaStreamSynchronize(b->st);  // a chunk may still be running
   for (auto m : {b->rs, b->ps, b->t, b->aps, b->u}) mfield_free(m);
   cudaFree(b->xs);
   for (auto f : {b->rt, b->r, b->up, b->bd, b->u64, b->r32, b->u32, b->s32}) field_free(f);
@@ -306,6 +308,8 @@ static void batch_free(qcdgpu_batch b)
   cudaFree(b->tms);
   cudaFree(b->part);
   cudaFree(b->l1);
+  cudaFree(b->rudev);
+  cudaFreeHost(b->ruhost);
   cudaFreeHost(b->hs);
   for (auto e : b->graphs)
     if (e) cudaGraphExecDestroy(e);
@@ -365,6 +369,8 @@ static qcdgpu_batch batch_new(qcdgpu_gauge g, int cap, bool eo)
             QG_CUDA(cudaMalloc(&b->tms, cap * sizeof(float))) &&
             QG_CUDA(cudaMalloc(&b->part, (size_t)nb * cap * sizeof(double))) &&
             QG_CUDA(cudaMalloc(&b->l1, (size_t)kMSGroups * cap * sizeof(double) + 256)) &&
+            QG_CUDA(cudaMalloc(&b->rudev, (size_t)4 * cap * sizeof(double))) &&
+            QG_CUDA(cudaMallocHost(&b->ruhost, (size_t)4 * cap * sizeof(double))) &&
             QG_CUDA(cudaMallocHost(&b->hs, ns * sizeof(double))) &&
             QG_CUDA(cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming)) &&
             QG_CUDA(cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming)) &&
@@ -386,34 +392,42 @@ static bool slot_bd(qcdgpu_batch B, const BSlot &sl)
   return blas_copy(B->bd, sl.b);
 }
 
-// rt = bd - D x (FP64), r = D^+ rt; slot k of rs <- r; returns |rt| / |b| and |r|^2.
+// rt = bd - D x (FP64), r = D^+ rt; slot k of rs <- r. |rt|^2 and |r|^2 are
+// left on the device at res[0] and res[2]: the residuals of all updating
+// slots are enqueued back to back and read with one synchronisation.
 // Even/odd: rt = c_e - M x_e in FP64 (equal to the full residual), and the
 // restart residual M^+ rt in FP32 (it only seeds the FP16 iteration).
-static bool slot_residual(qcdgpu_batch B, int k, const BSlot &sl, double *rel, double *rr)
+static bool slot_residual(qcdgpu_batch B, int k, const BSlot &sl, double *res)
 {
   if (B->eo) {
     qcdgpu_gauge g32 = gauge_at(B->g, QCDGPU_F32);
-    double n2;
     const int ar = QCDGPU_ARITH_DF64;
-    if (!g32 || !dslash_eo(B->u64, sl.xe, nullptr, B->g, sl.mp4, sl.tm, false, 1, 1.0, true, 0, nullptr, ar) ||
-        !dslash_eo(B->rt, B->u64, sl.xe, B->g, sl.mp4, sl.tm, false, 0, -0.25, false, 2, nullptr, ar) ||
-        !blas_axpby(B->rt, 1.0, 0.0, sl.ce, -1.0, 0.0, B->rt) || !blas_norm2(B->rt, &n2))
-      return false;
-    *rel = sl.bn > 0 ? sqrt(n2) / sl.bn : 0.0;
-    return convert_field(B->r32, B->rt) &&
+    return g32 && dslash_eo(B->u64, sl.xe, nullptr, B->g, sl.mp4, sl.tm, false, 1, 1.0, true, 0, nullptr, ar) &&
+           dslash_eo(B->rt, B->u64, sl.xe, B->g, sl.mp4, sl.tm, false, 0, -0.25, false, 2, nullptr, ar) &&
+           blas_axpby(B->rt, 1.0, 0.0, sl.ce, -1.0, 0.0, B->rt) && blas_norm2_dev(B->rt, res) &&
+           convert_field(B->r32, B->rt) &&
            dslash_eo(B->u32, B->r32, nullptr, g32, sl.mp4, sl.tm, true, 1, 1.0, true, 0, nullptr) &&
            dslash_eo(B->s32, B->u32, B->r32, g32, sl.mp4, sl.tm, true, 0, -0.25, false, 2, nullptr) &&
-           blas_norm2(B->s32, rr) && mfield_set(B->rs, k, B->s32);
+           blas_norm2_dev(B->s32, res + 2) && mfield_set(B->rs, k, B->s32);
   }
-  if (!slot_bd(B, sl)) return false;
-  if (!dslash(B->rt, sl.x, B->g, sl.mp4, sl.tm, QCDGPU_OP_D, QCDGPU_ARITH_DF64)) return false;
-  if (!blas_axpby(B->rt, 1.0, 0.0, B->bd, -1.0, 0.0, B->rt)) return false;
-  double n2;
-  if (!blas_norm2(B->rt, &n2)) return false;
-  *rel = sl.bn > 0 ? sqrt(n2) / sl.bn : 0.0;
-  if (!dslash(B->r, B->rt, B->g, sl.mp4, sl.tm, QCDGPU_OP_DDAG, QCDGPU_ARITH_DF64)) return false;
-  if (!blas_norm2(B->r, rr)) return false;
-  return mfield_set(B->rs, k, B->r);
+  return slot_bd(B, sl) && dslash(B->rt, sl.x, B->g, sl.mp4, sl.tm, QCDGPU_OP_D, QCDGPU_ARITH_DF64) &&
+         blas_axpby(B->rt, 1.0, 0.0, B->bd, -1.0, 0.0, B->rt) && blas_norm2_dev(B->rt, res) &&
+         dslash(B->r, B->rt, B->g, sl.mp4, sl.tm, QCDGPU_OP_DDAG, QCDGPU_ARITH_DF64) &&
+         blas_norm2_dev(B->r, res + 2) && mfield_set(B->rs, k, B->r);
+}
+
+// rr and beta of up to 64 slots after their reliable updates, in one launch
+struct SlotRestart {
+  int n;
+  int slot[64];
+  double rr[64], beta[64];
+};
+__global__ void k_set_restart(double *s, int cap, SlotRestart r)
+{
+  const int i = threadIdx.x;
+  if (i >= r.n) return;
+  s[M_RR * cap + r.slot[i]] = r.rr[i];
+  s[M_BETA * cap + r.slot[i]] = r.beta[i];
 }
 
 static bool set_scalar(qcdgpu_batch B, int slot_kind, int k, double v)
@@ -483,14 +497,17 @@ int batch_add(qcdgpu_batch B, qcdgpu_field x, qcdgpu_field b, double kappa, doub
       return -2;
     }
   }
-  double rel, rr;
   auto give_back = [&]() {
     if (B->eo) B->spare.push_back({sl.ce, sl.to, sl.xe});
   };
-  if (!slot_residual(B, k, sl, &rel, &rr)) {
+  if (!slot_residual(B, k, sl, B->rudev + 4 * k) ||
+      !QG_CUDA(cudaMemcpyAsync(B->ruhost + 4 * k, B->rudev + 4 * k, sizeof(double) * 4, cudaMemcpyDeviceToHost,
+                               stream())) ||
+      !QG_CUDA(cudaStreamSynchronize(stream()))) {
     give_back();
     return -2;
   }
+  const double rel = sl.bn > 0 ? sqrt(B->ruhost[4 * k]) / sl.bn : 0.0, rr = B->ruhost[4 * k + 2];
   sl.true_res = rel;
   sl.maxr = sqrt(rr);
   sl.hint = tol * sl.maxr;
@@ -636,6 +653,19 @@ bool batch_launch(qcdgpu_batch B)
   return QG_CUDA(cudaEventRecord(B->ev, B->st));
 }
 
+bool batch_in_flight(qcdgpu_batch B) { return B->nchunk > 0; }
+
+bool batch_chunk_done(qcdgpu_batch B)
+{
+  if (B->nchunk == 0) return true;
+  const cudaError_t e = cudaEventQuery(B->ev);
+  if (e == cudaErrorNotReady) {
+    if (cudaPeekAtLastError() == cudaErrorNotReady) cudaGetLastError();  // not an error
+    return false;
+  }
+  return true;  // done, or an error that batch_finish reports
+}
+
 // Wait for the launched chunk, then reliable updates and retirement
 bool batch_finish(qcdgpu_batch B)
 {
@@ -668,28 +698,49 @@ bool batch_finish(qcdgpu_batch B)
     need[k] = fail[k] || update || hinted || sl.iters >= sl.maxiter;
     if (hinted) sl.hint *= 0.3;
   }
-  // reliable updates, then retirement from the highest slot down
-  std::vector<int> retire_status(n, -1);
+  // reliable updates: every updating slot's FP64 residual and restart are
+  // enqueued back to back, their norms read with one synchronisation, and
+  // the continuing slots' rr and beta written with one launch; then
+  // retirement from the highest slot down
+  std::vector<int> retire_status(n, -1), upd;
   for (int k = 0; k < n; k++) {
     if (!need[k]) continue;
     BSlot &sl = B->slots[(size_t)k];
     qcdgpu_field acc = B->eo ? sl.xe : sl.x;  // the slot's FP64 solution
     k_mx_flush<<<(unsigned)((V + 127) / 128), 128, 0, st>>>((double2 *)acc->data, acc->stride, mx(B), k);
     if (!QG_LAUNCHED("mrhs_flush_slot")) return false;
-    double rel, rr;
-    if (!slot_residual(B, k, sl, &rel, &rr)) return false;
-    sl.true_res = rel;
-    sl.updates++;
-    if (rel <= sl.tol) {
-      retire_status[k] = 0;
-    } else if (fail[k]) {
-      retire_status[k] = 2;
-    } else if (sl.iters >= sl.maxiter) {
-      retire_status[k] = 1;
-    } else {
-      double bnew = (beta_iter[k] > 0.0 && rr_iter[k] > 0.0) ? rr * beta_iter[k] / rr_iter[k] : 0.0;
-      if (!set_scalar(B, M_RR, k, rr) || !set_scalar(B, M_BETA, k, bnew)) return false;
-      sl.maxr = sqrt(rr);
+    if (!slot_residual(B, k, sl, B->rudev + 4 * k)) return false;
+    upd.push_back(k);
+  }
+  if (!upd.empty()) {
+    if (!QG_CUDA(cudaMemcpyAsync(B->ruhost, B->rudev, sizeof(double) * 4 * (size_t)n, cudaMemcpyDeviceToHost, st)) ||
+        !QG_CUDA(cudaStreamSynchronize(st)))
+      return false;
+    SlotRestart rs;
+    rs.n = 0;
+    for (int k : upd) {
+      BSlot &sl = B->slots[(size_t)k];
+      const double n2 = B->ruhost[4 * k], rr = B->ruhost[4 * k + 2];
+      const double rel = sl.bn > 0 ? sqrt(n2) / sl.bn : 0.0;
+      sl.true_res = rel;
+      sl.updates++;
+      if (rel <= sl.tol) {
+        retire_status[k] = 0;
+      } else if (fail[k]) {
+        retire_status[k] = 2;
+      } else if (sl.iters >= sl.maxiter) {
+        retire_status[k] = 1;
+      } else {
+        rs.slot[rs.n] = k;
+        rs.rr[rs.n] = rr;
+        rs.beta[rs.n] = (beta_iter[k] > 0.0 && rr_iter[k] > 0.0) ? rr * beta_iter[k] / rr_iter[k] : 0.0;
+        rs.n++;
+        sl.maxr = sqrt(rr);
+      }
+    }
+    if (rs.n > 0) {
+      k_set_restart<<<1, 64, 0, st>>>(B->s, cap, rs);
+      if (!QG_LAUNCHED("mrhs_set_restart")) return false;
     }
   }
   for (int k = n - 1; k >= 0; k--)

@@ -19,6 +19,8 @@
 #include <map>
 #include <vector>
 
+#include <thread>
+
 #include "mrhs.h"
 
 namespace qg {
@@ -172,6 +174,24 @@ static void collect(qcdgpu_server S, SrvGauge &G)
   }
 }
 
+// free slots of G's batch <- right-hand sides of its admitted requests, in
+// arrival order; then collect what was solved at admission
+static bool fill_slots(qcdgpu_server S, SrvGauge &G)
+{
+  while (G.batch && !G.pending.empty() && qcdgpu_batch_free_slots(G.batch) > 0) {
+    const int id = S->by_tag[G.pending.front()];
+    SrvRequest &r = S->reqs[id];
+    const int c = r.next_col;
+    int k = qcdgpu_batch_add(G.batch, r.x[(size_t)c], r.b[(size_t)c], r.kappa, r.mu, r.op, r.tol, r.maxiter, 0.1,
+                             id * 64 + c);
+    if (k == -2) return false;
+    if (k == -1) break;
+    if (++r.next_col == r.nrhs) G.pending.pop_front();
+  }
+  if (G.batch) collect(S, G);  // right-hand sides solved at admission
+  return true;
+}
+
 int progress(qcdgpu_server S)
 {
   // 1. admission in arrival order
@@ -197,31 +217,37 @@ int progress(qcdgpu_server S)
     }
     S->queue.pop_front();
   }
-  // 2. slot filling
+  // 2. slot filling (batches with a chunk running are filled when it ends)
   for (SrvGauge &G : S->gauges) {
-    while (G.batch && !G.pending.empty() && qcdgpu_batch_free_slots(G.batch) > 0) {
-      const int id = S->by_tag[G.pending.front()];
-      SrvRequest &r = S->reqs[id];
-      const int c = r.next_col;
-      int k = qcdgpu_batch_add(G.batch, r.x[(size_t)c], r.b[(size_t)c], r.kappa, r.mu, r.op, r.tol, r.maxiter, 0.1,
-                               id * 64 + c);
-      if (k == -2) return 3;
-      if (k == -1) break;
-      if (++r.next_col == r.nrhs) G.pending.pop_front();
-    }
-    if (G.batch) collect(S, G);  // right-hand sides solved at admission
+    if (!G.batch || batch_in_flight(G.batch)) continue;
+    if (!fill_slots(S, G)) return 3;
   }
-  // 3. one chunk on every busy batch: launch all, then finish each
-  std::vector<SrvGauge *> busy;
+  // 3. every batch runs on its own stream, independently of the others:
+  // an idle batch with work starts a chunk; a batch whose chunk has ended is
+  // finished (reliable updates, retirement), refilled and relaunched at
+  // once. The call returns when at least one chunk has ended, or at once if
+  // none is running, so small lattices' batches are not held to the pace of
+  // a large one's chunks.
   for (SrvGauge &G : S->gauges)
-    if (G.batch && qcdgpu_batch_active(G.batch) > 0) busy.push_back(&G);
-  for (SrvGauge *G : busy)
-    if (!batch_launch(G->batch)) return 3;
-  for (SrvGauge *G : busy) {
-    if (!batch_finish(G->batch)) return 3;
-    collect(S, *G);
+    if (G.batch && !batch_in_flight(G.batch) && qcdgpu_batch_active(G.batch) > 0 && !batch_launch(G.batch))
+      return 3;
+  for (;;) {
+    bool running = false, ended = false;
+    for (SrvGauge &G : S->gauges) {
+      if (!G.batch || !batch_in_flight(G.batch)) continue;
+      if (!batch_chunk_done(G.batch)) {
+        running = true;
+        continue;
+      }
+      if (!batch_finish(G.batch)) return 3;
+      collect(S, G);
+      ended = true;
+      if (!fill_slots(S, G)) return 3;
+      if (qcdgpu_batch_active(G.batch) > 0 && !batch_launch(G.batch)) return 3;
+    }
+    if (ended || !running) return 0;
+    std::this_thread::sleep_for(std::chrono::microseconds(20));
   }
-  return 0;
 }
 
 }  // namespace qg
