@@ -404,16 +404,18 @@ __global__ void __launch_bounds__(256) k_wilson_mrhs_simt(const MArgs a, double 
     }
   }
   if (partials) {
+    // the block covers slots 0 .. NS-1 (the occupied ones); partials keep
+    // the field's slot stride N
     extern __shared__ double sh[];
-    const int N = a.N, y = threadIdx.y;
+    const int N = a.N, y = threadIdx.y, NS = min(N, (int)blockDim.x * RP);
 #pragma unroll
     for (int q = 0; q < RP; q++)
-      if (threadIdx.x * RP + q < N) sh[y * N + threadIdx.x * RP + q] = n2[q];
+      if (threadIdx.x * RP + q < NS) sh[y * NS + threadIdx.x * RP + q] = n2[q];
     __syncthreads();
-    for (int r = threadIdx.x; r < N; r += blockDim.x)
+    for (int r = threadIdx.x; r < NS; r += blockDim.x)
       if (y == 0) {
         double t = 0.0;
-        for (int i = 0; i < (int)blockDim.y; i++) t += sh[i * N + r];
+        for (int i = 0; i < (int)blockDim.y; i++) t += sh[i * NS + r];
         partials[(int64_t)blockIdx.x * N + r] = t;
       }
   }
@@ -574,11 +576,14 @@ static bool launch_mrhs(const MArgs &a, bool dag, MrhsTune t, double *partials, 
 {
   cudaStream_t s = stream();
   const bool simt = t.variant == MRHS_SIMT;
-  const dim3 blk = simt_block(a.N, simt ? t.threads : 256, simt ? t.rp : 1);
+  // threads for the occupied slots only (the tuned block size holds more
+  // sites when fewer slots are occupied)
+  const dim3 blk = simt_block(simt ? a.nact : a.N, simt ? t.threads : 256, simt ? t.rp : 1);
   const unsigned nb = (unsigned)((a.V + blk.y - 1) / blk.y);
   const size_t shm = sizeof(double) * a.N * blk.y;
   if (simt) {
-    const size_t sm = partials ? shm : 0;
+    const int ns = (int)blk.x * t.rp < a.N ? (int)blk.x * t.rp : a.N;
+    const size_t sm = partials ? sizeof(double) * ns * blk.y : 0;
     // kernel mode from the epilogue (see k_wilson_mrhs_simt)
     const int mode = a.eo_par < 0 ? 0 : a.ainv ? 1 : 2;
 #define QG_SIMT(RP, MODE)                                                           \

@@ -61,15 +61,16 @@ __device__ __forceinline__ void mv_store(const MV &m, int x, int r, const float2
 static dim3 mblock(int N) { return dim3((unsigned)N, (unsigned)(256 / N > 0 ? 256 / N : 1)); }
 static unsigned mgrid(int V, int N) { return (unsigned)((V + mblock(N).y - 1) / mblock(N).y); }
 
-__device__ __forceinline__ void slot_partial(double v, double *partials)
+// block partials of the blockDim.x occupied slots, at slot stride N
+__device__ __forceinline__ void slot_partial(double v, double *partials, int N)
 {
   extern __shared__ double sh[];
-  const int N = blockDim.x, r = threadIdx.x, y = threadIdx.y;
-  sh[y * N + r] = v;
+  const int NS = blockDim.x, r = threadIdx.x, y = threadIdx.y;
+  sh[y * NS + r] = v;
   __syncthreads();
   if (y == 0) {
     double s = 0.0;
-    for (int i = 0; i < (int)blockDim.y; i++) s += sh[i * N + r];
+    for (int i = 0; i < (int)blockDim.y; i++) s += sh[i * NS + r];
     partials[(int64_t)blockIdx.x * N + r] = s;
   }
 }
@@ -109,7 +110,7 @@ __global__ void k_mupdate(MX xs, MV ps, MV rs, MV aps, int nact, const double *a
     mv_store(rs, x, r, a);
     n2 = (double)s2;
   }
-  slot_partial(n2, partials);
+  slot_partial(n2, partials, xs.N);
 }
 
 // f (FP64 field) += slot r of xs, then slot r of xs <- 0
@@ -570,8 +571,8 @@ static bool chunk_enqueue(qcdgpu_batch B, int n)
 {
   const int cap = B->cap;
   const int V = (int)B->Vs;
-  const dim3 blk = mblock(cap);
-  const unsigned nb = mgrid(V, cap);
+  const dim3 blk = mblock(n);  // threads for the n occupied slots
+  const unsigned nb = mgrid(V, n);
   const size_t shm = sizeof(double) * blk.x * blk.y;
   cudaStream_t st = stream();
   for (int j = 0; j < kMChunk; j++) {

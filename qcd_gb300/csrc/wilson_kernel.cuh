@@ -187,7 +187,6 @@ __global__ void __launch_bounds__(128) k_wilson(const DArgs a)
     }
     Spinor<SP, R>::store(a.out, a.out_norm, a.stride, x, acc);
     if (a.partials) {
-#pragma unroll
       // per-site sum in the working precision (FP64 arithmetic is scarce on
       // this part); the block sum is double
       R s2 = acc[0].re * acc[0].re + acc[0].im * acc[0].im;
