@@ -146,6 +146,38 @@ __device__ __forceinline__ void acc_add(FA &acc, F2 x)
   acc.s = s;
 }
 
+// acc = a * b into an empty accumulator: no error-free sum needed
+__device__ __forceinline__ FA mac0(F2 a, F2 b)
+{
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  return FA{p, __fmaf_rn(a.l, b.h, e)};
+}
+// acc += x for an unnormalised x
+__device__ __forceinline__ void acc_add_fa(FA &acc, FA x)
+{
+  float s, q;
+  two_sum(acc.s, x.s, s, q);
+  acc.e = __fadd_rn(acc.e, __fadd_rn(q, x.e));
+  acc.s = s;
+}
+__device__ __forceinline__ FA fneg(FA a) { return FA{-a.s, -a.e}; }
+struct CFA {  // complex accumulator value
+  FA re, im;
+};
+// z -> (i z if ifl) then negated if ng
+__device__ __forceinline__ CFA coefa(CFA z, bool ifl, bool ng)
+{
+  CFA r = ifl ? CFA{fneg(z.im), z.re} : z;
+  return ng ? CFA{fneg(r.re), fneg(r.im)} : r;
+}
+__device__ __forceinline__ void cacc_fa(CA &acc, CFA x)
+{
+  acc_add_fa(acc.re, x.re);
+  acc_add_fa(acc.im, x.im);
+}
+
 __device__ __forceinline__ CF cadd(CF a, CF b) { return CF{add(a.re, b.re), add(a.im, b.im)}; }
 __device__ __forceinline__ CF cneg(CF a) { return CF{neg(a.re), neg(a.im)}; }
 __device__ __forceinline__ CF ci(CF a) { return CF{neg(a.im), a.re}; }  // i a
@@ -316,29 +348,46 @@ __device__ __forceinline__ double group_ff(const DArgs &a, int grp, int col, int
     hs[grp][0][col][lane] = CF{split_d(d0.x), split_d(d0.y)};
     hs[grp][1][col][lane] = CF{split_d(d1.x), split_d(d1.y)};
     group_bar(grp);
-    CA u0 = {{0.f, 0.f}, {0.f, 0.f}}, u1 = u0;
+    CA u0, u1;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       CF g0 = hs[grp][0][k][lane], g1 = hs[grp][1][k][lane];
       // forward: U[col][k]; backward: conj(U[k][col])
       CF wl = act ? load_link(gf, a.gstride, ly, mu, back ? 3 * k + col : 3 * col + k) : CF{{0.f, 0.f}, {0.f, 0.f}};
       F2 wr = wl.re, wi = back ? neg(wl.im) : wl.im, mwi = neg(wi);
-      mac(u0.re, wr, g0.re);
+      if (k == 0) {
+        u0.re = mac0(wr, g0.re);
+        u0.im = mac0(wr, g0.im);
+        u1.re = mac0(wr, g1.re);
+        u1.im = mac0(wr, g1.im);
+      } else {
+        mac(u0.re, wr, g0.re);
+        mac(u0.im, wr, g0.im);
+        mac(u1.re, wr, g1.re);
+        mac(u1.im, wr, g1.im);
+      }
       mac(u0.re, mwi, g0.im);
-      mac(u0.im, wr, g0.im);
       mac(u0.im, wi, g0.re);
-      mac(u1.re, wr, g1.re);
       mac(u1.re, mwi, g1.im);
-      mac(u1.im, wr, g1.im);
       mac(u1.im, wi, g1.re);
     }
-    const CF v0{fin(u0.re), fin(u0.im)}, v1{fin(u1.re), fin(u1.im)};
+    // the products enter the spinor accumulators unnormalised (the first
+    // hop assigns them)
+    const CFA v0{u0.re, u0.im}, v1{u1.re, u1.im};
     const bool jA = (mu == 1 || mu == 2);
     const bool negA = mu == 0 ? S > 0 : S < 0, negB = mu == 1 ? S < 0 : S > 0;
-    cacc(acc[0], v0);
-    cacc(acc[1], v1);
-    cacc(acc[2], coef(jA ? v1 : v0, odd, negA));
-    cacc(acc[3], coef(jA ? v0 : v1, odd, negB));
+    const CFA l2 = coefa(jA ? v1 : v0, odd, negA), l3 = coefa(jA ? v0 : v1, odd, negB);
+    if (d == 0) {
+      acc[0] = CA{v0.re, v0.im};
+      acc[1] = CA{v1.re, v1.im};
+      acc[2] = CA{l2.re, l2.im};
+      acc[3] = CA{l3.re, l3.im};
+    } else {
+      cacc_fa(acc[0], v0);
+      cacc_fa(acc[1], v1);
+      cacc_fa(acc[2], l2);
+      cacc_fa(acc[3], l3);
+    }
     group_bar(grp);  // hs is rewritten by the next hop
   }
   if (!act) return 0.0;
