@@ -577,8 +577,10 @@ static bool launch_mrhs(const MArgs &a, bool dag, MrhsTune t, double *partials, 
   cudaStream_t s = stream();
   const bool simt = t.variant == MRHS_SIMT;
   // threads for the occupied slots only (the tuned block size holds more
-  // sites when fewer slots are occupied)
-  const dim3 blk = simt_block(simt ? a.nact : a.N, simt ? t.threads : 256, simt ? t.rp : 1);
+  // sites when fewer slots are occupied), except when the launch writes
+  // per-slot partial sums: their grouping into blocks, and so their summation
+  // order, must not depend on which other slots are occupied
+  const dim3 blk = simt_block(simt && !partials ? a.nact : a.N, simt ? t.threads : 256, simt ? t.rp : 1);
   const unsigned nb = (unsigned)((a.V + blk.y - 1) / blk.y);
   const size_t shm = sizeof(double) * a.N * blk.y;
   if (simt) {

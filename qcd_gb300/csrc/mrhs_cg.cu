@@ -571,13 +571,16 @@ static bool chunk_enqueue(qcdgpu_batch B, int n)
 {
   const int cap = B->cap;
   const int V = (int)B->Vs;
-  const dim3 blk = mblock(n);  // threads for the n occupied slots
-  const unsigned nb = mgrid(V, n);
+  // the update writes per-slot partial sums: its block shape follows the
+  // capacity, so their summation order does not depend on the mix; the
+  // direction update uses threads for the n occupied slots only
+  const dim3 blk = mblock(cap), blkp = mblock(n);
+  const unsigned nb = mgrid(V, cap), nbp = mgrid(V, n);
   const size_t shm = sizeof(double) * blk.x * blk.y;
   cudaStream_t st = stream();
   for (int j = 0; j < kMChunk; j++) {
     // p = r + beta p (beta = 0 keeps a fresh slot's p = r)
-    k_mp<<<nb, blk, 0, st>>>(mv(B->ps), mv(B->rs), n, B->s + M_BETA * cap);
+    k_mp<<<nbp, blkp, 0, st>>>(mv(B->ps), mv(B->rs), n, B->s + M_BETA * cap);
     if (!QG_LAUNCHED("mrhs_p")) return false;
     // p^+ A^+ A p = |A p|^2, summed per slot in the epilogue of t = A p
     // (A = D, or the Schur complement M = A_ee - H_eo A_oo^{-1} H_oe / 4 as
