@@ -168,16 +168,18 @@ static bool check_op_args(qcd_vector *Dv, qcd_vector *v, qcd_gaugeField *u)
 // Pipelined apply for page-locked host vectors: the lattice is cut into S
 // slabs of whole z-planes (up to 24). Each stage runs on its own stream,
 // chained per slab by events, so the copy engines stream their slabs back
-// to back: c_in copies slab k in, s_in reorders it to the field layout, the
-// operator runs as soon as slabs k-1..k+1 are in (consecutive slabs
-// alternating between the library stream and op2, so thin slabs share the
-// GPU), s_out reorders the result and c_out copies it out. Slabs 0 and S-1
-// need each other (periodic z), so the order of application is
-// 1 .. S-2, S-1, 0. The host link bounds it: 254 MB per 24^3x48 apply at
-// the 340 GB/s both directions reach together is 0.75 ms.
-static cudaStream_t g_c_in, g_s_in, g_s_out, g_c_out, g_s_op2;
+// to back: c_in copies slab k in, the operator runs as soon as slabs
+// k-1..k+1 are in (consecutive slabs rotating over three streams, so thin
+// slabs share the GPU) and c_out copies the result out. With float-float
+// arithmetic the operator reads and writes the host layout in the staging
+// buffers directly; with native FP64 s_in reorders each slab to the field
+// layout first and s_out reorders the result back. Slabs 0 and S-1 need
+// each other (periodic z), so the order of application is 1 .. S-2, S-1, 0.
+// The host link bounds it: 254 MB per 24^3x48 apply at the 340 GB/s both
+// directions reach together is 0.75 ms.
+static cudaStream_t g_c_in, g_s_in, g_s_out, g_c_out, g_s_op2, g_s_op3;
 static std::vector<cudaEvent_t> g_ev_cin, g_ev_in, g_ev_op, g_ev_rout;
-static cudaEvent_t g_ev_start, g_ev_done, g_ev_op2;
+static cudaEvent_t g_ev_start, g_ev_done, g_ev_op2, g_ev_op3;
 static void *g_stage_in, *g_stage_out;  // device copies of the host layout
 static size_t g_stage_bytes;
 
@@ -194,11 +196,12 @@ static int pipeline_slabs(const qcdgpu_field f)
 static bool pipeline_ready(int S)
 {
   if (!g_s_in) {
-    for (cudaStream_t *q : {&g_c_in, &g_s_in, &g_s_out, &g_c_out, &g_s_op2})
+    for (cudaStream_t *q : {&g_c_in, &g_s_in, &g_s_out, &g_c_out, &g_s_op2, &g_s_op3})
       if (!QG_CUDA(cudaStreamCreateWithFlags(q, cudaStreamNonBlocking))) return false;
     if (!QG_CUDA(cudaEventCreateWithFlags(&g_ev_start, cudaEventDisableTiming)) ||
         !QG_CUDA(cudaEventCreateWithFlags(&g_ev_done, cudaEventDisableTiming)) ||
-        !QG_CUDA(cudaEventCreateWithFlags(&g_ev_op2, cudaEventDisableTiming)))
+        !QG_CUDA(cudaEventCreateWithFlags(&g_ev_op2, cudaEventDisableTiming)) ||
+        !QG_CUDA(cudaEventCreateWithFlags(&g_ev_op3, cudaEventDisableTiming)))
       return false;
   }
   while ((int)g_ev_in.size() < S) {
@@ -219,56 +222,70 @@ static bool enqueue_pipeline(cudaStream_t origin, qcdgpu_field out, qcdgpu_field
 {
   const int64_t V = in->V, slab = V / S;
   const size_t sbytes = (size_t)V * 24 * sizeof(double) / S;
+  const bool direct = g_f64_arith == QCDGPU_ARITH_DF64;
+  // the event that marks slab k as readable by the operator
+  const std::vector<cudaEvent_t> &ready = direct ? g_ev_cin : g_ev_in;
   if (!QG_CUDA(cudaEventRecord(g_ev_start, origin))) return false;
-  for (cudaStream_t q : {g_c_in, g_s_in, g_s_out, g_c_out, g_s_op2})
+  for (cudaStream_t q : {g_c_in, g_s_in, g_s_out, g_c_out, g_s_op2, g_s_op3})
     if (!QG_CUDA(cudaStreamWaitEvent(q, g_ev_start, 0))) return false;
-  // host -> device copies, back to back
-  for (int k = 0; k < S; k++)
+  // The stages are enqueued slab by slab, interleaved across the streams,
+  // so the first slabs' results are already queued for copy-out while the
+  // host is still enqueueing later slabs (enqueueing all copy-ins, then all
+  // operators, ... leaves the copy-out stream empty until the host has
+  // issued every call of the apply). Each stream sees its own operations in
+  // the same order either way.
+  auto copy_in = [&](int k) {
     if (!QG_CUDA(cudaMemcpyAsync((char *)g_stage_in + k * sbytes, (const char *)vin + k * sbytes, sbytes,
                                  cudaMemcpyHostToDevice, g_c_in)) ||
         !QG_CUDA(cudaEventRecord(g_ev_cin[k], g_c_in)))
       return false;
-  {
+    if (direct) return true;
     StreamScope scope(g_s_in);
-    for (int k = 0; k < S; k++)
-      if (!QG_CUDA(cudaStreamWaitEvent(g_s_in, g_ev_cin[k], 0)) ||
-          !spinor_from_aos_sites(in, g_stage_in, k * slab, (k + 1) * slab) ||
-          !QG_CUDA(cudaEventRecord(g_ev_in[k], g_s_in)))
+    return QG_CUDA(cudaStreamWaitEvent(g_s_in, g_ev_cin[k], 0)) &&
+           spinor_from_aos_sites(in, g_stage_in, k * slab, (k + 1) * slab) &&
+           QG_CUDA(cudaEventRecord(g_ev_in[k], g_s_in));
+  };
+  // operator on slab k once slab `need` is in (slabs arrive in order), then
+  // the reorder and copy-out of its result; consecutive slabs rotate over
+  // three streams, so a thin slab's launch shares the GPU with the next ones
+  // (the last three slabs all wait for the last copy-in)
+  int nop = 0;
+  auto apply_out = [&](int k, int need) {
+    const int r = nop++ % 3;
+    const cudaStream_t q = r == 0 ? origin : r == 1 ? g_s_op2 : g_s_op3;
+    {
+      StreamScope scope(q);
+      if (!QG_CUDA(cudaStreamWaitEvent(q, ready[need], 0)) ||
+          !(direct ? dslash_sites_aos(g_stage_out, g_stage_in, in, g, mp4, tm, op, (int)(k * slab),
+                                      (int)((k + 1) * slab))
+                   : dslash_sites(out, in, g, mp4, tm, op, -1, (int)(k * slab), (int)((k + 1) * slab))) ||
+          !QG_CUDA(cudaEventRecord(g_ev_op[k], q)))
         return false;
-  }
-  std::vector<int> order;
-  for (int k = 1; k < S - 1; k++) order.push_back(k);
-  order.push_back(S - 1);
-  order.push_back(0);
-  // consecutive slabs alternate between two streams, so a thin slab's
-  // launch shares the GPU with the next one
-  for (size_t i = 0; i < order.size(); i++) {
-    const int k = order[i];
-    const int need = (k == 0 || k == S - 1) ? S - 1 : k + 1;
-    const cudaStream_t q = i % 2 ? g_s_op2 : origin;
-    StreamScope scope(q);
-    if (!QG_CUDA(cudaStreamWaitEvent(q, g_ev_in[need], 0)) ||
-        !dslash_sites(out, in, g, mp4, tm, op, -1, (int)(k * slab), (int)((k + 1) * slab)) ||
-        !QG_CUDA(cudaEventRecord(g_ev_op[k], q)))
-      return false;
-  }
-  {
-    StreamScope scope(g_s_out);
-    for (int k : order)
+    }
+    if (direct) return QG_CUDA(cudaStreamWaitEvent(g_c_out, g_ev_op[k], 0)) &&
+                       QG_CUDA(cudaMemcpyAsync((char *)vout + k * sbytes, (const char *)g_stage_out + k * sbytes,
+                                               sbytes, cudaMemcpyDeviceToHost, g_c_out));
+    {
+      StreamScope scope(g_s_out);
       if (!QG_CUDA(cudaStreamWaitEvent(g_s_out, g_ev_op[k], 0)) ||
           !spinor_to_aos_sites(out, g_stage_out, k * slab, (k + 1) * slab) ||
           !QG_CUDA(cudaEventRecord(g_ev_rout[k], g_s_out)))
         return false;
-  }
-  // device -> host copies, back to back as the slabs are ready
-  for (int k : order)
-    if (!QG_CUDA(cudaStreamWaitEvent(g_c_out, g_ev_rout[k], 0)) ||
-        !QG_CUDA(cudaMemcpyAsync((char *)vout + k * sbytes, (const char *)g_stage_out + k * sbytes, sbytes,
-                                 cudaMemcpyDeviceToHost, g_c_out)))
-      return false;
+    }
+    return QG_CUDA(cudaStreamWaitEvent(g_c_out, g_ev_rout[k], 0)) &&
+           QG_CUDA(cudaMemcpyAsync((char *)vout + k * sbytes, (const char *)g_stage_out + k * sbytes, sbytes,
+                                   cudaMemcpyDeviceToHost, g_c_out));
+  };
+  // slabs 1 .. S-2 as their upper neighbours arrive; 0 and S-1 need each
+  // other (periodic z), so they go last
+  if (!copy_in(0) || !copy_in(1)) return false;
+  for (int k = 2; k < S; k++)
+    if (!copy_in(k) || !apply_out(k - 1, k)) return false;
+  if (!apply_out(S - 1, S - 1) || !apply_out(0, S - 1)) return false;
   // join every side stream back into the origin
   if (!QG_CUDA(cudaEventRecord(g_ev_done, g_c_out)) || !QG_CUDA(cudaStreamWaitEvent(origin, g_ev_done, 0)) ||
-      !QG_CUDA(cudaEventRecord(g_ev_op2, g_s_op2)) || !QG_CUDA(cudaStreamWaitEvent(origin, g_ev_op2, 0)))
+      !QG_CUDA(cudaEventRecord(g_ev_op2, g_s_op2)) || !QG_CUDA(cudaStreamWaitEvent(origin, g_ev_op2, 0)) ||
+      !QG_CUDA(cudaEventRecord(g_ev_op3, g_s_op3)) || !QG_CUDA(cudaStreamWaitEvent(origin, g_ev_op3, 0)))
     return false;
   return true;
 }

@@ -35,8 +35,11 @@ static bool launch_native(const DArgs &a, int prec, int recon)
   return QG_LAUNCHED("wilson");
 }
 
+// in_aos / out_aos (float-float arithmetic only): read and write spinors in
+// the host layout at these device addresses instead of in / out's data
 static bool dslash_once(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4, double tm,
-                        bool dag, bool q, int arith, double *partials = nullptr, int x0 = 0, int x1 = -1)
+                        bool dag, bool q, int arith, double *partials = nullptr, int x0 = 0, int x1 = -1,
+                        const void *in_aos = nullptr, void *out_aos = nullptr)
 {
   DArgs a;
   a.partials = partials;
@@ -80,7 +83,17 @@ static bool dslash_once(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, doubl
     if (!gf) return false;
     a.gauge = gf->data;
     a.gstride = gf->stride;
+    if (in_aos) {
+      a.in = in_aos;
+      a.out = out_aos;
+      a.in_norm = a.out_norm = nullptr;
+      a.aos = 1;
+    }
     return dslash_df64(a, dag);
+  }
+  if (in_aos) {
+    set_error("dslash on host-layout spinors: float-float arithmetic only");
+    return false;
   }
   return dag ? launch_native<true>(a, in->prec, g->recon) : launch_native<false>(a, in->prec, g->recon);
 }
@@ -218,6 +231,22 @@ bool dslash_sites(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4,
   }
   if (arith < 0) arith = g_f64_arith;
   return dslash_once(out, in, g, mp4, tm, false, op == QCDGPU_OP_Q, arith, nullptr, x0, x1);
+}
+
+// D or Q on sites [x0, x1) of spinors in the host layout (12 double2 per
+// site) at device addresses in_aos / out_aos, computed by the float-float
+// kernel; `shape` is an FP64 field of the lattice (its data is not used)
+bool dslash_sites_aos(void *out_aos, const void *in_aos, qcdgpu_field shape, qcdgpu_gauge g, double mp4, double tm,
+                      int op, int x0, int x1)
+{
+  if (!out_aos || !in_aos || !shape || !g || out_aos == in_aos || shape->prec != QCDGPU_F64 ||
+      g->prec != QCDGPU_F64 || shape->V != g->V || (op != QCDGPU_OP_D && op != QCDGPU_OP_Q) || x0 < 0 ||
+      x1 > shape->V || x0 >= x1) {
+    set_error("dslash over a site range of host-layout spinors: FP64, op D or Q, 0 <= x0 < x1 <= V");
+    return false;
+  }
+  return dslash_once(shape, shape, g, mp4, tm, false, op == QCDGPU_OP_Q, QCDGPU_ARITH_DF64, nullptr, x0, x1, in_aos,
+                     out_aos);
 }
 
 // out = D in (dag: D^+ in) on fields checked by the caller; when partials is

@@ -34,6 +34,10 @@ struct DArgs {
   int ainv;   // 1: hopping term multiplied by A^{-1}
   double ch, ai_r, ai_i;  // A^{-1} = ai_r + i ai_i g5
   float ch_h, ch_l, ai_r_h, ai_r_l, ai_i_h, ai_i_l;
+  // 1: in and out are in the host layout, [site][spin][colour] complex
+  // double (12 double2 per site), instead of component blocks of `stride`
+  // sites (full-lattice float-float kernel only)
+  int aos = 0;
 };
 
 // |v|^2 summed over the block into partials[blockIdx.x]; every thread of the

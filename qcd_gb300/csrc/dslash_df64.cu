@@ -298,8 +298,9 @@ __device__ __forceinline__ void cp_async_wait()
 constexpr int kFFThreads = 384;
 constexpr size_t kFFStageBytes = 2 * 4 * kFFThreads * sizeof(double2);
 
-// the float-float operator for one group's 32 sites; returns the thread's |out|^2
-template <bool DAG, bool EO>
+// the float-float operator for one group's 32 sites; returns the thread's |out|^2.
+// AOS: in and out in the host layout (site-major, 12 double2 per site)
+template <bool DAG, bool EO, bool AOS>
 __device__ __forceinline__ double group_ff(const DArgs &a, int grp, int col, int lane, int e, bool act, int x,
                                            const int c[4], CF (*hs)[2][3][32], double2 *stage)
 {
@@ -314,7 +315,9 @@ __device__ __forceinline__ double group_ff(const DArgs &a, int grp, int col, int
       const int b02 = (mu2 == 0 || mu2 == 3) ? 2 : 3;
       const int comp[4] = {col, 3 + col, 3 * b02 + col, 3 * (5 - b02) + col};
 #pragma unroll
-      for (int i = 0; i < 4; i++) cp_async16(stage + (st * 4 + i) * kFFThreads + tid, sp + (int64_t)comp[i] * a.stride + ys2);
+      for (int i = 0; i < 4; i++)
+        cp_async16(stage + (st * 4 + i) * kFFThreads + tid,
+                   AOS ? sp + (int64_t)ys2 * 12 + comp[i] : sp + (int64_t)comp[i] * a.stride + ys2);
     }
     cp_async_commit();
   };
@@ -437,7 +440,7 @@ __device__ __forceinline__ double group_ff(const DArgs &a, int grp, int col, int
     for (int s = 0; s < 4; s++) {
       // (m+4) psi + i tm g5 psi - acc/2 for component (spin s, colour col)
       const int k = 3 * s + col;
-      CF sv = load_sp(sp, a.stride, x, k);
+      CF sv = AOS ? load_sp(sp + (int64_t)x * 12, 1, 0, k) : load_sp(sp, a.stride, x, k);
       F2 g5tm = s < 2 ? tm : neg(tm), mg5tm = neg(g5tm);
       F2 ar = fin(acc[s].re), ai = fin(acc[s].im);
       FA re{__fmul_rn(ar.h, -0.5f), __fmul_rn(ar.l, -0.5f)};
@@ -458,7 +461,7 @@ __device__ __forceinline__ double group_ff(const DArgs &a, int grp, int col, int
         }
       }
       double vr = join_d(dr), vi = join_d(di);
-      out[(int64_t)k * a.stride + x] = make_double2(vr, vi);
+      out[AOS ? (int64_t)x * 12 + k : (int64_t)k * a.stride + x] = make_double2(vr, vi);
       n2 += vr * vr + vi * vi;
     }
   }
@@ -467,7 +470,7 @@ __device__ __forceinline__ double group_ff(const DArgs &a, int grp, int col, int
 
 // EO: even/odd kernel on half fields (sites of parity a.eo_par; neighbours
 // read at (full index) >> 1) with the epilogue ch * [A^{-1}] H in + {z | A z}
-template <bool DAG, bool EO>
+template <bool DAG, bool EO, bool AOS>
 __global__ void __launch_bounds__(384, 3) k_wilson_ff(const DArgs a)
 {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -478,7 +481,7 @@ __global__ void __launch_bounds__(384, 3) k_wilson_ff(const DArgs a)
   int c[4];
   const int x = ff_site<EO>(a, e, act, c);
   extern __shared__ double2 ff_stage[];
-  const double n2 = group_ff<DAG, EO>(a, grp, col, lane, e, act, x, c, hs, ff_stage);
+  const double n2 = group_ff<DAG, EO, AOS>(a, grp, col, lane, e, act, x, c, hs, ff_stage);
   if (a.partials) block_partial(n2, a.partials);
 }
 
@@ -532,15 +535,15 @@ bool gauge_to_ff(qcdgpu_gauge d, qcdgpu_gauge s)
 
 // the staging buffer is dynamic shared memory (48 KB, above the default
 // limit): opted in once per instantiation
-template <bool D, bool E>
+template <bool D, bool E, bool A = false>
 static void launch_ff(const DArgs &a, unsigned grid)
 {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_wilson_ff<D, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFFStageBytes);
+    cudaFuncSetAttribute(k_wilson_ff<D, E, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFFStageBytes);
     attr = true;
   }
-  k_wilson_ff<D, E><<<grid, kFFThreads, kFFStageBytes, stream()>>>(a);
+  k_wilson_ff<D, E, A><<<grid, kFFThreads, kFFStageBytes, stream()>>>(a);
 }
 
 bool dslash_df64(const DArgs &a, bool dag, bool eo)
@@ -549,6 +552,9 @@ bool dslash_df64(const DArgs &a, bool dag, bool eo)
   if (eo) {
     if (dag) launch_ff<true, true>(a, grid);
     else launch_ff<false, true>(a, grid);
+  } else if (a.aos) {
+    if (dag) launch_ff<true, false, true>(a, grid);
+    else launch_ff<false, false, true>(a, grid);
   } else {
     if (dag) launch_ff<true, false>(a, grid);
     else launch_ff<false, false>(a, grid);

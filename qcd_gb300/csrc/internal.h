@@ -129,6 +129,10 @@ bool spinor_to_aos_sites(qcdgpu_field f, void *dev_aos, int64_t x0, int64_t x1);
 // dslash.cu: op D or Q on sites x0 .. x1-1 only
 bool dslash_sites(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4, double tm, int op, int arith,
                   int x0, int x1);
+// the same with the spinors in the host layout (12 double2 per site) at
+// device addresses, float-float arithmetic; `shape` gives the lattice
+bool dslash_sites_aos(void *out_aos, const void *in_aos, qcdgpu_field shape, qcdgpu_gauge g, double mp4, double tm,
+                      int op, int x0, int x1);
 
 // lime.cu: LIME files (ILDG gauge fields, ETMC spinors) <-> the host layout
 // [V][4][3][3] / [V][4][3] complex double in device memory
