@@ -398,16 +398,23 @@ int qcdgpu_mfield_get(qcdgpu_field f, qcdgpu_mfield m, int r);
  * the FP64 gauge field */
 int qcdgpu_dslash_mrhs(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_gauge g, double kappa, double mu, int op,
                        int nact);
-/* The operator has two kernels: SIMT (one thread per site and RHS, links
- * shared through L1) and tensor cores (one warp per site, link x RHS block
- * products as TF32 MMAs). By default (-1) the first call for a lattice
- * volume and slot count times the SIMT kernel with 64-, 128- and 256-thread
- * blocks and the tensor-core kernel and keeps the fastest; 1 forces the
- * tensor-core kernel, 64 / 128 / 256 the SIMT kernel with that block size. */
+/* The operator has three kernels: SIMT (one thread per site and RHS, links
+ * shared through L1), tcgen05 tensor cores (one FP16 GEMM per site and
+ * 16-slot group, the eight hops concatenated along K, FP32 accumulators in
+ * tensor memory; slot counts that are multiples of 16) and mma.sync tensor
+ * cores (one warp per site, TF32; full lattice only). By default (-1) the
+ * first call for a lattice volume and slot count times the SIMT kernel with
+ * 64-, 128- and 256-thread blocks and one or two slots per thread and the
+ * tensor-core kernels, and keeps the fastest; 1 forces the mma.sync kernel,
+ * 2 the tcgen05 kernel, 64 / 128 / 256 (+1: two slots per thread) the SIMT
+ * kernel with that block size. */
 int qcdgpu_set_mrhs_variant(int variant);
-/* the tuned choice for (L, nrhs): variant 0 SIMT / 1 tensor cores and the
- * SIMT block size; returns 1 when nothing has been tuned for it yet */
+/* the tuned choice for (L, nrhs): variant 0 SIMT / 1 mma.sync / 2 tcgen05
+ * and the SIMT block size; returns 1 when nothing has been tuned for it yet */
 int qcdgpu_mrhs_tuned(const int L[4], int nrhs, int *variant, int *threads);
+/* *n = tiles the tcgen05 kernel abandoned after its bounded wait for the
+ * tensor cores ran out (0 unless the hardware stalled) */
+int qcdgpu_mrhs_tc_timeouts(unsigned *n);
 
 /* Batched solver with continuous admission (no reference counterpart). A
  * batch of `capacity` slots (1..64) runs mixed-precision CG on the normal

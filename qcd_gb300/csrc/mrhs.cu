@@ -4,8 +4,11 @@
 // (site, RHS), laid out [component 0..11][site][rhs] as half2 (re, im), so
 // the RHS of one site and component are contiguous.
 //
-// Operator (tensor cores): one warp per site. For each of the eight hops the
-// warp builds, for 16 RHS at a time, the matrix A (16 RHS x 12 reals of the
+// Operator: three kernels, picked per (volume, slot count) by timing. SIMT:
+// one thread per site and one or two slots, links shared through L1.
+// tcgen05: one FP16 GEMM per site with the eight hops concatenated along K
+// (see k_wilson_mrhs_tc). mma.sync (below): one warp per site. For each of
+// the eight hops the warp builds, for 16 RHS at a time, the matrix A (16 RHS x 12 reals of the
 // projected half spinor, padded to 16) and multiplies it with
 //   B = realified ( R_mu (x) U_mu )   (12 x 24, padded to 16 x 24)
 // where U_mu is the link (or U^+ for backward hops, phase e^{+-i th/L}
@@ -254,16 +257,12 @@ __device__ __forceinline__ void mload_rp(const MArgs &a, const __half2 *d, const
   }
 }
 
-// h = upper half of (1 + S g_mu) s for slot r of the multi-RHS spinor at y,
-// projected on packed half pairs (as the single-RHS FP16 kernel does)
+// h = nrm * upper half of (1 + S g_mu) s for the spinor s held as its three
+// 16-byte words, projected on packed half pairs (as the single-RHS FP16
+// kernel does)
 template <int MU, int S>
-__device__ __forceinline__ void mload_project(const __half2 *d, int64_t V, int N, int y, int r, float nrm,
-                                              C<float> h[6])
+__device__ __forceinline__ void project_words(const uint4 w[3], float nrm, C<float> h[6])
 {
-  const uint4 *p = (const uint4 *)d;
-  uint4 w[3];
-#pragma unroll
-  for (int j = 0; j < 3; j++) w[j] = p[((int64_t)j * V + y) * N + r];
   const __half2 *hv = reinterpret_cast<const __half2 *>(w);
   constexpr bool IM = MU & 1;
   constexpr int B0 = (MU == 0 || MU == 3) ? 2 : 3, B1 = 5 - B0;
@@ -275,6 +274,18 @@ __device__ __forceinline__ void mload_project(const __half2 *d, int64_t V, int N
     h[c] = C<float>{nrm * f0.x, nrm * f0.y};
     h[3 + c] = C<float>{nrm * f1.x, nrm * f1.y};
   }
+}
+
+// the same for slot r of the multi-RHS spinor at y
+template <int MU, int S>
+__device__ __forceinline__ void mload_project(const __half2 *d, int64_t V, int N, int y, int r, float nrm,
+                                              C<float> h[6])
+{
+  const uint4 *p = (const uint4 *)d;
+  uint4 w[3];
+#pragma unroll
+  for (int j = 0; j < 3; j++) w[j] = p[((int64_t)j * V + y) * N + r];
+  project_words<MU, S>(w, nrm, h);
 }
 
 template <int MU, bool DAG, int RP, bool EO>
@@ -550,8 +561,380 @@ __global__ void k_mnorm(const __half2 *d, const float *dn, int V, int N, int nac
   }
 }
 
+// ------------------------------------------------- tensor cores (tcgen05)
+// One GEMM per site holds all eight hops: the hops are concatenated along K.
+//   D (64 x 8) = A (64 x 64) B (64 x 8), FP16 operands, FP32 accumulator in
+// tensor memory, for a group of 16 RHS. Row i = spin * 16 + slot of A holds,
+// in K chunk dd (hop dd = 2 mu + backward), the projected half spinor of the
+// slot at the neighbour (rows of spins 0, 1) or its spin-rebuilt image (rows
+// of spins 2, 3: the permutation and the factors +-1, +-i of
+// (1 + S g_mu), which commute with the link) as 3 complex = 6 halves, scaled
+// by the neighbour's norm over the largest of the slot's eight neighbour
+// norms; B holds, per hop, the realified 3 x 3 link (U, or U^+ for backward
+// hops, boundary phase folded in) in FP16. Per tile of 8 sites: 128 threads
+// build A (one thread per site and slot) and B (two threads per link), one
+// thread issues 8 x 4 MMAs (M = 64, N = 8, K = 16) into 64 tensor-memory
+// columns and commits them to an mbarrier, the warps read the accumulators
+// back (warp w holds spin w of the 16 slots in its lanes 0..15), and the
+// epilogue (diagonal term, A^{-1}, FP16 rounding with per-site norm, per-slot
+// |out|^2) runs one thread per site and slot. The slot's rescale factor
+// multiplies the accumulator back.
+constexpr int kTcSites = 8;     // sites per tile (one MMA chain each)
+constexpr int kTcTiles = 16;    // tiles per CTA
+constexpr int kTcThreads = 128;
+constexpr size_t kTcABytes = (size_t)kTcSites * 8192;  // 64 rows x 64 K halves per site
+constexpr size_t kTcBBytes = (size_t)kTcSites * 1024;  // 8 rows x 64 K halves per site
+constexpr size_t kTcSmem = kTcABytes + kTcBBytes + sizeof(double) * kTcSites * 16;
+
+__device__ unsigned g_mrhs_tc_timeouts;  // tiles abandoned after a bounded mbarrier wait
+
+__device__ __forceinline__ uint32_t tc_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: no swizzle, K-major core matrices of 8
+// rows x 16 bytes; lbo = byte step between K-adjacent core matrices, sbo =
+// byte step between 8-row groups; bits 46-48 hold the fixed value 0b001
+__device__ __forceinline__ uint64_t tc_sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+
+// instruction descriptor, kind::f16: D FP32 (bits 4-5 = 1), A and B FP16
+// (bits 7-12 = 0), both K-major (bits 15, 16 = 0), N >> 3 at bit 17, M >> 4
+// at bit 24
+constexpr uint32_t tc_idesc(int M, int N) { return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24); }
+
+__device__ __forceinline__ uint32_t pack_h2(float a, float b)
+{
+  const __half2 h = __floats2half2_rn(a, b);
+  return *(const uint32_t *)&h;
+}
+
+// the 8-half row (re0, im0, re1, im1, re2, im2, 0, 0) of f * v (f = +-1 or
+// +-i as (fr, fi)) for a complex colour 3-vector v
+__device__ __forceinline__ uint4 tc_row(const C<float> v[3], float fr, float fi)
+{
+  uint4 w;
+  w.x = pack_h2(fr * v[0].re - fi * v[0].im, fr * v[0].im + fi * v[0].re);
+  w.y = pack_h2(fr * v[1].re - fi * v[1].im, fr * v[1].im + fi * v[1].re);
+  w.z = pack_h2(fr * v[2].re - fi * v[2].im, fr * v[2].im + fi * v[2].re);
+  w.w = 0u;
+  return w;
+}
+
+// rows of hop (MU, S) for the four spins: the upper half h0 (spin 0), h1
+// (spin 1) and the lower spins 2, 3 that (1 + S g_mu) rebuilds from them
+// (the rules of accumulate<MU, S>)
+template <int MU, int S>
+__device__ __forceinline__ void tc_hop_rows(const C<float> h[6], uint4 rows[4])
+{
+  const C<float> *h0 = h, *h1 = h + 3;
+  const float s = (float)S;
+  rows[0] = tc_row(h0, 1.f, 0.f);
+  rows[1] = tc_row(h1, 1.f, 0.f);
+  if (MU == 0) {
+    rows[2] = tc_row(h0, -s, 0.f);
+    rows[3] = tc_row(h1, -s, 0.f);
+  } else if (MU == 1) {
+    rows[2] = tc_row(h1, 0.f, s);
+    rows[3] = tc_row(h0, 0.f, s);
+  } else if (MU == 2) {
+    rows[2] = tc_row(h1, s, 0.f);
+    rows[3] = tc_row(h0, -s, 0.f);
+  } else {
+    rows[2] = tc_row(h0, 0.f, s);
+    rows[3] = tc_row(h1, 0.f, -s);
+  }
+}
+
+// neighbour of x in hop dd (2 mu + backward)
+__device__ __forceinline__ int tc_nb(const Geom &g, int x, const int c[4], int dd)
+{
+  return (dd & 1) ? bwd(g, x, c, dd >> 1) : fwd(g, x, c, dd >> 1);
+}
+
+template <bool DAG, int DD, bool EO>
+__device__ __forceinline__ void tc_build_hop(const MArgs &a, int ys, int r, float sc, unsigned char *Asite, int rl)
+{
+  constexpr int MU = DD >> 1, SF = DAG ? +1 : -1, S = (DD & 1) ? -SF : SF;
+  const uint4 *p = (const uint4 *)a.in;
+  uint4 w[3];
+#pragma unroll
+  for (int j = 0; j < 3; j++) w[j] = p[((int64_t)j * a.V + ys) * a.N + r];
+  C<float> h[6];
+  project_words<MU, S>(w, sc, h);
+  uint4 rows[4];
+  tc_hop_rows<MU, S>(h, rows);
+#pragma unroll
+  for (int sp = 0; sp < 4; sp++) {
+    const int i = sp * 16 + rl;  // A row
+    *(uint4 *)(Asite + (i >> 3) * 1024 + DD * 128 + (i & 7) * 16) = rows[sp];
+  }
+}
+
+template <bool DAG, int MODE>
+__global__ void __launch_bounds__(kTcThreads, 3) k_wilson_mrhs_tc(const MArgs a, double *partials)
+{
+  extern __shared__ __align__(16) unsigned char tc_dyn[];
+  unsigned char *As = tc_dyn, *Bs = tc_dyn + kTcABytes;
+  double *red = (double *)(tc_dyn + kTcABytes + kTcBBytes);
+  float *X = (float *)tc_dyn;  // accumulators [site][spin][slot][6], over A once the MMAs are done
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tbase;
+  constexpr bool EO = MODE != 0;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int s = tid >> 4, rl = tid & 15;  // this thread's site in the tile and slot in the group
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&mbar)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(tc_smem(&tbase)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tbase;
+  const int G = a.N >> 4;
+  uint32_t phase = 0;
+  double run[4] = {0.0, 0.0, 0.0, 0.0};  // per-slot |out|^2 of the CTA (threads 0..15)
+  bool failed = false;
+  for (int tile = 0; tile < kTcTiles && !failed; tile++) {
+    const int base = (blockIdx.x * kTcTiles + tile) * kTcSites;
+    if (base >= a.V) break;
+    const int e = base + s;  // output index
+    const bool act = e < a.V;
+    int c[4], x = e;
+    if (act) {
+      if (EO) {
+        coords(a.geo, 2 * e, c);
+        const int b = (a.eo_par ^ c[1] ^ c[2] ^ c[3]) & 1;
+        x = 2 * e + b;
+        c[0] += b;
+      } else {
+        coords(a.geo, x, c);
+      }
+    }
+    // B: link of hop dd for site s, output colour rows half*4 .. half*4+3
+    {
+      const int dd = rl >> 1, half = rl & 1, mu = dd >> 1;
+      uint4 rows[4] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0),
+                       make_uint4(0, 0, 0, 0)};
+      if (act) {
+        const bool back = dd & 1;
+        const int y = tc_nb(a.geo, x, c, dd);
+        C<float> U[9];
+        Link<QCDGPU_F32, 18, float>::load(a.gauge, a.gstride, back ? y : x, mu, U);
+        const bool tw = (a.twist_mask >> mu) & 1;
+        const C<float> ph{tw ? a.phr[mu] : 1.f, tw ? (back ? -a.phi[mu] : a.phi[mu]) : 0.f};
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+          const int i = half * 2 + q;  // output colour (2: only for half 1, q 0)
+          if (i < 3) {
+            C<float> m[3];
+#pragma unroll
+            for (int j = 0; j < 3; j++) m[j] = ph * (back ? conj(U[3 * j + i]) : U[3 * i + j]);
+            // row n = 2i (re): (Re m_j, -Im m_j) ; row n = 2i + 1 (im): (Im m_j, Re m_j)
+            rows[2 * q] = make_uint4(pack_h2(m[0].re, -m[0].im), pack_h2(m[1].re, -m[1].im),
+                                     pack_h2(m[2].re, -m[2].im), 0u);
+            rows[2 * q + 1] = make_uint4(pack_h2(m[0].im, m[0].re), pack_h2(m[1].im, m[1].re),
+                                         pack_h2(m[2].im, m[2].re), 0u);
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; q++) *(uint4 *)(Bs + s * 1024 + dd * 128 + (half * 4 + q) * 16) = rows[q];
+    }
+    // neighbours and their norms are the same for every slot group
+    int ys[8];
+#pragma unroll
+    for (int dd = 0; dd < 8; dd++) {
+      const int y = act ? tc_nb(a.geo, x, c, dd) : 0;
+      ys[dd] = EO ? (y >> 1) : y;
+    }
+    for (int grp = 0; grp < G && !failed; grp++) {
+      const int r = grp * 16 + rl;
+      unsigned char *Asite = As + s * 8192;
+      float sc = 0.f;  // the slot's rescale: the largest neighbour norm
+      if (act) {
+        float nr[8];
+#pragma unroll
+        for (int dd = 0; dd < 8; dd++) {
+          nr[dd] = a.in_norm[(int64_t)ys[dd] * a.N + r];
+          sc = fmaxf(sc, nr[dd]);
+        }
+        const float inv = sc > 0.f ? 1.0f / sc : 0.f;
+        tc_build_hop<DAG, 0, EO>(a, ys[0], r, nr[0] * inv, Asite, rl);
+        tc_build_hop<DAG, 1, EO>(a, ys[1], r, nr[1] * inv, Asite, rl);
+        tc_build_hop<DAG, 2, EO>(a, ys[2], r, nr[2] * inv, Asite, rl);
+        tc_build_hop<DAG, 3, EO>(a, ys[3], r, nr[3] * inv, Asite, rl);
+        tc_build_hop<DAG, 4, EO>(a, ys[4], r, nr[4] * inv, Asite, rl);
+        tc_build_hop<DAG, 5, EO>(a, ys[5], r, nr[5] * inv, Asite, rl);
+        tc_build_hop<DAG, 6, EO>(a, ys[6], r, nr[6] * inv, Asite, rl);
+        tc_build_hop<DAG, 7, EO>(a, ys[7], r, nr[7] * inv, Asite, rl);
+      } else {
+#pragma unroll
+        for (int sp = 0; sp < 4; sp++) {
+          const int i = sp * 16 + rl;
+#pragma unroll
+          for (int dd = 0; dd < 8; dd++)
+            *(uint4 *)(Asite + (i >> 3) * 1024 + dd * 128 + (i & 7) * 16) = make_uint4(0, 0, 0, 0);
+        }
+      }
+      // the tensor cores read what the threads wrote
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      if (tid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        constexpr uint32_t idesc = tc_idesc(64, 8);
+#pragma unroll 1
+        for (int t = 0; t < kTcSites; t++) {
+#pragma unroll
+          for (int kk = 0; kk < 4; kk++) {
+            const uint64_t ad = tc_sdesc(tc_smem(As + t * 8192 + kk * 256), 128, 1024);
+            const uint64_t bd = tc_sdesc(tc_smem(Bs + t * 1024 + kk * 256), 128, 1024);
+            const uint32_t dt = tmem + (uint32_t)(t * 8), acc = kk > 0;
+            asm volatile(
+                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(dt),
+                "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+          }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         tc_smem(&mbar))
+                     : "memory");
+      }
+      // bounded wait for the commit; a timeout abandons the kernel's work
+      uint32_t done = 0;
+      for (int it = 0; it < (1 << 24) && !done; it++)
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(tc_smem(&mbar)), "r"(phase)
+            : "memory");
+      if (__syncthreads_or(!done)) {
+        // the MMAs may still be in flight: wait once more, bounded, before
+        // the tensor memory is released
+        for (int it = 0; it < (1 << 24) && !done; it++)
+          asm volatile(
+              "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+              : "=r"(done)
+              : "r"(tc_smem(&mbar)), "r"(phase)
+              : "memory");
+        if (tid == 0) atomicAdd(&g_mrhs_tc_timeouts, 1u);
+        failed = true;
+        break;
+      }
+      phase ^= 1u;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      // accumulators -> X[site][spin = warp][slot = lane][6]
+#pragma unroll
+      for (int t = 0; t < kTcSites; t++) {
+        uint32_t v[8];
+        const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(t * 8);
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                     : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+                     : "r"(ta));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (lane < 16) {
+          float *xo = X + ((t * 4 + warp) * 16 + lane) * 6;
+#pragma unroll
+          for (int k = 0; k < 6; k++) xo[k] = __uint_as_float(v[k]);
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      // epilogue: one thread per (site, slot)
+      double n2 = 0.0;
+      if (act) {
+        C<float> acc[12];
+#pragma unroll
+        for (int sp = 0; sp < 4; sp++) {
+          const float *xi = X + ((s * 4 + sp) * 16 + rl) * 6;
+#pragma unroll
+          for (int cc = 0; cc < 3; cc++) acc[3 * sp + cc] = C<float>{sc * xi[2 * cc], sc * xi[2 * cc + 1]};
+        }
+        constexpr int zmode = MODE == 1 ? 0 : 2;
+        constexpr bool ainv = MODE == 1;
+        constexpr float ch = MODE == 0 ? -0.5f : MODE == 1 ? 1.0f : -0.25f;
+        C<float> zs[1][12];
+        float znrm[1] = {0.f};
+        if (zmode) mload_rp<1>(a, EO ? a.z : a.in, EO ? a.z_norm : a.in_norm, e, r, zs, znrm);
+        const float mp4r = a.mp4s ? a.mp4s[r] : a.mp4;
+        const float tmr = a.tms ? (DAG ? -a.tms[r] : a.tms[r]) : a.tm;
+        if (ainv) {  // A^{-1} = (mp4 - i tm g5) / (mp4^2 + tm^2)
+          const float den = 1.0f / (mp4r * mp4r + tmr * tmr), ar = mp4r * den, ai = -tmr * den;
+#pragma unroll
+          for (int k = 0; k < 12; k++) {
+            const float g5ai = k < 6 ? ai : -ai;
+            acc[k] = C<float>{ar * acc[k].re - g5ai * acc[k].im, ar * acc[k].im + g5ai * acc[k].re};
+          }
+        }
+        const float zsc = zmode ? znrm[0] : 0.f;
+        const float zm = zmode == 2 ? mp4r * zsc : zsc, zt = zmode == 2 ? tmr * zsc : 0.f;
+        float mx = 0.f;
+#pragma unroll
+        for (int k = 0; k < 12; k++) {
+          const float g5tm = k < 6 ? zt : -zt;
+          const C<float> zk = zmode ? zs[0][k] : C<float>{0.f, 0.f};
+          acc[k] = C<float>{zm * zk.re - g5tm * zk.im + ch * acc[k].re, zm * zk.im + g5tm * zk.re + ch * acc[k].im};
+          mx = fmaxf(mx, fmaxf(fabsf(acc[k].re), fabsf(acc[k].im)));
+        }
+        if (!(mx >= 1.17549435e-38f)) mx = 0.f;
+        const float inv = mx > 0.f ? 1.0f / mx : 0.f;
+        if (r < a.nact) {
+          float2 o[12];
+#pragma unroll
+          for (int k = 0; k < 12; k++) o[k] = make_float2(acc[k].re, acc[k].im);
+          mstore_raw(a.out, a.V, a.N, e, r, o, inv);
+          a.out_norm[(int64_t)e * a.N + r] = mx;
+          if (partials) {  // |out|^2 of the stored (rounded) values
+            float s2 = 0.f;
+#pragma unroll
+            for (int k = 0; k < 12; k++) {
+              const float2 f = __half22float2(__floats2half2_rn(o[k].x * inv, o[k].y * inv));
+              s2 += f.x * f.x + f.y * f.y;
+            }
+            n2 = (double)(s2 * mx * mx);
+          }
+        }
+      }
+      if (partials) {  // the CTA's per-slot sums, in a fixed order
+        red[s * 16 + rl] = n2;
+        __syncthreads();
+        if (tid < 16) {
+          double t = 0.0;
+          for (int i = 0; i < kTcSites; i++) t += red[i * 16 + tid];
+          run[grp] += t;
+        }
+      }
+      __syncthreads();  // X and red are rewritten by the next group
+    }
+  }
+  if (partials && tid < 16)
+    for (int grp = 0; grp < G; grp++) partials[(int64_t)blockIdx.x * a.N + grp * 16 + tid] = run[grp];
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
+}
+
+unsigned mrhs_tc_grid(int64_t V) { return (unsigned)((V + kTcSites * kTcTiles - 1) / (kTcSites * kTcTiles)); }
+
+template <bool D, int M>
+static void launch_tc(const MArgs &a, double *partials, unsigned grid, cudaStream_t s)
+{
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_wilson_mrhs_tc<D, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+    attr = true;
+  }
+  k_wilson_mrhs_tc<D, M><<<grid, kTcThreads, kTcSmem, s>>>(a, partials);
+}
+
 struct MrhsTune {
-  int variant;  // MRHS_SIMT or MRHS_MMA
+  int variant;  // MRHS_SIMT, MRHS_MMA or MRHS_TC
   int threads;  // SIMT: N x (sites per block) target, 64, 128 or 256
   int rp;       // SIMT: RHS slots per thread (1, or 2 when N is even)
 };
@@ -575,6 +958,26 @@ unsigned mrhs_max_blocks(int64_t V, int N)
 static bool launch_mrhs(const MArgs &a, bool dag, MrhsTune t, double *partials, unsigned *nblocks)
 {
   cudaStream_t s = stream();
+  if (t.variant == MRHS_TC) {
+    if (a.N % 16 != 0 || a.N > 64) {
+      set_error("tensor-core (tcgen05) multi-RHS kernel: slot count a multiple of 16, at most 64 (got %d)", a.N);
+      return false;
+    }
+    const unsigned grid = mrhs_tc_grid(a.V);
+    const int mode = a.eo_par < 0 ? 0 : a.ainv ? 1 : 2;
+    if (dag) {
+      if (mode == 0) launch_tc<true, 0>(a, partials, grid, s);
+      else if (mode == 1) launch_tc<true, 1>(a, partials, grid, s);
+      else launch_tc<true, 2>(a, partials, grid, s);
+    } else {
+      if (mode == 0) launch_tc<false, 0>(a, partials, grid, s);
+      else if (mode == 1) launch_tc<false, 1>(a, partials, grid, s);
+      else launch_tc<false, 2>(a, partials, grid, s);
+    }
+    if (!QG_LAUNCHED("wilson_mrhs_tc")) return false;
+    if (nblocks) *nblocks = grid;
+    return true;
+  }
   const bool simt = t.variant == MRHS_SIMT;
   // threads for the occupied slots only (the tuned block size holds more
   // sites when fewer slots are occupied), except when the launch writes
@@ -640,6 +1043,7 @@ static bool launch_mrhs(const MArgs &a, bool dag, MrhsTune t, double *partials, 
 static MrhsTune mrhs_tune(const MArgs &a, bool dag)
 {
   if (g_mrhs_variant == MRHS_MMA) return MrhsTune{MRHS_MMA, 256, 1};
+  if (g_mrhs_variant == MRHS_TC) return MrhsTune{MRHS_TC, kTcThreads, 1};
   if (g_mrhs_variant >= 64) {  // forced block size; +1: two slots per thread
     const int rp = (g_mrhs_variant & 1) && a.N % 2 == 0 ? 2 : 1;
     return MrhsTune{MRHS_SIMT, g_mrhs_variant & ~1, rp};
@@ -652,9 +1056,10 @@ static MrhsTune mrhs_tune(const MArgs &a, bool dag)
   cudaStream_t s = stream();
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return fallback;
-  const MrhsTune cands[] = {{MRHS_SIMT, 64, 1}, {MRHS_SIMT, 128, 1}, {MRHS_SIMT, 256, 1}, {MRHS_SIMT, 64, 2},
-                            {MRHS_SIMT, 128, 2}, {MRHS_SIMT, 256, 2}, {MRHS_MMA, 256, 1}};
-  const int ncand = a.eo_par < 0 ? 7 : 6;  // no tensor-core even/odd kernel
+  const MrhsTune cands[] = {{MRHS_SIMT, 64, 1},  {MRHS_SIMT, 128, 1}, {MRHS_SIMT, 256, 1},
+                            {MRHS_SIMT, 64, 2},  {MRHS_SIMT, 128, 2}, {MRHS_SIMT, 256, 2},
+                            {MRHS_TC, kTcThreads, 1}, {MRHS_MMA, 256, 1}};
+  const int ncand = a.eo_par < 0 ? 8 : 7;  // the mma.sync kernel has no even/odd mode
   cudaEvent_t e0, e1;
   if (cudaEventCreate(&e0) != cudaSuccess) return fallback;
   if (cudaEventCreate(&e1) != cudaSuccess) {
@@ -666,6 +1071,7 @@ static MrhsTune mrhs_tune(const MArgs &a, bool dag)
   for (int ic = 0; ic < ncand; ic++) {
     const MrhsTune &c = cands[ic];
     if (c.variant == MRHS_SIMT && (c.threads < a.N || (c.rp == 2 && a.N % 2 != 0))) continue;
+    if (c.variant == MRHS_TC && a.N % 16 != 0) continue;
     if (!launch_mrhs(a, dag, c, nullptr, nullptr)) break;  // warm-up
     cudaEventRecord(e0, s);
     bool ok = true;
@@ -829,14 +1235,20 @@ int qcdgpu_mfield_set(qcdgpu_mfield m, int r, qcdgpu_field f) { return qg::mfiel
 int qcdgpu_mfield_get(qcdgpu_field f, qcdgpu_mfield m, int r) { return qg::mfield_get(f, m, r) ? 0 : 1; }
 int qcdgpu_set_mrhs_variant(int v)
 {
-  if (v != qg::MRHS_AUTO && v != qg::MRHS_MMA && v != 64 && v != 128 && v != 256 && v != 65 && v != 129 &&
-      v != 257) {
-    qg::set_error("multi-RHS variant: -1 (tuned), 1 (tensor cores), 64 / 128 / 256 (SIMT, slots x sites per "
-                  "block), +1 for two slots per thread");
+  if (v != qg::MRHS_AUTO && v != qg::MRHS_MMA && v != qg::MRHS_TC && v != 64 && v != 128 && v != 256 && v != 65 &&
+      v != 129 && v != 257) {
+    qg::set_error("multi-RHS variant: -1 (tuned), 1 (tensor cores, mma.sync), 2 (tensor cores, tcgen05; slot "
+                  "counts that are multiples of 16), 64 / 128 / 256 (SIMT, slots x sites per block), +1 for two "
+                  "slots per thread");
     return 1;
   }
   qg::g_mrhs_variant = v;
   return 0;
+}
+
+int qcdgpu_mrhs_tc_timeouts(unsigned *n)
+{
+  return cudaMemcpyFromSymbol(n, qg::g_mrhs_tc_timeouts, sizeof(unsigned)) == cudaSuccess ? 0 : 1;
 }
 
 int qcdgpu_mrhs_tuned(const int L[4], int nrhs, int *variant, int *threads)

@@ -79,7 +79,7 @@ bool dslash_mrhs_eo(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_mfield z, qcdgpu
                     unsigned *nblocks);
 
 // operator variants picked by the tuner
-enum { MRHS_AUTO = -1, MRHS_SIMT = 0, MRHS_MMA = 1 };
+enum { MRHS_AUTO = -1, MRHS_SIMT = 0, MRHS_MMA = 1, MRHS_TC = 2 };
 
 }  // namespace qg
 

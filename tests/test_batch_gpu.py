@@ -142,3 +142,51 @@ def test_batch_full_and_zero_rhs(gpu, orc):
     batch.close()
     for f in (fb, fz, x1, x2, xz, g):
         f.close()
+
+
+def test_batch_on_tcgen05_kernel(gpu, orc, eo):
+    """The batched solver on the tcgen05 multi-RHS kernel (16-slot capacity):
+    every request converges to its FP64 true residual, and a request solved
+    alone and behind three others gives bit-identical solutions."""
+    import ctypes as C
+
+    u = orc.gauge_synthetic(L, 15, EPS_PLAQ_060)
+    g = q.Gauge(L, TH).load(u)
+    q.set_mrhs_variant(2)
+    try:
+        params = [(0.15, 0.0, q.OP_D, 1e-10), (0.14, 0.02, q.OP_D, 1e-10), (0.155, 0.0, q.OP_Q, 1e-10),
+                  (0.13, 0.0, q.OP_D, 1e-9), (0.145, 0.01, q.OP_D, 1e-10)]
+        reqs, fields, srcs = [], [], []
+        for i, (kappa, mu, op, tol) in enumerate(params):
+            b = orc.gaussian_spinor(L, 700 + i) * (10.0 ** (i % 3 - 1))
+            fb, fx = q.Field(L).load(b), q.Field(L)
+            srcs.append(b)
+            fields += [fb, fx]
+            reqs.append((i, fx, fb, kappa, mu, op, tol))
+        batch = q.Batch(g, 16, eo=eo)
+        res = _run(batch, reqs)
+        assert sorted(res) == list(range(len(params)))
+        for i, (kappa, mu, op, tol) in enumerate(params):
+            assert res[i][0] == 0, (i, res[i])
+            x = reqs[i][1].store()
+            true = orc.true_residual(x, srcs[i], u, L, TH, kappa, mu, op="Q" if op == q.OP_Q else "D")
+            assert true <= tol, (i, true, tol)
+        batch.close()
+        # alone vs in a mix, same capacity
+        b = np.zeros((np.prod(L), 4, 3, 2))
+        b[7, 2, 1, 1] = 1.0
+        fb, fx_alone, fx_mix = q.Field(L).load(b), q.Field(L), q.Field(L)
+        fields += [fb, fx_alone, fx_mix]
+        batch = q.Batch(g, 16, eo=eo)
+        _run(batch, [(0, fx_alone, fb, 0.15, 0.01, q.OP_D, 1e-10)])
+        mix = [(10 + i, reqs[i][1], reqs[i][2], 0.14, 0.0, q.OP_D, 1e-10) for i in range(3)]
+        res = _run(batch, mix + [(0, fx_mix, fb, 0.15, 0.01, q.OP_D, 1e-10)])
+        assert res[0][0] == 0
+        assert np.array_equal(fx_alone.store(), fx_mix.store())
+        batch.close()
+        n = C.c_uint(0)
+        assert q.lib().qcdgpu_mrhs_tc_timeouts(C.byref(n)) == 0 and n.value == 0
+    finally:
+        q.set_mrhs_variant(-1)
+    for f in fields + [g]:
+        f.close()
