@@ -562,31 +562,37 @@ __global__ void k_mnorm(const __half2 *d, const float *dn, int V, int N, int nac
 }
 
 // ------------------------------------------------- tensor cores (tcgen05)
-// One GEMM per site holds all eight hops: the hops are concatenated along K.
-//   D (64 x 8) = A (64 x 64) B (64 x 8), FP16 operands, FP32 accumulator in
-// tensor memory, for a group of 16 RHS. Row i = spin * 16 + slot of A holds,
-// in K chunk dd (hop dd = 2 mu + backward), the projected half spinor of the
-// slot at the neighbour (rows of spins 0, 1) or its spin-rebuilt image (rows
-// of spins 2, 3: the permutation and the factors +-1, +-i of
-// (1 + S g_mu), which commute with the link) as 3 complex = 6 halves, scaled
-// by the neighbour's norm over the largest of the slot's eight neighbour
-// norms; B holds, per hop, the realified 3 x 3 link (U, or U^+ for backward
-// hops, boundary phase folded in) in FP16. Per tile of 8 sites: 128 threads
-// build A (one thread per site and slot) and B (two threads per link), one
-// thread issues 8 x 4 MMAs (M = 64, N = 8, K = 16) into 64 tensor-memory
-// columns and commits them to an mbarrier, the warps read the accumulators
-// back (warp w holds spin w of the 16 slots in its lanes 0..15), and the
-// epilogue (diagonal term, A^{-1}, FP16 rounding with per-site norm, per-slot
-// |out|^2) runs one thread per site and slot. The slot's rescale factor
-// multiplies the accumulator back.
+// One GEMM per site and 16-slot group holds all eight hops:
+//   D^T (24 x 16) = L (24 x 96) H^T (96 x 16),
+// FP16 operands, FP32 accumulator in tensor memory. Row o = (spin S, colour
+// i, re/im) of L is the site's link matrix: in K block h (12 values: input
+// spin s, colour j, re/im) it holds the realified c M_ij, where M = U_mu (or
+// U_mu^+ for backward hops, boundary phase folded in) and c the entry (0, 1,
+// +-1 or +-i) of the 4 x 2 matrix that rebuilds spin S from the projected
+// upper half of (1 +- g_mu); L is built once per site for all slots. Row n of
+// H is slot n's projected half spinor at each of the eight neighbours (packed
+// half pairs, as the FP16 kernels project them), scaled by that neighbour's
+// norm over the slot's largest. The MMA is issued with M = 64 (the smallest
+// M): rows 24..63 of the A operand read whatever follows in shared memory and
+// land in accumulator rows that are never read. Per tile of 8 sites: 128
+// threads build L (two threads per site and hop) and H (one thread per site
+// and slot), one thread issues 8 x 6 MMAs (M = 64, N = 16, K = 16) into 128
+// tensor-memory columns and commits them to an mbarrier, warps 0 and 1 read
+// the 24 accumulator rows back, and the epilogue (diagonal term, A^{-1}, FP16
+// rounding with per-site norm, per-slot |out|^2) runs one thread per site and
+// slot. The slot's rescale factor multiplies the accumulator back.
 constexpr int kTcSites = 8;     // sites per tile (one MMA chain each)
 constexpr int kTcTiles = 16;    // tiles per CTA
 constexpr int kTcThreads = 128;
-constexpr size_t kTcABytes = (size_t)kTcSites * 8192;  // 64 rows x 64 K halves per site
-constexpr size_t kTcBBytes = (size_t)kTcSites * 1024;  // 8 rows x 64 K halves per site
-constexpr size_t kTcSmem = kTcABytes + kTcBBytes + sizeof(double) * kTcSites * 16;
+constexpr int kTcK = 96;                                       // 8 hops x 12
+constexpr uint32_t kTcSbo = (kTcK / 8) * 128;                  // bytes per 8-row group
+constexpr size_t kTcLBytes = (size_t)kTcSites * 3 * kTcSbo;    // 24 rows per site
+constexpr size_t kTcHBytes = (size_t)kTcSites * 2 * kTcSbo;    // 16 rows per site
+constexpr size_t kTcSmem = kTcLBytes + kTcHBytes + sizeof(double) * kTcSites * 16;
+// the M = 64 operand of the last site reads 64 rows from its start: inside the allocation
+static_assert((kTcSites - 1) * 3 * kTcSbo + 8 * kTcSbo <= kTcSmem, "tcgen05 A operand overruns shared memory");
 
-__device__ unsigned g_mrhs_tc_timeouts;  // tiles abandoned after a bounded mbarrier wait
+__device__ unsigned g_mrhs_tc_timeouts;  // rounds abandoned after a bounded mbarrier wait
 
 __device__ __forceinline__ uint32_t tc_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -610,40 +616,54 @@ __device__ __forceinline__ uint32_t pack_h2(float a, float b)
   return *(const uint32_t *)&h;
 }
 
-// the 8-half row (re0, im0, re1, im1, re2, im2, 0, 0) of f * v (f = +-1 or
-// +-i as (fr, fi)) for a complex colour 3-vector v
-__device__ __forceinline__ uint4 tc_row(const C<float> v[3], float fr, float fi)
+// shared stores that the compiler may reorder against global loads (the
+// tensor cores read them after a fence and a barrier)
+__device__ __forceinline__ void sts128(uint32_t a, uint32_t x, uint32_t y, uint32_t z, uint32_t w)
 {
-  uint4 w;
-  w.x = pack_h2(fr * v[0].re - fi * v[0].im, fr * v[0].im + fi * v[0].re);
-  w.y = pack_h2(fr * v[1].re - fi * v[1].im, fr * v[1].im + fi * v[1].re);
-  w.z = pack_h2(fr * v[2].re - fi * v[2].im, fr * v[2].im + fi * v[2].re);
-  w.w = 0u;
-  return w;
+  asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(a), "r"(x), "r"(y), "r"(z), "r"(w));
+}
+__device__ __forceinline__ void sts64(uint32_t a, uint32_t x, uint32_t y)
+{
+  asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(a), "r"(x), "r"(y));
 }
 
-// rows of hop (MU, S) for the four spins: the upper half h0 (spin 0), h1
-// (spin 1) and the lower spins 2, 3 that (1 + S g_mu) rebuilds from them
-// (the rules of accumulate<MU, S>)
-template <int MU, int S>
-__device__ __forceinline__ void tc_hop_rows(const C<float> h[6], uint4 rows[4])
+// the 12 halves (6 words) v of K block h in the row at `row` (address of
+// the row inside its core-matrix group): block h starts at K = 12 h, i.e.
+// at a whole core matrix (h even) or half-way through one (h odd)
+__device__ __forceinline__ void tc_put12(uint32_t row, int h, const uint32_t v[6])
 {
-  const C<float> *h0 = h, *h1 = h + 3;
-  const float s = (float)S;
-  rows[0] = tc_row(h0, 1.f, 0.f);
-  rows[1] = tc_row(h1, 1.f, 0.f);
-  if (MU == 0) {
-    rows[2] = tc_row(h0, -s, 0.f);
-    rows[3] = tc_row(h1, -s, 0.f);
-  } else if (MU == 1) {
-    rows[2] = tc_row(h1, 0.f, s);
-    rows[3] = tc_row(h0, 0.f, s);
-  } else if (MU == 2) {
-    rows[2] = tc_row(h1, s, 0.f);
-    rows[3] = tc_row(h0, -s, 0.f);
+  const uint32_t c = (uint32_t)(12 * h) >> 3;  // first core matrix
+  if ((h & 1) == 0) {
+    sts128(row + c * 128, v[0], v[1], v[2], v[3]);
+    sts64(row + (c + 1) * 128, v[4], v[5]);
   } else {
-    rows[2] = tc_row(h0, 0.f, s);
-    rows[3] = tc_row(h1, 0.f, -s);
+    sts64(row + c * 128 + 8, v[0], v[1]);
+    sts128(row + (c + 1) * 128, v[2], v[3], v[4], v[5]);
+  }
+}
+
+// entry (c, source spin) of the matrix that rebuilds spin sp (0..3) from the
+// projected upper half of (1 + S g_mu) (the rules of accumulate<MU, S>)
+__device__ __forceinline__ void tc_rebuild(int mu, int S, int sp, int &src, float &cr, float &ci)
+{
+  const float s = (float)S;
+  cr = 0.f;
+  ci = 0.f;
+  if (sp < 2) {
+    src = sp;
+    cr = 1.f;
+  } else if (mu == 0) {
+    src = sp - 2;
+    cr = -s;
+  } else if (mu == 1) {
+    src = 3 - sp;
+    ci = s;
+  } else if (mu == 2) {
+    src = 3 - sp;
+    cr = sp == 2 ? s : -s;
+  } else {
+    src = sp - 2;
+    ci = sp == 2 ? s : -s;
   }
 }
 
@@ -653,43 +673,51 @@ __device__ __forceinline__ int tc_nb(const Geom &g, int x, const int c[4], int d
   return (dd & 1) ? bwd(g, x, c, dd >> 1) : fwd(g, x, c, dd >> 1);
 }
 
-template <bool DAG, int DD, bool EO>
-__device__ __forceinline__ void tc_build_hop(const MArgs &a, int ys, int r, float sc, unsigned char *Asite, int rl)
+// slot r's row of H, K block DD: the projected half spinor at neighbour ys,
+// scaled by sc2
+template <bool DAG, int DD>
+__device__ __forceinline__ void tc_h_block(const MArgs &a, int ys, int r, __half2 sc2, uint32_t row)
 {
   constexpr int MU = DD >> 1, SF = DAG ? +1 : -1, S = (DD & 1) ? -SF : SF;
+  constexpr bool IM = MU & 1;
+  constexpr int B0 = (MU == 0 || MU == 3) ? 2 : 3, B1 = 5 - B0;
+  constexpr int SG0 = S > 0 ? -1 : 1, SG1 = MU < 2 ? SG0 : -SG0;
   const uint4 *p = (const uint4 *)a.in;
   uint4 w[3];
 #pragma unroll
   for (int j = 0; j < 3; j++) w[j] = p[((int64_t)j * a.V + ys) * a.N + r];
-  C<float> h[6];
-  project_words<MU, S>(w, sc, h);
-  uint4 rows[4];
-  tc_hop_rows<MU, S>(h, rows);
+  const __half2 *hv = reinterpret_cast<const __half2 *>(w);
+  uint32_t v[6];
 #pragma unroll
-  for (int sp = 0; sp < 4; sp++) {
-    const int i = sp * 16 + rl;  // A row
-    *(uint4 *)(Asite + (i >> 3) * 1024 + DD * 128 + (i & 7) * 16) = rows[sp];
+  for (int c = 0; c < 3; c++) {
+    const __half2 h0 = __hmul2(hcomb<IM>(hv[c], hv[3 * B0 + c], SG0), sc2);
+    const __half2 h1 = __hmul2(hcomb<IM>(hv[3 + c], hv[3 * B1 + c], SG1), sc2);
+    v[c] = *(const uint32_t *)&h0;
+    v[3 + c] = *(const uint32_t *)&h1;
   }
+  tc_put12(row, DD, v);
 }
 
 template <bool DAG, int MODE>
 __global__ void __launch_bounds__(kTcThreads, 3) k_wilson_mrhs_tc(const MArgs a, double *partials)
 {
   extern __shared__ __align__(16) unsigned char tc_dyn[];
-  unsigned char *As = tc_dyn, *Bs = tc_dyn + kTcABytes;
-  double *red = (double *)(tc_dyn + kTcABytes + kTcBBytes);
-  float *X = (float *)tc_dyn;  // accumulators [site][spin][slot][6], over A once the MMAs are done
+  unsigned char *Ls = tc_dyn, *Hs = tc_dyn + kTcLBytes;
+  double *red = (double *)(tc_dyn + kTcLBytes + kTcHBytes);
+  float *X = (float *)Hs;  // accumulators [site][slot][24], over H once the MMAs are done
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tbase;
   constexpr bool EO = MODE != 0;
+  constexpr int SF = DAG ? +1 : -1;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int s = tid >> 4, rl = tid & 15;  // this thread's site in the tile and slot in the group
+  const uint32_t Lb = tc_smem(Ls), Hb = tc_smem(Hs);
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&mbar)));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(tc_smem(&tbase)));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(tc_smem(&tbase)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -716,37 +744,54 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_wilson_mrhs_tc(const MArgs a,
         coords(a.geo, x, c);
       }
     }
-    // B: link of hop dd for site s, output colour rows half*4 .. half*4+3
+    // L: thread (site s, hop h, half) writes the rows of output spins 2 half, 2 half + 1
     {
-      const int dd = rl >> 1, half = rl & 1, mu = dd >> 1;
-      uint4 rows[4] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0),
-                       make_uint4(0, 0, 0, 0)};
+      const int h = rl >> 1, half = rl & 1, mu = h >> 1;
+      const bool back = h & 1;
+      const int S = back ? -SF : SF;
+      C<float> M[9];
       if (act) {
-        const bool back = dd & 1;
-        const int y = tc_nb(a.geo, x, c, dd);
+        const int y = tc_nb(a.geo, x, c, h);
         C<float> U[9];
         Link<QCDGPU_F32, 18, float>::load(a.gauge, a.gstride, back ? y : x, mu, U);
         const bool tw = (a.twist_mask >> mu) & 1;
         const C<float> ph{tw ? a.phr[mu] : 1.f, tw ? (back ? -a.phi[mu] : a.phi[mu]) : 0.f};
 #pragma unroll
-        for (int q = 0; q < 2; q++) {
-          const int i = half * 2 + q;  // output colour (2: only for half 1, q 0)
-          if (i < 3) {
-            C<float> m[3];
+        for (int i = 0; i < 3; i++)
 #pragma unroll
-            for (int j = 0; j < 3; j++) m[j] = ph * (back ? conj(U[3 * j + i]) : U[3 * i + j]);
-            // row n = 2i (re): (Re m_j, -Im m_j) ; row n = 2i + 1 (im): (Im m_j, Re m_j)
-            rows[2 * q] = make_uint4(pack_h2(m[0].re, -m[0].im), pack_h2(m[1].re, -m[1].im),
-                                     pack_h2(m[2].re, -m[2].im), 0u);
-            rows[2 * q + 1] = make_uint4(pack_h2(m[0].im, m[0].re), pack_h2(m[1].im, m[1].re),
-                                         pack_h2(m[2].im, m[2].re), 0u);
-          }
-        }
+          for (int j = 0; j < 3; j++) M[3 * i + j] = ph * (back ? conj(U[3 * j + i]) : U[3 * i + j]);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 9; k++) M[k] = C<float>{0.f, 0.f};
       }
 #pragma unroll
-      for (int q = 0; q < 4; q++) *(uint4 *)(Bs + s * 1024 + dd * 128 + (half * 4 + q) * 16) = rows[q];
+      for (int q = 0; q < 2; q++) {
+        const int sp = 2 * half + q;
+        int src;
+        float cr, ci;
+        tc_rebuild(mu, S, sp, src, cr, ci);
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          uint32_t vre[6], vim[6];
+#pragma unroll
+          for (int j = 0; j < 3; j++) {
+            // z = c M_ij; row re: (Re z, -Im z), row im: (Im z, Re z), in the source spin's columns
+            const float zr = cr * M[3 * i + j].re - ci * M[3 * i + j].im;
+            const float zi = cr * M[3 * i + j].im + ci * M[3 * i + j].re;
+            const uint32_t pre = pack_h2(zr, -zi), pim = pack_h2(zi, zr);
+            vre[j] = src == 0 ? pre : 0u;
+            vre[3 + j] = src == 1 ? pre : 0u;
+            vim[j] = src == 0 ? pim : 0u;
+            vim[3 + j] = src == 1 ? pim : 0u;
+          }
+          const int o = 6 * sp + 2 * i;  // rows o (re) and o + 1 (im)
+          const uint32_t site = Lb + (uint32_t)s * 3 * kTcSbo;
+          tc_put12(site + (uint32_t)(o >> 3) * kTcSbo + (uint32_t)(o & 7) * 16, h, vre);
+          tc_put12(site + (uint32_t)((o + 1) >> 3) * kTcSbo + (uint32_t)((o + 1) & 7) * 16, h, vim);
+        }
+      }
     }
-    // neighbours and their norms are the same for every slot group
+    // neighbours are the same for every slot group
     int ys[8];
 #pragma unroll
     for (int dd = 0; dd < 8; dd++) {
@@ -755,8 +800,9 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_wilson_mrhs_tc(const MArgs a,
     }
     for (int grp = 0; grp < G && !failed; grp++) {
       const int r = grp * 16 + rl;
-      unsigned char *Asite = As + s * 8192;
-      float sc = 0.f;  // the slot's rescale: the largest neighbour norm
+      // H row rl of site s
+      const uint32_t hrow = Hb + (uint32_t)s * 2 * kTcSbo + (uint32_t)(rl >> 3) * kTcSbo + (uint32_t)(rl & 7) * 16;
+      float sc = 0.f;  // the slot's rescale: its largest neighbour norm
       if (act) {
         float nr[8];
 #pragma unroll
@@ -765,22 +811,18 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_wilson_mrhs_tc(const MArgs a,
           sc = fmaxf(sc, nr[dd]);
         }
         const float inv = sc > 0.f ? 1.0f / sc : 0.f;
-        tc_build_hop<DAG, 0, EO>(a, ys[0], r, nr[0] * inv, Asite, rl);
-        tc_build_hop<DAG, 1, EO>(a, ys[1], r, nr[1] * inv, Asite, rl);
-        tc_build_hop<DAG, 2, EO>(a, ys[2], r, nr[2] * inv, Asite, rl);
-        tc_build_hop<DAG, 3, EO>(a, ys[3], r, nr[3] * inv, Asite, rl);
-        tc_build_hop<DAG, 4, EO>(a, ys[4], r, nr[4] * inv, Asite, rl);
-        tc_build_hop<DAG, 5, EO>(a, ys[5], r, nr[5] * inv, Asite, rl);
-        tc_build_hop<DAG, 6, EO>(a, ys[6], r, nr[6] * inv, Asite, rl);
-        tc_build_hop<DAG, 7, EO>(a, ys[7], r, nr[7] * inv, Asite, rl);
+        tc_h_block<DAG, 0>(a, ys[0], r, __float2half2_rn(nr[0] * inv), hrow);
+        tc_h_block<DAG, 1>(a, ys[1], r, __float2half2_rn(nr[1] * inv), hrow);
+        tc_h_block<DAG, 2>(a, ys[2], r, __float2half2_rn(nr[2] * inv), hrow);
+        tc_h_block<DAG, 3>(a, ys[3], r, __float2half2_rn(nr[3] * inv), hrow);
+        tc_h_block<DAG, 4>(a, ys[4], r, __float2half2_rn(nr[4] * inv), hrow);
+        tc_h_block<DAG, 5>(a, ys[5], r, __float2half2_rn(nr[5] * inv), hrow);
+        tc_h_block<DAG, 6>(a, ys[6], r, __float2half2_rn(nr[6] * inv), hrow);
+        tc_h_block<DAG, 7>(a, ys[7], r, __float2half2_rn(nr[7] * inv), hrow);
       } else {
+        const uint32_t z[6] = {0u, 0u, 0u, 0u, 0u, 0u};
 #pragma unroll
-        for (int sp = 0; sp < 4; sp++) {
-          const int i = sp * 16 + rl;
-#pragma unroll
-          for (int dd = 0; dd < 8; dd++)
-            *(uint4 *)(Asite + (i >> 3) * 1024 + dd * 128 + (i & 7) * 16) = make_uint4(0, 0, 0, 0);
-        }
+        for (int dd = 0; dd < 8; dd++) tc_put12(hrow, dd, z);
       }
       // the tensor cores read what the threads wrote
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -788,14 +830,14 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_wilson_mrhs_tc(const MArgs a,
       __syncthreads();
       if (tid == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        constexpr uint32_t idesc = tc_idesc(64, 8);
+        constexpr uint32_t idesc = tc_idesc(64, 16);
 #pragma unroll 1
         for (int t = 0; t < kTcSites; t++) {
 #pragma unroll
-          for (int kk = 0; kk < 4; kk++) {
-            const uint64_t ad = tc_sdesc(tc_smem(As + t * 8192 + kk * 256), 128, 1024);
-            const uint64_t bd = tc_sdesc(tc_smem(Bs + t * 1024 + kk * 256), 128, 1024);
-            const uint32_t dt = tmem + (uint32_t)(t * 8), acc = kk > 0;
+          for (int kk = 0; kk < kTcK / 16; kk++) {
+            const uint64_t ad = tc_sdesc(Lb + (uint32_t)t * 3 * kTcSbo + kk * 256, 128, kTcSbo);
+            const uint64_t bd = tc_sdesc(Hb + (uint32_t)t * 2 * kTcSbo + kk * 256, 128, kTcSbo);
+            const uint32_t dt = tmem + (uint32_t)(t * 16), acc = kk > 0;
             asm volatile(
                 "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
                 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(dt),
@@ -806,6 +848,11 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_wilson_mrhs_tc(const MArgs a,
                          tc_smem(&mbar))
                      : "memory");
       }
+      // the z term of the epilogue does not wait for the tensor cores
+      constexpr int zmode = MODE == 1 ? 0 : 2;
+      C<float> zs[1][12];
+      float znrm[1] = {0.f};
+      if (zmode && act) mload_rp<1>(a, EO ? a.z : a.in, EO ? a.z_norm : a.in_norm, e, r, zs, znrm);
       // bounded wait for the commit; a timeout abandons the kernel's work
       uint32_t done = 0;
       for (int it = 0; it < (1 << 24) && !done; it++)
@@ -829,19 +876,23 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_wilson_mrhs_tc(const MArgs a,
       }
       phase ^= 1u;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      // accumulators -> X[site][spin = warp][slot = lane][6]
+      // accumulator rows 0..23 (warp 0 lanes 0..15, warp 1 lanes 0..7) -> X[site][slot][row]
+      if (warp < 2) {
 #pragma unroll
-      for (int t = 0; t < kTcSites; t++) {
-        uint32_t v[8];
-        const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(t * 8);
-        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                     : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
-                     : "r"(ta));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (lane < 16) {
-          float *xo = X + ((t * 4 + warp) * 16 + lane) * 6;
+        for (int t = 0; t < kTcSites; t++) {
+          uint32_t v[16];
+          const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(t * 16);
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+              : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+              : "r"(ta));
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          const int o = warp * 16 + lane;  // accumulator row
+          if (lane < 16 && o < 24) {
 #pragma unroll
-          for (int k = 0; k < 6; k++) xo[k] = __uint_as_float(v[k]);
+            for (int n = 0; n < 16; n++) X[(t * 16 + n) * 24 + o] = __uint_as_float(v[n]);
+          }
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -850,18 +901,11 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_wilson_mrhs_tc(const MArgs a,
       double n2 = 0.0;
       if (act) {
         C<float> acc[12];
+        const float *xi = X + (s * 16 + rl) * 24;
 #pragma unroll
-        for (int sp = 0; sp < 4; sp++) {
-          const float *xi = X + ((s * 4 + sp) * 16 + rl) * 6;
-#pragma unroll
-          for (int cc = 0; cc < 3; cc++) acc[3 * sp + cc] = C<float>{sc * xi[2 * cc], sc * xi[2 * cc + 1]};
-        }
-        constexpr int zmode = MODE == 1 ? 0 : 2;
+        for (int k = 0; k < 12; k++) acc[k] = C<float>{sc * xi[2 * k], sc * xi[2 * k + 1]};
         constexpr bool ainv = MODE == 1;
         constexpr float ch = MODE == 0 ? -0.5f : MODE == 1 ? 1.0f : -0.25f;
-        C<float> zs[1][12];
-        float znrm[1] = {0.f};
-        if (zmode) mload_rp<1>(a, EO ? a.z : a.in, EO ? a.z_norm : a.in_norm, e, r, zs, znrm);
         const float mp4r = a.mp4s ? a.mp4s[r] : a.mp4;
         const float tmr = a.tms ? (DAG ? -a.tms[r] : a.tms[r]) : a.tm;
         if (ainv) {  // A^{-1} = (mp4 - i tm g5) / (mp4^2 + tm^2)
@@ -910,14 +954,14 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_wilson_mrhs_tc(const MArgs a,
           run[grp] += t;
         }
       }
-      __syncthreads();  // X and red are rewritten by the next group
+      __syncthreads();  // X (over H) and red are rewritten by the next group
     }
   }
   if (partials && tid < 16)
     for (int grp = 0; grp < G; grp++) partials[(int64_t)blockIdx.x * a.N + grp * 16 + tid] = run[grp];
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
 }
 
 unsigned mrhs_tc_grid(int64_t V) { return (unsigned)((V + kTcSites * kTcTiles - 1) / (kTcSites * kTcTiles)); }
