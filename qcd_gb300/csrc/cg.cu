@@ -3,15 +3,16 @@
 //
 // The iteration is written once (cgnr_core) for any system operator A given
 // as kernels: A = D on the full lattice, or the even/odd Schur complement
-// (solve_cgnr_eo). One inner iteration is six launches and no host
+// (solve_cgnr_eo). One inner iteration is four operations (five launches
+// for the even/odd operator, whose A is two hops) and no host
 // synchronisation:
 //   1. t = A p            (operator kernel; its epilogue also sums |t|^2 =
-//                          p^+ A^+ A p per block)
-//   2. scalar kernel:     pAp = sum of the block partials, alpha = rr / pAp
-//   3. Ap = A^+ t         (operator kernel)
-//   4. update kernel:     x' += alpha p, r -= alpha Ap, per-block |r|^2
-//   5. scalar kernel:     rr' = sum, beta = rr'/rr, history[i] = rr'
-//   6. p = r + beta p     (reads beta from device memory)
+//                          p^+ A^+ A p per block, and the block that
+//                          finishes last forms alpha = rr / pAp)
+//   2. Ap = A^+ t         (operator kernel)
+//   3. update kernel:     x' += alpha p, r -= alpha Ap, per-block |r|^2; its
+//                          last block forms rr', beta = rr'/rr, history[i]
+//   4. p = r + beta p     (reads beta from device memory)
 // The host enqueues a chunk of iterations, then reads the residual history
 // once and decides. Reliable updates (Sleijpen & van der Vorst, Computing 56
 // (1996) 141; Clark et al., Comput. Phys. Commun. 181 (2010) 1517): when the
@@ -34,64 +35,10 @@ namespace qg {
 using namespace qgd;
 
 bool dslash_partials(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4, double tm, bool dag,
-                     int arith, double *partials);
+                     int arith, double *partials, const CgFuse *fuse = nullptr);
 double *big_partials(int64_t n);
 
-// scalar slots
-enum { S_RR = 0, S_PAP = 1, S_RRNEW = 2, S_ALPHA = 3, S_BETA = 4, S_HIST = 8 };
 constexpr int kChunk = 16;
-
-// the CG scalars from a reduced total: mode 0 t = p^+ A p -> alpha;
-// mode 1 t = |r|^2 -> beta and the residual history
-__device__ __forceinline__ void cg_scalars_from(double t, double *s, int mode, int hist)
-{
-  if (mode == 0) {
-    s[S_PAP] = t;
-    s[S_ALPHA] = t > 0.0 ? s[S_RR] / t : nan("");  // p^+ A p <= 0: breakdown
-  } else {
-    s[S_RRNEW] = t;
-    s[S_BETA] = t / s[S_RR];
-    s[S_RR] = t;
-    s[S_HIST + hist] = t;
-  }
-}
-
-// Called by every thread of a 128-thread block after block_partial wrote the
-// block's partial: the block that finishes last sums all gridDim.x partials
-// in index order (the same order whichever block is last), updates the
-// scalars and re-arms the counter. No block waits for another.
-__device__ __forceinline__ void cg_last_block(const double *partials, unsigned *done, double *s, int mode, int hist)
-{
-  __shared__ unsigned last;
-  __shared__ double sh[32];
-  if (threadIdx.x == 0) {
-    __threadfence();  // this block's partial before its count
-    last = atomicAdd(done, 1u) == gridDim.x - 1 ? 1u : 0u;
-  }
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  // eight independent loads in flight per thread, summed in a fixed order
-  const int n = (int)gridDim.x;
-  double v = 0.0;
-  const int nt = (int)blockDim.x;
-  for (int i0 = threadIdx.x; i0 < n; i0 += 8 * nt) {
-    double w[8];
-#pragma unroll
-    for (int k = 0; k < 8; k++) w[k] = i0 + k * nt < n ? __ldcg(partials + i0 + k * nt) : 0.0;
-#pragma unroll
-    for (int k = 0; k < 8; k++) v += w[k];
-  }
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int i = 0; i < nt >> 5; i++) t += sh[i];
-    cg_scalars_from(t, s, mode, hist);
-    *done = 0u;
-  }
-}
 
 // The two fused reductions run kCgSpt sites per thread in blocks of
 // kCgThreads: fewer blocks, so the last block sums fewer partials.
@@ -158,44 +105,6 @@ __global__ void __launch_bounds__(128) k_cg_p(void *ps, float *psn, const void *
 
 // per-block Re <a, b> (used for p^+ A p when the storage rounds D p: with
 // FP16 fields A p = D^+ round(D p), and |D p|^2 would not match it)
-template <int P, typename R>
-__global__ void __launch_bounds__(kCgThreads) k_dot_re(const void *a, const float *an, const void *b, const float *bn,
-                                                       int64_t stride, int V, double *partials, double *s,
-                                                       unsigned *done, int hist)
-{
-  double d = 0.0;
-#pragma unroll
-  for (int i = 0; i < kCgSpt; i++) {
-  const int x = (int)(blockIdx.x * kCgSites + i * kCgThreads + threadIdx.x);
-  if (x < V) {
-    C<R> va[12], vb[12];
-    Spinor<P, R>::load(a, an, stride, x, va);
-    Spinor<P, R>::load(b, bn, stride, x, vb);
-    R t = (R)0;
-#pragma unroll
-    for (int k = 0; k < 12; k++) t += va[k].re * vb[k].re + va[k].im * vb[k].im;
-    d += (double)t;  // per-site sum in the working precision, block sum in double
-  }
-  }
-  block_partial(d, partials);
-  cg_last_block(partials, done, s, 0, hist);
-}
-
-// one block: sum n partials in a fixed order and update the scalars
-__global__ void k_cg_scalars(const double *partials, int n, double *s, int mode, int hist)
-{
-  double v = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) v += partials[i];
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  __shared__ double sh[32];
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int i = 0; i < (int)(blockDim.x >> 5); i++) t += sh[i];
-    cg_scalars_from(t, s, mode, hist);
-  }
-}
 
 #define QG_PREC_DISPATCH(prec, KERNEL, ...)                                          \
   do {                                                                               \
@@ -208,8 +117,9 @@ __global__ void k_cg_scalars(const double *partials, int n, double *s, int mode,
 // Operators of the system A y = c that cgnr_core solves through A^+ A.
 struct CgOps {
   int L[4];  // lattice of the system's fields (the half lattice for even/odd)
-  // inner precision: t = A p (with partials: |t|^2 per 128-site block), aps = A^+ t
-  std::function<bool(qcdgpu_field, qcdgpu_field, double *)> op;
+  // inner precision: t = A p (with partials: |t|^2 per 128-site block, and
+  // with fuse the CG step from them), aps = A^+ t
+  std::function<bool(qcdgpu_field, qcdgpu_field, double *, const CgFuse *)> op;
   std::function<bool(qcdgpu_field, qcdgpu_field)> opdag;
   // FP64 storage (accurate arithmetic): out = A in, out = A^+ in
   std::function<bool(qcdgpu_field, qcdgpu_field)> op64, opdag64;
@@ -349,19 +259,10 @@ static int cgnr_core(qcdgpu_field y, qcdgpu_field c, double cn, const CgOps &ops
         if (!QG_LAUNCHED("cg_p")) return false;
       }
       first = false;
-      if (prec != QCDGPU_F16) {
-        // p^+ A^+ A p = |A p|^2 summed in the epilogue of the first operator
-        if (!ops.op(t, ps, part)) return false;
-        k_cg_scalars<<<1, 256, 0, st>>>(part, (int)nb, s, 0, j);
-        if (!QG_LAUNCHED("cg_scalars")) return false;
-        if (!ops.opdag(aps, t)) return false;
-      } else {
-        if (!ops.op(t, ps, nullptr) || !ops.opdag(aps, t)) return false;
-        // p^+ A p and alpha in one launch
-        k_dot_re<QCDGPU_F16, float><<<nbr, kCgThreads, 0, st>>>(ps->data, ps->norm, aps->data, aps->norm, ps->stride, V,
-                                                                 part, s, done, j);
-        if (!QG_LAUNCHED("cg_dot")) return false;
-      }
+      // p^+ A^+ A p = |A p|^2, summed in the epilogue of the first operator;
+      // its last block forms alpha
+      const CgFuse fz{done, s, j};
+      if (!ops.op(t, ps, part, &fz) || !ops.opdag(aps, t)) return false;
 #define QG_CG_UPD(P, R)                                                                                           \
   k_cg_update<P, R><<<nbr, kCgThreads, 0, st>>>(xs->data, xs->norm, ps->data, ps->norm, rs->data, rs->norm, aps->data, \
                                                 aps->norm, xs->stride, V, s, part, done + 1, j)
@@ -454,8 +355,8 @@ int solve_cgnr_engine(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4
   if (!bd || !gi) return 3;
   CgOps ops;
   memcpy(ops.L, b->L, sizeof(ops.L));
-  ops.op = [&](qcdgpu_field o, qcdgpu_field i, double *part) {
-    return dslash_partials(o, i, gi, mp4, tm, false, -1, part);
+  ops.op = [&](qcdgpu_field o, qcdgpu_field i, double *part, const CgFuse *fuse) {
+    return dslash_partials(o, i, gi, mp4, tm, false, -1, part, fuse);
   };
   ops.opdag = [&](qcdgpu_field o, qcdgpu_field i) { return dslash_partials(o, i, gi, mp4, tm, true, -1, nullptr); };
   ops.op64 = [&](qcdgpu_field o, qcdgpu_field i) { return dslash(o, i, g, mp4, tm, QCDGPU_OP_D, QCDGPU_ARITH_DF64); };
@@ -503,9 +404,9 @@ int solve_cgnr_eo(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, do
   CgOps ops;
   memcpy(ops.L, Lh, sizeof(ops.L));
   const int ar = QCDGPU_ARITH_DF64;  // FP64 fields: float-float arithmetic
-  ops.op = [&](qcdgpu_field o, qcdgpu_field i, double *part) {
+  ops.op = [&](qcdgpu_field o, qcdgpu_field i, double *part, const CgFuse *fuse) {
     return dslash_eo(ti, i, nullptr, gi, mp4, tm, false, 1, 1.0, true, 0, nullptr, ar) &&
-           dslash_eo(o, ti, i, gi, mp4, tm, false, 0, -0.25, false, 2, part, ar);
+           dslash_eo(o, ti, i, gi, mp4, tm, false, 0, -0.25, false, 2, part, ar, fuse);
   };
   ops.opdag = [&](qcdgpu_field o, qcdgpu_field i) {
     return dslash_eo(ti, i, nullptr, gi, mp4, tm, true, 1, 1.0, true, 0, nullptr, ar) &&

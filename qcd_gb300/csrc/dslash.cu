@@ -39,10 +39,15 @@ static bool launch_native(const DArgs &a, int prec, int recon)
 // the host layout at these device addresses instead of in / out's data
 static bool dslash_once(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4, double tm,
                         bool dag, bool q, int arith, double *partials = nullptr, int x0 = 0, int x1 = -1,
-                        const void *in_aos = nullptr, void *out_aos = nullptr)
+                        const void *in_aos = nullptr, void *out_aos = nullptr, const CgFuse *fuse = nullptr)
 {
   DArgs a;
   a.partials = partials;
+  if (partials && fuse) {
+    a.cg_done = fuse->done;
+    a.cg_s = fuse->s;
+    a.cg_hist = fuse->hist;
+  }
   a.x0 = x0;
   a.out = out->data;
   a.out_norm = out->norm;
@@ -139,7 +144,7 @@ bool dslash(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4, doubl
 // with A = mp4 + i tm g5 (D^+: tm -> -tm and the hopping term of D^+).
 // in, out, z are fields on the half lattice {L_t / 2, L_x, L_y, L_z}.
 bool dslash_eo(qcdgpu_field out, qcdgpu_field in, qcdgpu_field z, qcdgpu_gauge g, double mp4, double tm, bool dag,
-               int par, double ch, bool ainv, int zmode, double *partials, int arith)
+               int par, double ch, bool ainv, int zmode, double *partials, int arith, const CgFuse *fuse)
 {
   if (!out || !in || !g || out == in || (zmode && (!z || z == out)) || in->prec != out->prec ||
       in->prec != g->prec || (z && z->prec != in->prec) || g->L[0] % 2 != 0 || in->L[0] * 2 != g->L[0] ||
@@ -150,6 +155,11 @@ bool dslash_eo(qcdgpu_field out, qcdgpu_field in, qcdgpu_field z, qcdgpu_gauge g
   }
   DArgs a;
   a.partials = partials;
+  if (partials && fuse) {
+    a.cg_done = fuse->done;
+    a.cg_s = fuse->s;
+    a.cg_hist = fuse->hist;
+  }
   a.x0 = 0;
   a.out = out->data;
   a.out_norm = out->norm;
@@ -251,12 +261,13 @@ bool dslash_sites_aos(void *out_aos, const void *in_aos, qcdgpu_field shape, qcd
 
 // out = D in (dag: D^+ in) on fields checked by the caller; when partials is
 // non-null, block b of the launch (128 sites each) also writes the sum of
-// |out|^2 over its sites to partials[b]
+// |out|^2 over its sites to partials[b], and with fuse the block that
+// finishes last forms the CG step from them
 bool dslash_partials(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4, double tm, bool dag,
-                     int arith, double *partials)
+                     int arith, double *partials, const CgFuse *fuse)
 {
   if (arith < 0) arith = g_f64_arith;
-  return dslash_once(out, in, g, mp4, tm, dag, false, arith, partials);
+  return dslash_once(out, in, g, mp4, tm, dag, false, arith, partials, 0, -1, nullptr, nullptr, fuse);
 }
 
 int g_f64_arith = QCDGPU_ARITH_F64;

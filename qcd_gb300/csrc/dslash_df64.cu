@@ -482,7 +482,7 @@ __global__ void __launch_bounds__(384, 3) k_wilson_ff(const DArgs a)
   const int x = ff_site<EO>(a, e, act, c);
   extern __shared__ double2 ff_stage[];
   const double n2 = group_ff<DAG, EO, AOS>(a, grp, col, lane, e, act, x, c, hs, ff_stage);
-  if (a.partials) block_partial(n2, a.partials);
+  if (a.partials) block_partial_cg(n2, a);
 }
 
 // ------------------------------------------------------ float-pair links

@@ -147,8 +147,12 @@ bool dslash(qcdgpu_field out, qcdgpu_field in, qcdgpu_gauge g, double mp4, doubl
 // even/odd kernel on half fields {L_t/2, L_x, L_y, L_z} (native arithmetic):
 // out (parity par) = ch * [A^{-1}] H in + {0 | z | A z}, A = mp4 + i tm g5
 // arith: QCDGPU_ARITH_DF64 runs FP64 fields in float-float arithmetic
+// with partials and fuse, the block that finishes last also forms the CG
+// step alpha from the partials (dslash_args.h: CgFuse)
+struct CgFuse;
 bool dslash_eo(qcdgpu_field out, qcdgpu_field in, qcdgpu_field z, qcdgpu_gauge g, double mp4, double tm, bool dag,
-               int par, double ch, bool ainv, int zmode, double *partials, int arith = QCDGPU_ARITH_F64);
+               int par, double ch, bool ainv, int zmode, double *partials, int arith = QCDGPU_ARITH_F64,
+               const CgFuse *fuse = nullptr);
 
 // cg.cu: even/odd helpers -- full FP64 field <-> its two half fields, and
 // out = A in or A^{-1} in on a half field (A = mp4 + i tm g5)

@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(128) k_wilson(const DArgs a)
       n2 = (double)s2;
     }
   }
-  if (a.partials) block_partial(n2, a.partials);
+  if (a.partials) block_partial_cg(n2, a);
 }
 
 // Even/odd kernel: thread e handles the site of parity a.eo_par whose full
@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(128) k_wilson_eo(const DArgs a)
       n2 = (double)s2;
     }
   }
-  if (a.partials) block_partial(n2, a.partials);
+  if (a.partials) block_partial_cg(n2, a);
 }
 
 }  // namespace qg
