@@ -247,7 +247,11 @@ int qcdgpu_set_stream(void *stream);
 int qcdgpu_sync(void);
 /* restore invert.c's shipped GCR update (1) or the algorithm's (0, default) */
 void qcdgpu_set_gcr_compat(int shipped);
-/* arithmetic of the FP64 operator used by the Part-2 entry points */
+/* arithmetic of the FP64 operator used by the qcd.h entry points, the FP64
+ * solvers and qcdgpu_dslash with arith < 0. Default QCDGPU_ARITH_DF64:
+ * float-float on the FP32 pipes, 3.6x the native rate on GB300 at the same
+ * per-site parity (<= 1e-13); |x| below 2^-1022 counts as zero there.
+ * QCDGPU_ARITH_F64 selects native IEEE double. */
 int qcdgpu_set_f64_arith(int arith);
 /* slabs of the pipelined host-buffer operator apply (0: automatic, the largest
  * of 24, 16, 12, 8, 6, 4, 3 dividing L_z; otherwise a divisor of L_z, >= 3);

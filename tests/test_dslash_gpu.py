@@ -92,7 +92,7 @@ def test_pipelined_host_apply_matches_oracle(gpu, orc, arith):
             assert site_rel_err(Dv.a, ref_q) <= TOL64, S
     finally:
         lib.qcdgpu_set_pipeline_slabs(0)
-        lib.qcdgpu_set_f64_arith(q.ARITH_F64)
+        lib.qcdgpu_set_f64_arith(q.ARITH_DF64)  # the library default
         for o in (v, Dv, u):
             o.close()
         geo.close()
