@@ -336,7 +336,7 @@ __device__ __forceinline__ void mhop_pair(const MArgs &a, int x, const int c[4],
 // out = A^{-1} H in; MODE 2 out = A z - H in / 4 (the two halves of the Schur
 // complement). The epilogue is fixed at compile time for each mode.
 template <bool DAG, int RP, int MODE>
-__global__ void __launch_bounds__(256) k_wilson_mrhs_simt(const MArgs a, double *partials)
+__global__ void __launch_bounds__(256, 2) k_wilson_mrhs_simt(const MArgs a, double *partials)
 {
   constexpr bool EO = MODE != 0;
   const int r0 = threadIdx.x * RP;
