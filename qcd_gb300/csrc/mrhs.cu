@@ -986,17 +986,43 @@ struct MrhsTune {
 static int g_mrhs_variant = MRHS_AUTO;
 static std::map<std::pair<int64_t, int>, MrhsTune> g_mrhs_tuned;
 
-// block (N / rp slot threads, sites per block)
+// block (N / rp slot threads, sites per block). `threads` / N sites is the
+// target; of the counts from half to twice that (at least up to 4, at most
+// 256 threads) the one that leaves the fewest idle lanes in the block's last
+// warp is taken, the nearest to the target on a tie (48 slots at two per
+// thread: 4 sites of 24 threads fill three warps, where 1 site leaves a
+// quarter of its warp idle)
 static dim3 simt_block(int N, int threads, int rp = 1)
 {
+  const int x = (N + rp - 1) / rp;  // threads per site
   const int sb = threads / N > 0 ? threads / N : 1;
-  return dim3((unsigned)((N + rp - 1) / rp), (unsigned)sb);
+  const int hi = 2 * sb > 4 ? 2 * sb : 4;
+  int best = sb;
+  int best_idle = 1 << 30, best_warps = 1;
+  for (int c = sb / 2 > 1 ? sb / 2 : 1; c <= hi && x * c <= 256; c++) {
+    const int t = x * c, warps = (t + 31) / 32, idle = warps * 32 - t;
+    // idle / (32 warps) compared exactly: fewer idle lanes per lane, then nearer the target
+    const long long lhs = (long long)idle * best_warps, rhs = (long long)best_idle * warps;
+    if (best_idle == 1 << 30 || lhs < rhs || (lhs == rhs && abs(c - sb) < abs(best - sb))) {
+      best = c;
+      best_idle = idle;
+      best_warps = warps;
+    }
+  }
+  return dim3((unsigned)x, (unsigned)best);
 }
 
+// the largest block count of any shape that writes per-slot partial sums
 unsigned mrhs_max_blocks(int64_t V, int N)
 {
-  const dim3 b = simt_block(N, 64);  // the smallest sites-per-block of any shape
-  return (unsigned)((V + b.y - 1) / b.y);
+  unsigned m = 0;
+  for (int threads : {64, 128, 256})
+    for (int rp : {1, 2}) {
+      const dim3 b = simt_block(N, threads, rp);
+      const unsigned nb = (unsigned)((V + b.y - 1) / b.y);
+      if (nb > m) m = nb;
+    }
+  return m;
 }
 
 static bool launch_mrhs(const MArgs &a, bool dag, MrhsTune t, double *partials, unsigned *nblocks)
