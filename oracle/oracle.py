@@ -25,19 +25,25 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libqcdref.so")
-REF_TREE = "/root/reference"
+# where the reference's source tree lies, for `make ref`: the build entry
+# point passes it (environment variable QCD_REFERENCE_TREE)
+REF_TREE_ENV = "QCD_REFERENCE_TREE"
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 
 
-def build(with_ref: bool | None = None) -> None:
-    """Compile the restatement and, when the reference tree exists, the reference."""
+def build(with_ref: bool | None = None, ref_tree: str | None = None) -> None:
+    """Compile the restatement and, when a reference source tree is given
+    (``ref_tree`` or $QCD_REFERENCE_TREE) and exists, the reference."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    ref_tree = ref_tree or os.environ.get(REF_TREE_ENV)
     if with_ref is None:
-        with_ref = os.path.isdir(REF_TREE)
+        with_ref = bool(ref_tree) and os.path.isdir(ref_tree)
     if with_ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_TREE}"], check=True)
+        if not ref_tree:
+            raise RuntimeError(f"building the reference needs its source tree (${REF_TREE_ENV})")
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_tree}"], check=True)
 
 
 def _L(L):
@@ -64,6 +70,8 @@ class Oracle:
             f = getattr(lib, name)
             f.argtypes = [_dp, _dp, _dp, _ip, _dp, C.c_double, C.c_double]
             f.restype = None
+        lib.orc_dslash_fast.argtypes = [_dp, _dp, _dp, _ip, _dp, C.c_double, C.c_double]
+        lib.orc_dslash_fast.restype = C.c_int
         lib.orc_gamma5.argtypes = [_dp, _dp, C.c_size_t]
         lib.orc_norm.argtypes = [_dp, C.c_size_t]
         lib.orc_norm.restype = C.c_double
@@ -110,6 +118,18 @@ class Oracle:
         out = np.empty_like(v)
         f = {"D": self.lib.orc_dslash, "Q": self.lib.orc_qop, "Ddag": self.lib.orc_dslash_dag}[op]
         f(out, np.ascontiguousarray(v), np.ascontiguousarray(u), _L(L), _th(theta), m, tm)
+        return out
+
+    def dslash_fast(self, v, u, L, theta, kappa=None, m=None, tm=0.0, out=None):
+        """D v by the timed CPU baseline (qcd_cpu_timing.c: the reference's
+        half-spinor algorithm at -O3); not the parity checker"""
+        if m is None:
+            m = 1.0 / (2.0 * kappa) - 4.0
+        if out is None:
+            out = np.empty_like(v)
+        rc = self.lib.orc_dslash_fast(out, v, u, _L(L), _th(theta), m, tm)
+        if rc != 0:
+            raise MemoryError("orc_dslash_fast: neighbour tables not allocated")
         return out
 
     def gamma5(self, v):

@@ -182,3 +182,46 @@ def test_twop_oracle_matches_golden(orc, golden, case):
     corr = orc.twop_proton(prop(cu), prop(cd), L, tuple(int(x) for x in g["xsrc"]), int(g["t0"]), int(g["t1"]),
                            TWOP_MOMS)
     assert np.max(np.abs(corr - g["corr"])) <= 2e-6 * np.max(np.abs(g["corr"]))
+
+
+@pytest.mark.parametrize("case", ["wilson_L6442", "wilson_L4444_theta"])
+def test_timed_cpu_operator_matches_golden(orc, golden, case):
+    """the CPU baseline's timed operator (half-spinor algorithm, -O3) computes
+    the reference's D: golden outputs of qcd_applyWilsonTMOp at 1e-13 per site"""
+    g = golden[case]
+    L, th, kappa, tm = g["L"], g["theta"], float(g["kappa"]), float(g["tm"])
+    out = orc.dslash_fast(g["v"], g["u"], L, th, m=1.0 / (2.0 * kappa) - 4.0, tm=tm)
+    assert site_rel_err(out, g["out_TMOp"]) <= TOL
+
+
+def test_timed_cpu_operator_vs_checker_all_phases(orc):
+    L, th = (6, 4, 2, 4), (np.pi, 0.4, -0.3, 1.1)
+    u = orc.gauge_synthetic(L, 9, 0.43374)
+    v = orc.gaussian_spinor(L, 10)
+    for tm in (0.0, 0.21):
+        assert site_rel_err(orc.dslash_fast(v, u, L, th, kappa=0.14, tm=tm),
+                            orc.dslash(v, u, L, th, kappa=0.14, tm=tm)) <= TOL
+
+
+def test_timed_cpu_operator_runs_at_the_reference_speed(orc, ref):
+    """the CPU baseline times the reference's algorithm, not a slower one: on
+    the benchmark's 24^3 x 48 lattice, on this core, its apply takes within
+    15% of the reference's own qcd_applyWilsonTMOp (best of three each,
+    interleaved)"""
+    import time
+
+    L, th = (48, 24, 24, 24), (np.pi, 0.0, 0.0, 0.0)
+    u = orc.gauge_synthetic(L, 1000, 0.43374)
+    v = orc.gaussian_spinor(L, 2000)
+    out = np.empty_like(v)
+    t_fast, t_ref = [], []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        orc.dslash_fast(v, u, L, th, kappa=0.15, out=out)
+        t_fast.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        r = ref.dslash(v, u, L, th, kappa=0.15)
+        t_ref.append(time.perf_counter() - t0)
+    assert site_rel_err(out, r) <= TOL
+    ratio = min(t_fast) / min(t_ref)
+    assert 0.85 <= ratio <= 1.15, (min(t_fast), min(t_ref))
