@@ -163,6 +163,27 @@ qcd_real_8 qcd_normVector(qcd_vector *vec);
 /* include/qcd_gamma.h (lib/src/qcd_gamma.c:521) */
 void qcd_gamma5Vector(qcd_vector *v);
 
+/* include/qcd_wilson.h:628-633 (lib/src/qcd_wilson.c:18-103): host helpers
+ * on one site's spin-colour vector [4][3]. (1 +- gamma_mu) vec for mu = 0..5
+ * (gamma_4 = -gamma_0, gamma_5 in slot 5, as the reference's tables; other mu
+ * leave result untouched); U vec and U^+ vec for a 3 x 3 colour matrix on
+ * every spin; (mp4 + i tm gamma_5) vec; vec * phi in place. */
+void qcd_onePlusGamma(qcd_complex_16 result[][3], qcd_complex_16 vec[][3], qcd_uint_2 mu);
+void qcd_oneMinusGamma(qcd_complex_16 result[][3], qcd_complex_16 vec[][3], qcd_uint_2 mu);
+void qcd_applyU(qcd_complex_16 result[][3], qcd_complex_16 u[][3], qcd_complex_16 vec[][3]);
+void qcd_applyUDagger(qcd_complex_16 result[][3], qcd_complex_16 u[][3], qcd_complex_16 vec[][3]);
+void qcd_massTerms(qcd_complex_16 result[][3], qcd_complex_16 vec[][3], qcd_real_8 mp4, qcd_real_8 tm);
+void qcd_phaseMul(qcd_complex_16 vec[][3], qcd_complex_16 phi);
+
+/* include/qcd_stochastic.h:5 (lib/src/qcd_stochastic.c:8-58): vec <- Z4
+ * noise {1, i, -1, -i}, independent per site and spin-colour component, on
+ * time-slice t_slice (every site when t_slice < 0; zero when t_slice is past
+ * the lattice), generated on the GPU. The reference draws from GSL's ranlux;
+ * this library draws every call a new vector from its own counter-based
+ * stream, restarted by qcdgpu_set_noise_seed. Errors: qcdgpu_last_error. */
+void qcd_z2Vector(qcd_vector *vec, int t_slice);
+int qcdgpu_set_noise_seed(uint64_t seed);
+
 /* Source construction, computed on the GPU.
  * include/qcd_smearing.h:41 (lib/src/qcd_smearing.c:209): one 3D APE step,
  * apeu_mu = Proj_SU3(u_mu + alpha * spatial staples) for mu = 1..3, temporal
@@ -296,6 +317,10 @@ int qcdgpu_field_store(qcdgpu_field f, double *host);
 /* device-to-device copy with precision conversion */
 int qcdgpu_field_copy(qcdgpu_field dst, qcdgpu_field src);
 int qcdgpu_field_gaussian(qcdgpu_field f, uint64_t seed);
+/* noise source (no reference counterpart beyond qcd_z2Vector): kind 4 = Z4
+ * {1, i, -1, -i}, kind 2 = Z2 {1, -1} per spin-colour component, on
+ * time-slice t_slice (all sites when negative), from the seeded stream */
+int qcdgpu_field_noise(qcdgpu_field f, uint64_t seed, int t_slice, int kind);
 int qcdgpu_field_point(qcdgpu_field f, const int x[4], int spin, int colour);
 /* bytes of device memory the field occupies */
 size_t qcdgpu_field_bytes(qcdgpu_field f);
@@ -342,6 +367,16 @@ enum {
 int qcdgpu_solve(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double kappa, double mu,
                  qcdgpu_solve_params *p);
 
+/* Solvers keep their work fields in a pool between calls; this frees the
+ * pool's device memory (the next solve allocates again). Returns 0. */
+int qcdgpu_release_work(void);
+/* Fault injection for tests (no reference counterpart): the next n
+ * allocations of host vectors and gauge fields (qcd_initVector,
+ * qcd_initGaugeField) and of device fields and gauge fields fail as if memory
+ * were exhausted, so that callers' out-of-memory paths run without
+ * exhausting memory; n = 0 switches it off. */
+int qcdgpu_inject_alloc_failures(int n);
+
 /* No counterpart in the reference. The complex dot product
  * result[0] + i result[1] = sum_i conj(a_i) b_i, for callers that cannot
  * allocate device memory (their device heap belongs to a framework's
@@ -355,10 +390,6 @@ int qcdgpu_solve(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double kappa, d
  * message), and calls that overlap on the GPU race on that array. The first
  * call on each device looks the array's address up; make it before any
  * stream capture. Returns 0, or 1 on error (qcdgpu_last_error). */
-/* Solvers keep their work fields in a pool between calls; this frees the
- * pool's device memory (the next solve allocates again). Returns 0. */
-int qcdgpu_release_work(void);
-
 int qcdgpu_dot_noalloc(const double *a, const double *b, int64_t n, double *result, void *stream);
 
 /* Source construction on device fields (FP64): n APE steps out <- in (out
@@ -416,9 +447,19 @@ int qcdgpu_set_mrhs_variant(int variant);
 /* the tuned choice for (L, nrhs): variant 0 SIMT / 1 mma.sync / 2 tcgen05
  * and the SIMT block size; returns 1 when nothing has been tuned for it yet */
 int qcdgpu_mrhs_tuned(const int L[4], int nrhs, int *variant, int *threads);
-/* *n = tiles the tcgen05 kernel abandoned after its bounded wait for the
- * tensor cores ran out (0 unless the hardware stalled) */
+/* Every wait of the tcgen05 kernel for its MMAs is bounded. A wait that runs
+ * out makes the launch abandon its work (its output is invalid) and sets a
+ * failure flag: from then on the multi-RHS operator (qcdgpu_dslash_mrhs and
+ * the batches' operator calls), the next chunk boundary of a batch and
+ * qcdgpu_sync return 1 with a message, until qcdgpu_mrhs_tc_reset clears the
+ * flag. qcdgpu_mrhs_tc_timeouts synchronises the stream and gives *n = the
+ * abandoned tiles since the last reset (0 unless the hardware stalled). */
 int qcdgpu_mrhs_tc_timeouts(unsigned *n);
+int qcdgpu_mrhs_tc_reset(void);
+/* Test hook: with skip_mma != 0 the tcgen05 kernel issues no MMA, so its
+ * waits run out after `polls` mbarrier polls and the launch reports the
+ * timeout; (0, 0) restores normal operation (2^24 polls). */
+int qcdgpu_mrhs_tc_test_hook(int skip_mma, int polls);
 
 /* Batched solver with continuous admission (no reference counterpart). A
  * batch of `capacity` slots (1..64) runs mixed-precision CG on the normal

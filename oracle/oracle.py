@@ -106,6 +106,7 @@ class Oracle:
         lib.orc_gauss.restype = C.c_double
         lib.orc_gaussian_spinor.argtypes = [_dp, C.c_size_t, C.c_uint64]
         lib.orc_z4_spinor.argtypes = [_dp, C.c_size_t, C.c_uint64]
+        lib.orc_noise_spinor.argtypes = [_dp, _ip, C.c_uint64, C.c_int, C.c_int]
         lib.orc_gauge_synthetic.argtypes = [_dp, _ip, C.c_uint64, C.c_double]
         lib.orc_gauge_unit.argtypes = [_dp, C.c_size_t]
         lib.orc_twop_proton.argtypes = [_dp, _dp, _ip, _ip, C.c_int, C.c_int, _ip, C.c_int, _dp]
@@ -229,6 +230,11 @@ class Oracle:
     def gaussian_spinor(self, L, seed):
         v = np.empty((volume(L), 4, 3, 2))
         self.lib.orc_gaussian_spinor(v, volume(L), seed)
+        return v
+
+    def noise_spinor(self, L, seed, t_slice=-1, kind=4):
+        v = np.empty((volume(L), 4, 3, 2))
+        self.lib.orc_noise_spinor(v, _L(L), seed, t_slice, kind)
         return v
 
     def z4_spinor(self, L, seed):

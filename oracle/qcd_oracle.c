@@ -720,6 +720,29 @@ void orc_gaussian_spinor(double *v, size_t V, uint64_t seed)
 /* Z4 noise {+1,+i,-1,-i} per spin-colour component on every site, the
  * values of qcd_z2Vector (lib/src/qcd_stochastic.c:8-58); the stream is this
  * generator's (the reference draws from GSL's ranlux, absent here). */
+/* Z4 (kind 4) or Z2 (kind 2) noise on time-slice ts (all sites when ts < 0),
+ * the stochastic source of lib/src/qcd_stochastic.c:8-58 drawn from this
+ * counter-based stream instead of GSL's ranlux: component k of site l from
+ * counter 12 l + k (Z4: top two bits; Z2: top bit) */
+void orc_noise_spinor(double *v, const int L[4], uint64_t seed, int ts, int kind)
+{
+  size_t V = vol(L);
+  static const double re[4] = {1, 0, -1, 0}, im[4] = {0, 1, 0, -1};
+  for (size_t l = 0; l < V; l++)
+    for (int k = 0; k < 12; k++) {
+      size_t i = l * 12 + k;
+      uint64_t b = orc_rng_bits(seed, i);
+      if (ts >= 0 && (int)(l % (size_t)L[0]) != ts) {
+        v[2 * i] = 0.0; v[2 * i + 1] = 0.0;
+      } else if (kind == 2) {
+        v[2 * i] = (b >> 63) ? -1.0 : 1.0; v[2 * i + 1] = 0.0;
+      } else {
+        unsigned r = (unsigned)(b >> 62);
+        v[2 * i] = re[r]; v[2 * i + 1] = im[r];
+      }
+    }
+}
+
 void orc_z4_spinor(double *v, size_t V, uint64_t seed)
 {
   for (size_t i = 0; i < V * 12; i++) {

@@ -84,6 +84,8 @@ DROPIN_SYMBOLS = [
     "qcd_zeroVector", "qcd_setVector", "qcd_copyVector", "qcd_mulVectorC", "qcd_scaleVector",
     "qcd_subVector", "qcd_addVector", "qcd_axpyVector", "qcd_mulAdjointVectorVector",
     "qcd_normVector", "qcd_gamma5Vector", "qcd_communicateVectorPMGaugeP", "qcd_waitall",
+    "qcd_onePlusGamma", "qcd_oneMinusGamma", "qcd_applyU", "qcd_applyUDagger", "qcd_massTerms", "qcd_phaseMul",
+    "qcd_z2Vector",
     "gcr", "bicgstab", "cgnr",
 ]
 
@@ -156,6 +158,20 @@ def lib() -> C.CDLL:
     L.qcdgpu_field_copy.argtypes = [C.c_void_p, C.c_void_p]
     L.qcdgpu_field_gaussian.argtypes = [C.c_void_p, C.c_uint64]
     L.qcdgpu_field_point.argtypes = [C.c_void_p, _ip, C.c_int, C.c_int]
+    L.qcdgpu_field_noise.argtypes = [C.c_void_p, C.c_uint64, C.c_int, C.c_int]
+    L.qcd_z2Vector.argtypes = [vp, C.c_int]
+    L.qcd_z2Vector.restype = None
+    L.qcdgpu_set_noise_seed.argtypes = [C.c_uint64]
+    for n in ("qcd_onePlusGamma", "qcd_oneMinusGamma"):
+        getattr(L, n).argtypes = [_dp, _dp, C.c_uint16]
+        getattr(L, n).restype = None
+    for n in ("qcd_applyU", "qcd_applyUDagger"):
+        getattr(L, n).argtypes = [_dp, _dp, _dp]
+        getattr(L, n).restype = None
+    L.qcd_massTerms.argtypes = [_dp, _dp, C.c_double, C.c_double]
+    L.qcd_massTerms.restype = None
+    L.qcd_phaseMul.argtypes = [_dp, QcdComplex16]
+    L.qcd_phaseMul.restype = None
     L.qcdgpu_field_bytes.argtypes = [C.c_void_p]
     L.qcdgpu_field_bytes.restype = C.c_size_t
     L.qcdgpu_field_data.argtypes = [C.c_void_p]
@@ -182,6 +198,8 @@ def lib() -> C.CDLL:
                                         C.c_double, C.c_int]
     L.qcdgpu_set_mrhs_variant.argtypes = [C.c_int]
     L.qcdgpu_mrhs_tuned.argtypes = [_ip, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.qcdgpu_mrhs_tc_timeouts.argtypes = [C.POINTER(C.c_uint)]
+    L.qcdgpu_mrhs_tc_test_hook.argtypes = [C.c_int, C.c_int]
     L.qcdgpu_server_create.argtypes = [vpp, C.c_size_t, C.c_int]
     L.qcdgpu_server_destroy.argtypes = [C.c_void_p]
     L.qcdgpu_server_add_gauge.argtypes = [C.c_void_p, C.c_void_p]
@@ -309,6 +327,11 @@ class Field:
 
     def gaussian(self, seed: int) -> "Field":
         _check(lib().qcdgpu_field_gaussian(self.h, seed), "field_gaussian")
+        return self
+
+    def noise(self, seed: int, t_slice: int = -1, kind: int = 4) -> "Field":
+        """Z4 (kind 4) or Z2 (kind 2) noise on time-slice t_slice (all sites when negative)"""
+        _check(lib().qcdgpu_field_noise(self.h, seed, t_slice, kind), "field_noise")
         return self
 
     def point(self, x, spin, colour) -> "Field":

@@ -38,6 +38,7 @@ static std::unordered_set<const void *> g_pinned;  // host blocks from cudaMallo
 
 static void *host_alloc(size_t bytes)
 {
+  if (alloc_fault()) return nullptr;
   void *p = nullptr;
   if (cudaMallocHost(&p, bytes) == cudaSuccess) {
     g_pinned.insert(p);
@@ -618,6 +619,111 @@ void qcd_gamma5Vector(qcd_vector *v)
   if (f && blas_gamma5(f, f)) vec_done(v);
 }
 
+// ------------------------------------------------------------- noise
+// The reference's qcd_z2Vector (lib/src/qcd_stochastic.c:8-58) fills a vector
+// with Z4 noise {1, i, -1, -i} on one time-slice (every site when t_slice < 0;
+// a zero vector when t_slice is past the lattice) from GSL's ranlux stream.
+// Here every call draws a new vector from the library's own counter-based
+// stream: key (seed, call number), counter 12 x + spin-colour component.
+static uint64_t g_noise_seed = 1, g_noise_calls = 0;
+
+void qcd_z2Vector(qcd_vector *vec, int t_slice)
+{
+  QG_BLAS_GUARD;
+  qcdgpu_field f = vec_out(vec);
+  const uint64_t seed = g_noise_seed * 0x9E3779B97F4A7C15ull + g_noise_calls++;
+  if (f && field_noise(f, seed, t_slice, 4)) vec_done(vec);
+}
+
+// --------------------------------------------- per-site operator helpers
+// lib/src/qcd_wilson.c:18-103 (include/qcd_wilson.h:628-633): host functions
+// on one site's 4 x 3 spin-colour vector. gamma_mu (mu = 0..5) in the chiral
+// basis of qcd_gamma.c:46-103 (gamma_4 = -gamma_0, gamma_5 = diag(1, 1, -1,
+// -1)); each row has one non-zero entry: column kGamCol[mu][row], value
+// kGamVal[mu][row] in {1, -1, i, -i} as (re, im).
+static const int kGamCol[6][4] = {{2, 3, 0, 1}, {3, 2, 1, 0}, {3, 2, 1, 0}, {2, 3, 0, 1}, {2, 3, 0, 1}, {0, 1, 2, 3}};
+static const double kGamVal[6][4][2] = {{{-1, 0}, {-1, 0}, {-1, 0}, {-1, 0}}, {{0, -1}, {0, -1}, {0, 1}, {0, 1}},
+                                        {{-1, 0}, {1, 0}, {1, 0}, {-1, 0}},   {{0, -1}, {0, 1}, {0, 1}, {0, -1}},
+                                        {{1, 0}, {1, 0}, {1, 0}, {1, 0}},     {{1, 0}, {1, 0}, {-1, 0}, {-1, 0}}};
+
+static inline qcd_complex_16 cmul16(qcd_complex_16 a, qcd_complex_16 b)
+{
+  return qcd_complex_16{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+
+// result = (1 + sign gamma_mu) vec; entries are 0, +-1, +-i, so the sum of
+// the row's two terms is exact
+static void one_pm_gamma(qcd_complex_16 result[][3], qcd_complex_16 vec[][3], int mu, double sign)
+{
+  for (int al = 0; al < 4; al++) {
+    const int be = kGamCol[mu][al];
+    const qcd_complex_16 g{sign * kGamVal[mu][al][0], sign * kGamVal[mu][al][1]};
+    for (int c = 0; c < 3; c++) {
+      const qcd_complex_16 t = cmul16(g, vec[be][c]);
+      result[al][c] = qcd_complex_16{vec[al][c].re + t.re, vec[al][c].im + t.im};
+    }
+  }
+}
+
+void qcd_onePlusGamma(qcd_complex_16 result[][3], qcd_complex_16 vec[][3], qcd_uint_2 mu)
+{
+  if (mu > 5) return;
+  one_pm_gamma(result, vec, mu, 1.0);
+}
+
+void qcd_oneMinusGamma(qcd_complex_16 result[][3], qcd_complex_16 vec[][3], qcd_uint_2 mu)
+{
+  if (mu > 5) return;
+  one_pm_gamma(result, vec, mu, -1.0);
+}
+
+// result = u vec on every spin (colour matrix u[row][col])
+void qcd_applyU(qcd_complex_16 result[][3], qcd_complex_16 u[][3], qcd_complex_16 vec[][3])
+{
+  for (int al = 0; al < 4; al++)
+    for (int c1 = 0; c1 < 3; c1++) {
+      qcd_complex_16 s{0.0, 0.0};
+      for (int c2 = 0; c2 < 3; c2++) {
+        const qcd_complex_16 t = cmul16(u[c1][c2], vec[al][c2]);
+        s = qcd_complex_16{s.re + t.re, s.im + t.im};
+      }
+      result[al][c1] = s;
+    }
+}
+
+// result = u^+ vec on every spin
+void qcd_applyUDagger(qcd_complex_16 result[][3], qcd_complex_16 u[][3], qcd_complex_16 vec[][3])
+{
+  for (int al = 0; al < 4; al++)
+    for (int c1 = 0; c1 < 3; c1++) {
+      qcd_complex_16 s{0.0, 0.0};
+      for (int c2 = 0; c2 < 3; c2++) {
+        const qcd_complex_16 t = cmul16(qcd_complex_16{u[c2][c1].re, -u[c2][c1].im}, vec[al][c2]);
+        s = qcd_complex_16{s.re + t.re, s.im + t.im};
+      }
+      result[al][c1] = s;
+    }
+}
+
+// result = (mp4 + i tm gamma_5) vec
+void qcd_massTerms(qcd_complex_16 result[][3], qcd_complex_16 vec[][3], qcd_real_8 mp4, qcd_real_8 tm)
+{
+  const qcd_complex_16 itm{0.0, tm};
+  for (int al = 0; al < 4; al++)
+    for (int c = 0; c < 3; c++) {
+      const qcd_complex_16 g5v = cmul16(qcd_complex_16{kGamVal[5][al][0], 0.0}, vec[al][c]);
+      const qcd_complex_16 t = cmul16(g5v, itm);
+      result[al][c] = qcd_complex_16{vec[al][c].re * mp4 + t.re, vec[al][c].im * mp4 + t.im};
+    }
+}
+
+// vec <- vec phi
+void qcd_phaseMul(qcd_complex_16 vec[][3], qcd_complex_16 phi)
+{
+  for (int al = 0; al < 4; al++)
+    for (int c = 0; c < 3; c++) vec[al][c] = cmul16(vec[al][c], phi);
+}
+
 // -------------------------------------------------------- communication
 int qcd_communicateVectorPMGaugeP(qcd_vector *v, qcd_gaugeField *u)
 {
@@ -818,6 +924,13 @@ qcd_int_4 cgnr(qcd_vector *sol, qcd_vector *src, qcd_gaugeField *u, qcd_real_8 k
 }
 
 // ------------------------------------------------------------ residency
+int qcdgpu_set_noise_seed(uint64_t seed)
+{
+  g_noise_seed = seed;
+  g_noise_calls = 0;
+  return 0;
+}
+
 int qcdgpu_vector_make_resident(qcd_vector *v)
 {
   std::lock_guard<std::mutex> lk(g_mu);

@@ -33,6 +33,9 @@ namespace qg {
 
 // ------------------------------------------------------------------ errors
 void set_error(const char *fmt, ...);
+// true when the allocation about to be made must fail (fault injection for
+// tests, qcdgpu_inject_alloc_failures)
+bool alloc_fault();
 bool cuda_ok(cudaError_t e, const char *what);
 #define QG_CUDA(call) ::qg::cuda_ok((call), #call)
 #define QG_LAUNCHED(what) ::qg::after_launch(what)
@@ -184,6 +187,8 @@ bool blas_axpy_norm2_dev(qcdgpu_field y, double ar, double ai, qcdgpu_field x, d
 bool gauge_synthetic(qcdgpu_gauge g, uint64_t seed, double eps);
 bool field_gaussian(qcdgpu_field f, uint64_t seed);
 bool field_z4(qcdgpu_field f, uint64_t seed);
+// Z2 (kind 2) or Z4 (kind 4) noise on time-slice tslice (all when negative)
+bool field_noise(qcdgpu_field f, uint64_t seed, int tslice, int kind);
 bool field_point(qcdgpu_field f, const int x[4], int spin, int colour);
 double plaquette(qcdgpu_gauge g);
 

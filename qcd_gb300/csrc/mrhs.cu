@@ -594,6 +594,15 @@ static_assert((kTcSites - 1) * 3 * kTcSbo + 8 * kTcSbo <= kTcSmem, "tcgen05 A op
 
 __device__ unsigned g_mrhs_tc_timeouts;  // rounds abandoned after a bounded mbarrier wait
 
+// launch controls of the tensor-core kernel: the bound of each wait for the
+// MMAs (mbarrier polls), a test hook that issues no MMA (so the waits run
+// out), and a host-mapped flag the kernel sets when a wait ran out
+struct TcCtl {
+  int polls;
+  int skip_mma;
+  volatile unsigned *fail;
+};
+
 __device__ __forceinline__ uint32_t tc_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 // shared-memory matrix descriptor: no swizzle, K-major core matrices of 8
@@ -699,7 +708,7 @@ __device__ __forceinline__ void tc_h_block(const MArgs &a, int ys, int r, __half
 }
 
 template <bool DAG, int MODE>
-__global__ void __launch_bounds__(kTcThreads, 3) k_wilson_mrhs_tc(const MArgs a, double *partials)
+__global__ void __launch_bounds__(kTcThreads, 3) k_wilson_mrhs_tc(const MArgs a, double *partials, const TcCtl ctl)
 {
   extern __shared__ __align__(16) unsigned char tc_dyn[];
   unsigned char *Ls = tc_dyn, *Hs = tc_dyn + kTcLBytes;
@@ -828,7 +837,7 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_wilson_mrhs_tc(const MArgs a,
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncthreads();
-      if (tid == 0) {
+      if (tid == 0 && !ctl.skip_mma) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         constexpr uint32_t idesc = tc_idesc(64, 16);
 #pragma unroll 1
@@ -855,7 +864,7 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_wilson_mrhs_tc(const MArgs a,
       if (zmode && act) mload_rp<1>(a, EO ? a.z : a.in, EO ? a.z_norm : a.in_norm, e, r, zs, znrm);
       // bounded wait for the commit; a timeout abandons the kernel's work
       uint32_t done = 0;
-      for (int it = 0; it < (1 << 24) && !done; it++)
+      for (int it = 0; it < ctl.polls && !done; it++)
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
             : "=r"(done)
@@ -864,13 +873,16 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_wilson_mrhs_tc(const MArgs a,
       if (__syncthreads_or(!done)) {
         // the MMAs may still be in flight: wait once more, bounded, before
         // the tensor memory is released
-        for (int it = 0; it < (1 << 24) && !done; it++)
+        for (int it = 0; it < ctl.polls && !done; it++)
           asm volatile(
               "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
               : "=r"(done)
               : "r"(tc_smem(&mbar)), "r"(phase)
               : "memory");
-        if (tid == 0) atomicAdd(&g_mrhs_tc_timeouts, 1u);
+        if (tid == 0) {
+          atomicAdd(&g_mrhs_tc_timeouts, 1u);
+          *ctl.fail = 1u;
+        }
         failed = true;
         break;
       }
@@ -967,15 +979,38 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_wilson_mrhs_tc(const MArgs a,
 unsigned mrhs_tc_grid(int64_t V) { return (unsigned)((V + kTcSites * kTcTiles - 1) / (kTcSites * kTcTiles)); }
 
 template <bool D, int M>
-static void launch_tc(const MArgs &a, double *partials, unsigned grid, cudaStream_t s)
+static void launch_tc(const MArgs &a, double *partials, unsigned grid, cudaStream_t s, const TcCtl &ctl)
 {
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_wilson_mrhs_tc<D, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
     attr = true;
   }
-  k_wilson_mrhs_tc<D, M><<<grid, kTcThreads, kTcSmem, s>>>(a, partials);
+  k_wilson_mrhs_tc<D, M><<<grid, kTcThreads, kTcSmem, s>>>(a, partials, ctl);
 }
+
+// host side of the tensor-core kernel's failure reporting
+static int g_tc_polls = 1 << 24;
+static int g_tc_skip_mma = 0;
+static volatile unsigned *g_tc_fail_host = nullptr;  // page-locked, mapped
+static unsigned *g_tc_fail_dev = nullptr;
+
+static bool tc_fail_setup()
+{
+  if (g_tc_fail_host) return true;
+  void *h = nullptr, *d = nullptr;
+  if (!QG_CUDA(cudaHostAlloc(&h, sizeof(unsigned), cudaHostAllocMapped))) return false;
+  if (!QG_CUDA(cudaHostGetDevicePointer(&d, h, 0))) {
+    cudaFreeHost(h);
+    return false;
+  }
+  *(volatile unsigned *)h = 0u;
+  g_tc_fail_dev = (unsigned *)d;
+  g_tc_fail_host = (volatile unsigned *)h;
+  return true;
+}
+
+bool mrhs_tc_failed() { return g_tc_fail_host && *g_tc_fail_host; }
 
 struct MrhsTune {
   int variant;  // MRHS_SIMT, MRHS_MMA or MRHS_TC
@@ -1033,16 +1068,23 @@ static bool launch_mrhs(const MArgs &a, bool dag, MrhsTune t, double *partials, 
       set_error("tensor-core (tcgen05) multi-RHS kernel: slot count a multiple of 16, at most 64 (got %d)", a.N);
       return false;
     }
+    if (!tc_fail_setup()) return false;
+    if (*g_tc_fail_host) {
+      set_error("tensor-core multi-RHS kernel: an earlier launch abandoned its work after a bounded wait for the "
+                "tensor cores ran out (its output is invalid); qcdgpu_mrhs_tc_reset clears the state");
+      return false;
+    }
+    const TcCtl ctl{g_tc_polls, g_tc_skip_mma, g_tc_fail_dev};
     const unsigned grid = mrhs_tc_grid(a.V);
     const int mode = a.eo_par < 0 ? 0 : a.ainv ? 1 : 2;
     if (dag) {
-      if (mode == 0) launch_tc<true, 0>(a, partials, grid, s);
-      else if (mode == 1) launch_tc<true, 1>(a, partials, grid, s);
-      else launch_tc<true, 2>(a, partials, grid, s);
+      if (mode == 0) launch_tc<true, 0>(a, partials, grid, s, ctl);
+      else if (mode == 1) launch_tc<true, 1>(a, partials, grid, s, ctl);
+      else launch_tc<true, 2>(a, partials, grid, s, ctl);
     } else {
-      if (mode == 0) launch_tc<false, 0>(a, partials, grid, s);
-      else if (mode == 1) launch_tc<false, 1>(a, partials, grid, s);
-      else launch_tc<false, 2>(a, partials, grid, s);
+      if (mode == 0) launch_tc<false, 0>(a, partials, grid, s, ctl);
+      else if (mode == 1) launch_tc<false, 1>(a, partials, grid, s, ctl);
+      else launch_tc<false, 2>(a, partials, grid, s, ctl);
     }
     if (!QG_LAUNCHED("wilson_mrhs_tc")) return false;
     if (nblocks) *nblocks = grid;
@@ -1318,7 +1360,24 @@ int qcdgpu_set_mrhs_variant(int v)
 
 int qcdgpu_mrhs_tc_timeouts(unsigned *n)
 {
-  return cudaMemcpyFromSymbol(n, qg::g_mrhs_tc_timeouts, sizeof(unsigned)) == cudaSuccess ? 0 : 1;
+  if (!QG_CUDA(cudaStreamSynchronize(qg::stream()))) return 1;
+  return QG_CUDA(cudaMemcpyFromSymbol(n, qg::g_mrhs_tc_timeouts, sizeof(unsigned))) ? 0 : 1;
+}
+
+int qcdgpu_mrhs_tc_reset(void)
+{
+  if (!QG_CUDA(cudaStreamSynchronize(qg::stream()))) return 1;
+  const unsigned z = 0;
+  if (!QG_CUDA(cudaMemcpyToSymbol(qg::g_mrhs_tc_timeouts, &z, sizeof(z)))) return 1;
+  if (qg::g_tc_fail_host) *qg::g_tc_fail_host = 0u;
+  return 0;
+}
+
+int qcdgpu_mrhs_tc_test_hook(int skip_mma, int polls)
+{
+  qg::g_tc_skip_mma = skip_mma ? 1 : 0;
+  qg::g_tc_polls = polls > 0 ? polls : 1 << 24;
+  return 0;
 }
 
 int qcdgpu_mrhs_tuned(const int L[4], int nrhs, int *variant, int *threads)

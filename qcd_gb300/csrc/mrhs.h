@@ -78,6 +78,10 @@ bool dslash_mrhs_eo(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_mfield z, qcdgpu
                     const float *mp4s, const float *tms, int par, double ch, bool ainv, int zmode, double *partials,
                     unsigned *nblocks);
 
+// a tensor-core launch ran out of a bounded wait and abandoned its work (a
+// host-mapped flag the kernel sets: reading it needs no synchronisation)
+bool mrhs_tc_failed();
+
 // operator variants picked by the tuner
 enum { MRHS_AUTO = -1, MRHS_SIMT = 0, MRHS_MMA = 1, MRHS_TC = 2 };
 

@@ -681,6 +681,11 @@ bool batch_finish(qcdgpu_batch B)
   const int V = (int)B->Vs;
   cudaStream_t st = B->st;
   if (!QG_CUDA(cudaEventSynchronize(B->ev))) return false;
+  if (mrhs_tc_failed()) {
+    set_error("batch: the tensor-core multi-RHS kernel abandoned an apply after a bounded wait for the tensor "
+              "cores ran out; the chunk's results are invalid");
+    return false;
+  }
   std::vector<double> rr_iter(n), beta_iter(n);
   std::vector<int> need(n, 0), fail(n, 0);
   for (int k = 0; k < n; k++) {

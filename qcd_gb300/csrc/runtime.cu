@@ -3,10 +3,12 @@
 #include <stdarg.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
 #include <vector>
 
 #include "internal.h"
+#include "mrhs.h"
 
 namespace qg {
 
@@ -23,6 +25,18 @@ void set_error(const char *fmt, ...)
   va_end(ap);
   t_last_error = buf;
   fprintf(stderr, "qcdgpu: %s\n", buf);
+}
+
+// fault injection (tests): the next g_alloc_faults allocations of fields,
+// gauge fields and host vectors fail as if memory were exhausted
+static std::atomic<int> g_alloc_faults{0};
+
+bool alloc_fault()
+{
+  int n = g_alloc_faults.load();
+  while (n > 0)
+    if (g_alloc_faults.compare_exchange_weak(n, n - 1)) return true;
+  return false;
 }
 
 bool cuda_ok(cudaError_t e, const char *what)
@@ -77,6 +91,11 @@ qcdgpu_field field_new(const int L[4], int prec)
   f->stride = pad_stride(f->V);
   f->prec = prec;
   f->bytes = spinor_bytes(prec, f->stride);
+  if (alloc_fault()) {
+    set_error("out of device memory (injected) for a %zu-byte field", f->bytes);
+    delete f;
+    return nullptr;
+  }
   if (!QG_CUDA(cudaMalloc(&f->data, f->bytes))) {
     delete f;
     return nullptr;
@@ -119,6 +138,11 @@ qcdgpu_gauge gauge_new(const int L[4], const double theta[4], int prec, int reco
   size_t reals = (size_t)4 * recon;
   size_t esz = (prec == QCDGPU_F64 || prec == kGaugeFF) ? 8 : prec == QCDGPU_F32 ? 4 : 2;
   g->bytes = reals * esz * (size_t)g->stride;
+  if (alloc_fault()) {
+    set_error("out of device memory (injected) for a %zu-byte gauge field", g->bytes);
+    delete g;
+    return nullptr;
+  }
   if (!QG_CUDA(cudaMalloc(&g->data, g->bytes))) {
     delete g;
     return nullptr;
@@ -237,7 +261,21 @@ int qcdgpu_set_stream(void *s)
   return 0;
 }
 
-int qcdgpu_sync(void) { return QG_CUDA(cudaStreamSynchronize(qg::g_stream)) ? 0 : 1; }
+int qcdgpu_sync(void)
+{
+  if (!QG_CUDA(cudaStreamSynchronize(qg::g_stream))) return 1;
+  if (qg::mrhs_tc_failed()) {
+    qg::set_error("the tensor-core multi-RHS kernel abandoned an apply after a bounded wait ran out");
+    return 1;
+  }
+  return 0;
+}
+
+int qcdgpu_inject_alloc_failures(int n)
+{
+  qg::g_alloc_faults.store(n > 0 ? n : 0);
+  return 0;
+}
 
 int qcdgpu_release_work(void)
 {

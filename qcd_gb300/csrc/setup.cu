@@ -62,16 +62,30 @@ __global__ void k_gaussian(void *d, float *n, int64_t stride, int64_t V, uint64_
   Spinor<P, double>::store(d, n, stride, x, s);
 }
 
+// Noise spinors (the stochastic sources of qcd_stochastic.c:8-58): every
+// spin-colour component of the sites on time-slice tslice (all sites when
+// tslice < 0) is an independent draw from Z4 = {1, i, -1, -i} (kind 4, the
+// two top bits of the site's counter-based stream at 12 x + k) or Z2 = {1, -1}
+// (kind 2, the top bit); the other sites are zero. The reference draws from
+// GSL's ranlux (absent here); this stream is the library's own, seeded.
 template <int P>
-__global__ void k_z4(void *d, float *n, int64_t stride, int64_t V, uint64_t key)
+__global__ void k_noise(void *d, float *n, int64_t stride, int64_t V, uint64_t key, int L0, int tslice, int kind)
 {
   int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= V) return;
+  const bool on = tslice < 0 || (int)(x % L0) == tslice;
   C<double> s[12];
 #pragma unroll
   for (int k = 0; k < 12; k++) {
-    unsigned r = (unsigned)(rng_bits(key, (uint64_t)x * 12 + k) >> 62);
-    s[k] = C<double>{r == 0 ? 1.0 : r == 2 ? -1.0 : 0.0, r == 1 ? 1.0 : r == 3 ? -1.0 : 0.0};
+    const uint64_t b = rng_bits(key, (uint64_t)x * 12 + k);
+    if (!on) {
+      s[k] = C<double>{0.0, 0.0};
+    } else if (kind == 2) {
+      s[k] = C<double>{(b >> 63) ? -1.0 : 1.0, 0.0};
+    } else {
+      const unsigned r = (unsigned)(b >> 62);
+      s[k] = C<double>{r == 0 ? 1.0 : r == 2 ? -1.0 : 0.0, r == 1 ? 1.0 : r == 3 ? -1.0 : 0.0};
+    }
   }
   Spinor<P, double>::store(d, n, stride, x, s);
 }
@@ -97,15 +111,25 @@ bool field_gaussian(qcdgpu_field f, uint64_t seed)
   return QG_LAUNCHED("gaussian_spinor");
 }
 
-bool field_z4(qcdgpu_field f, uint64_t seed)
+bool field_noise(qcdgpu_field f, uint64_t seed, int tslice, int kind)
 {
+  if (!f || (kind != 2 && kind != 4)) {
+    set_error("noise: kind 2 (Z2) or 4 (Z4)");
+    return false;
+  }
   uint64_t key = rng_key(seed);
   unsigned g = blocks(f->V, 128);
-  if (f->prec == QCDGPU_F64) k_z4<QCDGPU_F64><<<g, 128, 0, stream()>>>(f->data, f->norm, f->stride, f->V, key);
-  else if (f->prec == QCDGPU_F32) k_z4<QCDGPU_F32><<<g, 128, 0, stream()>>>(f->data, f->norm, f->stride, f->V, key);
-  else k_z4<QCDGPU_F16><<<g, 128, 0, stream()>>>(f->data, f->norm, f->stride, f->V, key);
-  return QG_LAUNCHED("z4_spinor");
+  const int L0 = f->L[0];
+  if (f->prec == QCDGPU_F64)
+    k_noise<QCDGPU_F64><<<g, 128, 0, stream()>>>(f->data, f->norm, f->stride, f->V, key, L0, tslice, kind);
+  else if (f->prec == QCDGPU_F32)
+    k_noise<QCDGPU_F32><<<g, 128, 0, stream()>>>(f->data, f->norm, f->stride, f->V, key, L0, tslice, kind);
+  else
+    k_noise<QCDGPU_F16><<<g, 128, 0, stream()>>>(f->data, f->norm, f->stride, f->V, key, L0, tslice, kind);
+  return QG_LAUNCHED("noise_spinor");
 }
+
+bool field_z4(qcdgpu_field f, uint64_t seed) { return field_noise(f, seed, -1, 4); }
 
 bool field_point(qcdgpu_field f, const int x[4], int spin, int colour)
 {
@@ -295,6 +319,10 @@ int qcdgpu_gauge_synthetic(qcdgpu_gauge g, uint64_t seed, double eps)
 }
 double qcdgpu_plaquette(qcdgpu_gauge g) { return qg::plaquette(g); }
 int qcdgpu_field_gaussian(qcdgpu_field f, uint64_t seed) { return qg::field_gaussian(f, seed) ? 0 : 1; }
+int qcdgpu_field_noise(qcdgpu_field f, uint64_t seed, int t_slice, int kind)
+{
+  return qg::field_noise(f, seed, t_slice, kind) ? 0 : 1;
+}
 int qcdgpu_field_point(qcdgpu_field f, const int x[4], int spin, int colour)
 {
   return qg::field_point(f, x, spin, colour) ? 0 : 1;

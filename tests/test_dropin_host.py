@@ -129,3 +129,108 @@ def test_c_program_links_against_the_library(qlib, tmp_path):
     assert out.returncode == 0, out.stderr
     assert out.stdout.split()[0] == "256"
     assert int(out.stdout.split()[1]) == C.sizeof(q.QcdGeometry)
+
+
+def test_injected_allocation_failures_return_the_reference_error(qlib):
+    """host-side fault injection: the drop-in's allocation failures return the
+    reference's code 1 with its message (qcd_init.c:437-442, 614-665), leave
+    nothing allocated, and the next allocation succeeds again"""
+    lib = q.lib()
+    lib.qcdgpu_inject_alloc_failures.argtypes = [C.c_int]
+    geo = q.Geometry((4, 4, 4, 4))
+    assert geo.ok
+    try:
+        assert lib.qcdgpu_inject_alloc_failures(2) == 0
+        v = q.QcdVector()
+        assert lib.qcd_initVector(C.byref(v), C.byref(geo.s)) == 1
+        assert not v.initialized
+        assert "qcd_initVector" in lib.qcdgpu_last_error().decode()
+        assert "Out of memory" in lib.qcdgpu_last_error().decode()
+        u = q.QcdGaugeField()
+        assert lib.qcd_initGaugeField(C.byref(u), C.byref(geo.s)) == 1
+        assert "qcd_initGaugeField" in lib.qcdgpu_last_error().decode()
+        vec = q.Vector(geo)  # the injected failures are used up
+        vec.a[:] = 1.0
+        vec.close()
+    finally:
+        lib.qcdgpu_inject_alloc_failures(0)
+        geo.close()
+
+
+def _site_vectors(seed):
+    rng = np.random.default_rng(seed)
+    vec = rng.normal(size=(4, 3, 2))
+    u = rng.normal(size=(3, 3, 2))
+    return np.ascontiguousarray(vec), np.ascontiguousarray(u)
+
+
+def test_site_helpers_match_reference(qlib, ref):
+    """qcd_onePlusGamma / qcd_oneMinusGamma (mu = 0..5), qcd_applyU,
+    qcd_applyUDagger, qcd_massTerms and qcd_phaseMul against the reference's
+    own functions (lib/src/qcd_wilson.c:18-103) on the same inputs"""
+    lib = q.lib()
+    R = ref.lib
+    dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+    for n in ("qcd_onePlusGamma", "qcd_oneMinusGamma"):
+        getattr(R, n).argtypes = [dp, dp, C.c_uint16]
+    for n in ("qcd_applyU", "qcd_applyUDagger"):
+        getattr(R, n).argtypes = [dp, dp, dp]
+    R.qcd_massTerms.argtypes = [dp, dp, C.c_double, C.c_double]
+    R.qcd_phaseMul.argtypes = [dp, q.QcdComplex16]
+    for seed in range(3):
+        vec, u = _site_vectors(seed)
+        for mu in range(6):
+            for n in ("qcd_onePlusGamma", "qcd_oneMinusGamma"):
+                a, b = np.zeros_like(vec), np.zeros_like(vec)
+                getattr(lib, n)(a, vec, mu)
+                getattr(R, n)(b, vec, mu)
+                assert np.array_equal(a, b), (n, mu)  # entries 0, +-1, +-i: exact
+        for n in ("qcd_applyU", "qcd_applyUDagger"):
+            a, b = np.zeros_like(vec), np.zeros_like(vec)
+            getattr(lib, n)(a, u, vec)
+            getattr(R, n)(b, u, vec)
+            assert np.max(np.abs(a - b)) <= 1e-15 * np.max(np.abs(b)), n
+        a, b = np.zeros_like(vec), np.zeros_like(vec)
+        lib.qcd_massTerms(a, vec, 4.3, -0.27)
+        R.qcd_massTerms(b, vec, 4.3, -0.27)
+        assert np.max(np.abs(a - b)) <= 1e-15 * np.max(np.abs(b))
+        a, b = vec.copy(), vec.copy()
+        lib.qcd_phaseMul(a, q.QcdComplex16(0.6, -0.8))
+        R.qcd_phaseMul(b, q.QcdComplex16(0.6, -0.8))
+        assert np.max(np.abs(a - b)) <= 1e-15
+
+
+def test_site_helpers_algebra(qlib):
+    """the helpers against their definitions in the chiral basis (no reference
+    needed): (1 +- gamma_mu), gamma_4 = -gamma_0, gamma_5 = diag(1, 1, -1, -1)"""
+    G = np.zeros((6, 4, 4), dtype=complex)
+    G[0][0, 2] = G[0][1, 3] = G[0][2, 0] = G[0][3, 1] = -1
+    G[1][0, 3] = G[1][1, 2] = -1j
+    G[1][2, 1] = G[1][3, 0] = 1j
+    G[2][0, 3] = G[2][3, 0] = -1
+    G[2][1, 2] = G[2][2, 1] = 1
+    G[3][0, 2] = G[3][3, 1] = -1j
+    G[3][1, 3] = G[3][2, 0] = 1j
+    G[4] = -G[0]
+    G[5] = np.diag([1, 1, -1, -1])
+    lib = q.lib()
+    vec, u = _site_vectors(9)
+    vc = vec[..., 0] + 1j * vec[..., 1]
+    uc = u[..., 0] + 1j * u[..., 1]
+
+    def cx(a):
+        return a[..., 0] + 1j * a[..., 1]
+
+    for mu in range(6):
+        a = np.zeros_like(vec)
+        lib.qcd_onePlusGamma(a, vec, mu)
+        assert np.allclose(cx(a), (np.eye(4) + G[mu]) @ vc, atol=1e-15)
+        lib.qcd_oneMinusGamma(a, vec, mu)
+        assert np.allclose(cx(a), (np.eye(4) - G[mu]) @ vc, atol=1e-15)
+    a = np.zeros_like(vec)
+    lib.qcd_applyU(a, u, vec)
+    assert np.allclose(cx(a), vc @ uc.T, atol=1e-14)
+    lib.qcd_applyUDagger(a, u, vec)
+    assert np.allclose(cx(a), vc @ uc.conj(), atol=1e-14)
+    lib.qcd_massTerms(a, vec, 4.3, -0.27)
+    assert np.allclose(cx(a), 4.3 * vc + 1j * -0.27 * (G[5] @ vc), atol=1e-14)

@@ -71,3 +71,40 @@ def test_tcgen05_variant_rejects_slot_counts_it_cannot_tile(gpu, orc):
         q.set_mrhs_variant(-1)
         for o in (g, mi, mo):
             o.close()
+
+
+def test_tcgen05_bounded_wait_runs_out_and_is_reported(gpu, orc):
+    """the test hook issues no MMA, so every wait for the accumulator runs out
+    (4096 polls): the launch abandons its work, qcdgpu_sync and the next apply
+    report the failure, and after a reset the kernel is exact again"""
+    L = (8, 4, 6, 4)
+    th = (np.pi, 0.0, 0.0, 0.0)
+    u = orc.gauge_synthetic(L, 43, EPS_PLAQ_060)
+    g = q.Gauge(L, th).load(u)
+    mi, mo, f = q.MField(L, 16), q.MField(L, 16), q.Field(L)
+    srcs = [orc.gaussian_spinor(L, 200 + r) for r in range(16)]
+    for r in range(16):
+        mi.set(r, f.load(srcs[r]))
+    lib = q.lib()
+    q.set_mrhs_variant(2)
+    try:
+        assert lib.qcdgpu_mrhs_tc_test_hook(1, 4096) == 0
+        q.dslash_mrhs(mo, mi, g, 0.15, 0.0, q.OP_D, 16)  # the launch itself is accepted
+        assert lib.qcdgpu_sync() == 1
+        assert "bounded wait" in lib.qcdgpu_last_error().decode()
+        assert tc_timeouts() > 0
+        with pytest.raises(q.QcdGpuError):  # refused until the state is cleared
+            q.dslash_mrhs(mo, mi, g, 0.15, 0.0, q.OP_D, 16)
+    finally:
+        lib.qcdgpu_mrhs_tc_test_hook(0, 0)
+        assert lib.qcdgpu_mrhs_tc_reset() == 0
+    try:
+        assert tc_timeouts() == 0
+        q.dslash_mrhs(mo, mi, g, 0.15, 0.0, q.OP_D, 16)
+        assert lib.qcdgpu_sync() == 0
+        for r in (0, 15):
+            assert rel(mo.get(r, f).store(), orc.dslash(srcs[r], u, L, th, kappa=0.15)) <= TOL
+    finally:
+        q.set_mrhs_variant(-1)
+        for o in (g, mi, mo, f):
+            o.close()
