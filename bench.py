@@ -70,15 +70,50 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "src": "fallback"}
 
 
-def profile_traffic(name: str):
-    """DRAM bytes per launch from the committed ncu summary, if present"""
+def profile_value(name: str, key: str = "dram_bytes_per_launch"):
+    """a figure of the committed ncu summary (`key: value` line), if present"""
     p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.startswith("dram_bytes_per_launch:"):
+        if line.startswith(key + ":"):
             return float(line.split(":")[1])
     return None
+
+
+def profile_traffic(name: str):
+    """DRAM bytes per launch from the committed ncu summary, if present"""
+    return profile_value(name)
+
+
+def compute_ceiling(q, V, ms_native, ms_df64, sm_mhz):
+    """the FP64 operator against its arithmetic ceilings: the native kernel
+    against the FP64 FMA pipe (1320 flops per site at the FMA rate measured
+    here), the float-float kernel against instruction issue (its warp
+    instructions per apply from the committed ncu capture, four warp
+    instructions per clock per SM at the sampled SM clock)"""
+    import ctypes as C
+
+    out = {}
+    r64, r32 = C.c_double(), C.c_double()
+    if q.lib().qcdgpu_measure_fma_rate(0, C.byref(r64)) == 0 and ms_native:
+        floor = V * FLOPS_PER_SITE / (r64.value * 1e12) * 1e3
+        out["native_fp64"] = {"bound": "fp64 fma pipe", "fp64_tflops_measured": r64.value,
+                              "flops_per_site": FLOPS_PER_SITE, "floor_ms": floor, "kernel_ms": ms_native,
+                              "frac": floor / ms_native}
+    if q.lib().qcdgpu_measure_fma_rate(1, C.byref(r32)) == 0:
+        out["fp32_tflops_measured"] = r32.value
+    instr = profile_value("dslash_df64_24x24x24x48.md", "warp_instructions_per_launch")
+    if instr and ms_df64:
+        import torch
+
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        mhz = sm_mhz or 2070.0
+        floor = instr / (4.0 * sms * mhz * 1e6) * 1e3
+        out["float_float"] = {"bound": "instruction issue", "warp_instructions": instr, "sm_mhz": mhz,
+                              "floor_ms": floor, "kernel_ms": ms_df64, "frac": floor / ms_df64,
+                              "hbm_floor_ms": None}
+    return out
 
 
 class ClockSampler:
@@ -188,8 +223,10 @@ def config1_solves(q, budget_s: float) -> dict:
     kappa 0.150, solved to a true residual of 1e-10. CPU: the C restatement's
     FP64 CGNR on one host core, as many columns as fit the time budget (at
     least one). GPU: all 12 columns, even/odd CGNR with FP16 inner iterations
-    and plain FP64 CGNR. Identical inputs on both sides. (The case names
-    BiCGstab, which stagnates near 5e-3 on this ensemble at kappa 0.150.)"""
+    and plain FP64 CGNR, and the configuration's BiCGstab: BiCGstab(8) on the
+    even/odd system with FP64 and with FP32 inner iterations (plain BiCGstab
+    stagnates near 5e-3 on this ensemble at kappa 0.150). Identical inputs on
+    both sides."""
     import numpy as np
 
     from oracle.oracle import Oracle
@@ -226,13 +263,17 @@ def config1_solves(q, budget_s: float) -> dict:
     out = {"lattice_txyz": list(L), "kappa": KAPPA, "tol": 1e-10,
            "cpu_fp64_cgnr": {"rhs_solves_per_s": cols / cpu_s, "columns": cols, "iters": iters, "cores": 1,
                              "kind": "port", "true_residual_last": cpu_res, "normal_eq_tol": tol_ne}}
-    for name, solver, prec in (("gpu_eo_cgnr_f16", q.SOLVER_CGNR_EO, q.F16), ("gpu_fp64_cgnr", q.SOLVER_CGNR, q.F64)):
+    for name, solver, prec in (("gpu_eo_cgnr_f16", q.SOLVER_CGNR_EO, q.F16), ("gpu_fp64_cgnr", q.SOLVER_CGNR, q.F64),
+                               ("gpu_eo_bicgstab8_f64", q.SOLVER_BICGSTABL_EO, q.F64),
+                               ("gpu_eo_bicgstab8_f32", q.SOLVER_BICGSTABL_EO, q.F32)):
         xs = [q.Field(L) for _ in range(12)]
         bs = [q.Field(L).point((0, 0, 0, 0), c // 3, c % 3) for c in range(12)]
-        q.solve(xs[0], bs[0], g, KAPPA, 0.0, solver=solver, inner_prec=prec, tol=1e-10)  # warm-up
+        q.solve(xs[0], bs[0], g, KAPPA, 0.0, solver=solver, inner_prec=prec, tol=1e-10, restart=8,
+                maxiter=40000)  # warm-up
         q.sync()
         t0 = time.perf_counter()
-        ps = [q.solve(xs[c], bs[c], g, KAPPA, 0.0, solver=solver, inner_prec=prec, tol=1e-10) for c in range(12)]
+        ps = [q.solve(xs[c], bs[c], g, KAPPA, 0.0, solver=solver, inner_prec=prec, tol=1e-10, restart=8,
+                      maxiter=40000) for c in range(12)]
         q.sync()
         dt = time.perf_counter() - t0
         res = max(orc.true_residual(xs[c].store(), point(c), u, L, THETA, KAPPA) for c in range(12))
@@ -334,6 +375,29 @@ def solve_bench(q, orc_check, g, L, n_rhs):
         for k in ("mixed_cgnr_f16", "mixed_cgnr_f32", "eo_cgnr_f32", "eo_cgnr_f16"):
             if out[k]["rhs_solves_per_s"]:
                 out["speedup_" + k + "_vs_fp64"] = out[k]["rhs_solves_per_s"] / out["fp64_cgnr"]["rhs_solves_per_s"]
+    # the configuration's own source: a point at the origin, Gaussian-smeared
+    # (alpha 4.0, 50 steps) on APE-smeared links (alpha 0.5, 20 steps), built
+    # on the GPU; the solve runs on the unsmeared links
+    sm = {}
+    for spin_col in range(2):
+        q.smeared_source(b, g, (0, 0, 0, 0), spin_col, spin_col, 0.5, 20, 4.0, 50)
+        for name, solver, prec in (("fp64_cgnr", q.SOLVER_CGNR, q.F64), ("eo_cgnr_f16", q.SOLVER_CGNR_EO, q.F16)):
+            q.sync()
+            t0 = time.perf_counter()
+            p = q.solve(x, b, g, KAPPA, 0.0, solver=solver, inner_prec=prec, tol=1e-10)
+            q.sync()
+            d = sm.setdefault(name, {"s": [], "iters": [], "true_residual": [], "status": []})
+            d["s"].append(time.perf_counter() - t0)
+            d["iters"].append(p.iters)
+            d["true_residual"].append(p.true_residual)
+            d["status"].append(p.status)
+    for d in sm.values():
+        ok = all(st == 0 for st in d["status"])
+        d["rhs_solves_per_s"] = len(d["s"]) / sum(d["s"]) if ok else None
+    if sm["fp64_cgnr"]["rhs_solves_per_s"] and sm["eo_cgnr_f16"]["rhs_solves_per_s"]:
+        sm["speedup_eo_cgnr_f16_vs_fp64"] = sm["eo_cgnr_f16"]["rhs_solves_per_s"] / sm["fp64_cgnr"]["rhs_solves_per_s"]
+    sm["source"] = "point at the origin, Gaussian alpha 4.0 x 50 on APE alpha 0.5 x 20 links (two spin-colour columns)"
+    out["smeared_source"] = sm
     b.close()
     x.close()
     return out
@@ -430,12 +494,18 @@ def precision_bench(q, L, kappa, n_batch, cap):
     return out
 
 
-def batching_bench(q, L, kappa, nrhs):
-    """the batching configuration: nrhs point-source columns at L solved to
-    1e-10 by one even/odd batch of nrhs slots, beside one even/odd FP16 solve
-    and one plain FP64 solve of the first column"""
+def batching_bench(q, L, kappa, nrhs, caps=(4, 8, 16), sweep_rhs=16):
+    """The batching configuration at L (48^3 x 96), kappa: nrhs right-hand
+    sides = 8 source positions x 12 spin-colour columns, solved to 1e-10 by
+    even/odd batches with continuous admission. First the RHS-per-block sweep
+    inside the solve (the first sweep_rhs columns at each batch capacity in
+    caps; 32 per block does not fit: every slot keeps ~5.4 GB of FP64
+    even/odd state at this volume besides its 4 GB of FP64 x and b), then all
+    nrhs columns at the fastest capacity. Beside them one even/odd FP16 solve
+    and one plain FP64 solve of the first column."""
     g = q.Gauge(L, THETA).synthetic(4, EPS_PLAQ_060)
-    out = {"lattice_txyz": list(L), "kappa": kappa, "rhs": nrhs, "tol": 1e-10}
+    out = {"lattice_txyz": list(L), "kappa": kappa, "rhs": nrhs, "tol": 1e-10,
+           "sources": "points at t in {0, L_t/2} x (x, y, z) in {0, (L/2,0,0), (0,L/2,0), (0,0,L/2)}, 12 columns each"}
     b, x = q.Field(L), q.Field(L)
     for name, solver, prec in (("fp64_cgnr", q.SOLVER_CGNR, q.F64), ("eo_cgnr_f16", q.SOLVER_CGNR_EO, q.F16)):
         b.point((0, 0, 0, 0), 0, 0)
@@ -448,43 +518,72 @@ def batching_bench(q, L, kappa, nrhs):
                      "true_residual": p.true_residual, "status": p.status}
     b.close()
     x.close()
-    srcs = [q.Field(L).point(((c // 12) * L[0] // 2, 0, 0, 0), c % 12 // 3, c % 3) for c in range(nrhs)]
-    xs = [q.Field(L) for _ in range(nrhs)]
-    batch = q.Batch(g, nrhs, eo=True)
-    q.sync()
-    t0 = time.perf_counter()
-    for c in range(nrhs):
-        batch.add(xs[c], srcs[c], kappa, 0.0, q.OP_D, tol=1e-10, maxiter=40000, tag=c)
-    done = []
-    while batch.active:
-        batch.step(16)
-        done += batch.poll()
-    done += batch.poll()
-    q.sync()
-    dt = time.perf_counter() - t0
-    ok = len(done) == nrhs and all(d[1] == 0 for d in done)
-    out["batched_mrhs_eo"] = {"rhs_solves_per_s": nrhs / dt if ok else None, "wall_s": dt,
-                              "iters_max": max(d[2] for d in done), "max_true_residual": max(d[3] for d in done),
-                              "status": sorted({d[1] for d in done}), "bytes": batch.nbytes()}
+    h = L[1] // 2
+    spatial = ((0, 0, 0), (h, 0, 0), (0, h, 0), (0, 0, h))
+    positions = [(t, *xyz) for t in (0, L[0] // 2) for xyz in spatial]
+
+    def run(cap, n):
+        """columns 0..n-1 through an even/oddbatch of cap slots; x and b
+        fields are taken from a pool of cap pairs and returned on retirement"""
+        pool = [(q.Field(L), q.Field(L)) for _ in range(cap)]
+        free = list(range(cap))
+        batch = q.Batch(g, cap, eo=True)
+        busy, done = {}, []
+        q.sync()
+        t0 = time.perf_counter()
+        c = 0
+        while c < n or batch.active:
+            while c < n and free:
+                k = free.pop()
+                xf, bf = pool[k]
+                pos = positions[(c // 12) % len(positions)]
+                bf.point(pos, c % 12 // 3, c % 3)
+                batch.add(xf, bf, kappa, 0.0, q.OP_D, tol=1e-10, maxiter=40000, tag=c)
+                busy[c] = k
+                c += 1
+            batch.step(16)
+            for d in batch.poll():
+                done.append(d)
+                free.append(busy.pop(d[0]))
+        q.sync()
+        dt = time.perf_counter() - t0
+        nbytes = batch.nbytes()
+        batch.close()
+        for xf, bf in pool:
+            xf.close()
+            bf.close()
+        ok = len(done) == n and all(d[1] == 0 for d in done)
+        return {"slots": cap, "rhs": n, "rhs_solves_per_s": n / dt if ok else None, "wall_s": dt,
+                "iters_max": max(d[2] for d in done), "max_true_residual": max(d[3] for d in done),
+                "status": sorted({d[1] for d in done}), "batch_bytes": nbytes}
+
+    sweep = []
+    for cap in caps:
+        q.release_work()
+        sweep.append(run(cap, sweep_rhs))
+    out["rhs_per_block_sweep"] = sweep
+    ok = [r for r in sweep if r["rhs_solves_per_s"]]
+    best = max(ok, key=lambda r: r["rhs_solves_per_s"])["slots"] if ok else caps[-1]
+    q.release_work()
+    out["batched_mrhs_eo"] = run(best, nrhs)
     base = out["fp64_cgnr"]["rhs_solves_per_s"]
     if base and out["batched_mrhs_eo"]["rhs_solves_per_s"]:
         out["speedup_batched_mrhs_eo_vs_fp64"] = out["batched_mrhs_eo"]["rhs_solves_per_s"] / base
-    batch.close()
-    for f in srcs + xs + [g]:
-        f.close()
+    g.close()
     return out
 
 
-def serving_bench(q, seconds, rate, slots, budget_gb):
-    """Poisson stream over four resident gauge fields (one per volume)"""
+def serving_bench(q, seconds, rate, slots, budget_gb, weights=None):
+    """Poisson stream over four resident gauge fields (one per volume); with
+    weights, requests draw the volumes with those weights"""
     from qcd_gb300 import serving
 
     gauges = serving.build_gauges()
     srv = q.Server(int(budget_gb * 2**30), slots)
     ids = [srv.add_gauge(g) for g in gauges]
-    arr = serving.make_stream(rate, seconds, len(ids), seed=7)
+    arr = serving.make_stream(rate, seconds, len(ids), seed=7, weights=weights)
     res = serving.run_stream(srv, ids, arr, max_wall_s=seconds * 6 + 60)
-    res.update({"rate_hz": rate, "arrival_s": seconds, "slots": slots, "budget_gb": budget_gb,
+    res.update({"rate_hz": rate, "arrival_s": seconds, "slots": slots, "budget_gb": budget_gb, "volume_weights": weights,
                 "volumes_txyz": [list(L) for L in serving.SERVE_VOLUMES], "kappa": [0.14, 0.155],
                 "rhs_per_request": [1, 48], "tols": [1e-8, 1e-10]})
     srv.close()
@@ -545,8 +644,13 @@ def run_ours(args, rank, world, local_rank):
         q.release_work()
     if rank == 0 and not args.no_solve:
         precision = precision_bench(q, L_PREC, KAPPA_PREC, args.batch_rhs, args.batch_slots)
+    serving32 = None
     if rank == 0 and not args.no_serve:
         serving = serving_bench(q, args.serve_seconds, args.serve_rate, args.serve_slots, args.serve_budget_gb)
+        # the same stream on the 32^3 x 64 gauge field alone (the spec volume)
+        serving32 = serving_bench(q, args.serve32_seconds, args.serve32_rate, args.serve_slots, args.serve_budget_gb,
+                                  weights=(0, 0, 0, 1))
+    ceiling = compute_ceiling(q, V, ms_native, ms_df64, clocks["sm_mhz"] if clocks else None) if rank == 0 else None
     if rank != 0:
         return None
     peaks = measured_peaks()
@@ -565,7 +669,8 @@ def run_ours(args, rank, world, local_rank):
                      "frac": achieved_1 / peaks["hbm_gbs"], "peak_source": peaks["src"],
                      "traffic": profile_traffic("dslash_df64_24x24x24x48.md" if arith == "df64" else
                                                 "dslash_f64_24x24x24x48.md"),
-                     "traffic_source": "profiles/ ncu capture of the same kernel and lattice (dram read + write)"},
+                     "traffic_source": "profiles/ ncu capture of the same kernel and lattice (dram read + write)",
+                     "compute_ceiling": ceiling},
         "kernels_ms": {"f64": ms_native, "df64": ms_df64},
         "e2e": {"value": V * bps / (ms_e2e * 1e-3) / 1e9 * world, "unit": "GB/s", "ms_per_step": ms_e2e,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -583,11 +688,34 @@ def run_ours(args, rank, world, local_rank):
     eff = 8 * 192 + 8 * 144 + 192
     line["effective_bytes"] = {"bytes_per_site": eff, "GB/s": V * eff / (best_ms * 1e-3) / 1e9,
                                "note": "8 neighbour spinors + 8 links + output per site; not the roofline basis"}
+    line["serving_32x64"] = serving32
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds, 1)
         if not args.no_solve:
             line["config1_8x16"] = config1_solves(q, args.cpu_seconds / 2)
+    line["north_star"] = north_star(precision, serving32)
     return line
+
+
+def north_star(precision, serving32):
+    """the spec comparison at 32^3 x 64, kappa 0.155, true residual
+    1e-10 (last key of the line): RHS-solves/s of the plain FP64 GPU solve
+    (the drop-in), of the batched and the single even/odd mixed-precision
+    solves and of the served stream on that volume, their ratios to the plain
+    solve (target 4), and the served p50 / p99 latency"""
+    if not precision:
+        return None
+    base = precision["fp64_cgnr"]["rhs_solves_per_s"]
+    ns = {"lattice_txyz": precision["lattice_txyz"], "kappa": precision["kappa"], "tol": 1e-10, "target_ratio": 4.0,
+          "plain_fp64": base, "single_eo_f16": precision["eo_cgnr_f16"]["rhs_solves_per_s"],
+          "batched_eo": precision["batched_mrhs_eo"]["rhs_solves_per_s"],
+          "served": serving32["rhs_solves_per_s"] if serving32 else None,
+          "served_p50_s": serving32["p50_s"] if serving32 else None,
+          "served_p99_s": serving32["p99_s"] if serving32 else None,
+          "served_tols": "1e-8 or 1e-10 per request" if serving32 else None}
+    for k in ("single_eo_f16", "batched_eo", "served"):
+        ns["ratio_" + k] = ns[k] / base if base and ns[k] else None
+    return ns
 
 
 def run_only(args):
@@ -683,11 +811,14 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--batch-rhs", type=int, default=48, help="point-source columns of the batched 32^3x64 solve")
     ap.add_argument("--batch-slots", type=int, default=48)
-    ap.add_argument("--big-batch-rhs", type=int, default=16, help="point-source columns of the 48^3x96 batch")
+    ap.add_argument("--big-batch-rhs", type=int, default=96,
+                    help="point-source columns of the 48^3x96 batch (8 positions x 12 columns)")
     ap.add_argument("--serve-seconds", type=float, default=30.0)
     ap.add_argument("--serve-rate", type=float, default=2.0, help="request arrivals per second")
     ap.add_argument("--serve-slots", type=int, default=32)
     ap.add_argument("--serve-budget-gb", type=float, default=120.0)
+    ap.add_argument("--serve32-seconds", type=float, default=15.0, help="arrival window of the 32^3x64-only stream")
+    ap.add_argument("--serve32-rate", type=float, default=1.0, help="arrivals per second of the 32^3x64-only stream")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-seconds", type=float, default=20.0)
     ap.add_argument("--mrhs-n", type=int, default=16, help="--only mrhs / batch: RHS per block / batch slots")

@@ -361,7 +361,12 @@ enum {
   QCDGPU_SOLVER_CGNR = 2,
   /* CGNR on the even/odd (Schur) preconditioned system; the t extent must
    * be even. Same convergence test on the full true residual. */
-  QCDGPU_SOLVER_CGNR_EO = 3
+  QCDGPU_SOLVER_CGNR_EO = 3,
+  /* BiCGstab(l) (Sleijpen-Fokkema) on the even/odd Schur complement, l =
+   * restart when 1..16 (else 8); inner iterations in inner_prec with FP64
+   * defect correction. Plain BiCGstab stagnates near the critical kappa
+   * (SOLVER_BICGSTAB reports that as status 1); this one converges there. */
+  QCDGPU_SOLVER_BICGSTABL_EO = 4
 };
 /* solve A x = b with A = op(g; kappa, mu); x, b FP64 device fields */
 int qcdgpu_solve(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double kappa, double mu,
@@ -376,6 +381,10 @@ int qcdgpu_release_work(void);
  * were exhausted, so that callers' out-of-memory paths run without
  * exhausting memory; n = 0 switches it off. */
 int qcdgpu_inject_alloc_failures(int n);
+/* FMA throughput of this GPU in TFLOP/s (2 flops per FMA), kind 0 FP64 or 1
+ * FP32, from a kernel of independent FMA chains on every SM (no reference
+ * counterpart; the benchmark's compute ceilings). */
+int qcdgpu_measure_fma_rate(int kind, double *tflops);
 
 /* No counterpart in the reference. The complex dot product
  * result[0] + i result[1] = sum_i conj(a_i) b_i, for callers that cannot

@@ -27,7 +27,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libqcdgpu.so")
 F64, F32, F16 = 0, 1, 2
 OP_D, OP_Q, OP_DDAG, OP_DDAGD = 0, 1, 2, 3
 ARITH_F64, ARITH_DF64 = 0, 1
-SOLVER_GCR, SOLVER_BICGSTAB, SOLVER_CGNR, SOLVER_CGNR_EO = 0, 1, 2, 3
+SOLVER_GCR, SOLVER_BICGSTAB, SOLVER_CGNR, SOLVER_CGNR_EO, SOLVER_BICGSTABL_EO = 0, 1, 2, 3, 4
 
 _u8p = C.POINTER(C.c_uint64)
 
@@ -158,6 +158,7 @@ def lib() -> C.CDLL:
     L.qcdgpu_field_copy.argtypes = [C.c_void_p, C.c_void_p]
     L.qcdgpu_field_gaussian.argtypes = [C.c_void_p, C.c_uint64]
     L.qcdgpu_field_point.argtypes = [C.c_void_p, _ip, C.c_int, C.c_int]
+    L.qcdgpu_measure_fma_rate.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.qcdgpu_field_noise.argtypes = [C.c_void_p, C.c_uint64, C.c_int, C.c_int]
     L.qcd_z2Vector.argtypes = [vp, C.c_int]
     L.qcd_z2Vector.restype = None

@@ -25,6 +25,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <complex>
 #include <functional>
 #include <vector>
 
@@ -546,6 +547,251 @@ bool eo_diag(qcdgpu_field out, qcdgpu_field in, double mp4, double tm, bool inve
   k_eo_diag<<<(unsigned)((in->V + 127) / 128), 128, 0, stream()>>>((double2 *)out->data, (const double2 *)in->data,
                                                                     in->stride, (int)in->V, ar, ai);
   return QG_LAUNCHED("eo_diag");
+}
+
+
+// ------------------------------------------------- BiCGstab(l), even/odd
+// BiCGstab(l) (Sleijpen & Fokkema, ETNA 1 (1993) 11) on the even/odd Schur
+// complement M x_e = c_e of solve_cgnr_eo. Plain BiCGstab stagnates on this
+// operator near the critical kappa (its one-step minimal-residual polynomial
+// cannot damp eigenvalues of M that lie far off the real axis); BiCGstab(l)
+// replaces it by a degree-l minimal-residual polynomial every l BiCG steps.
+// One cycle: l BiCG steps (2 l applications of M, two dots each, read by
+// the host), then the minimal-residual step from the Gram matrix
+// G_ij = <r_i, r_j> of r_0 .. r_l (all dots queued, one synchronisation):
+// gamma solves G[1..l][1..l] gamma = G[1..l][0], and
+//   x += sum_j gamma_j r_{j-1},  r_0 -= sum_j gamma_j r_j,
+//   u_0 -= sum_j gamma_j u_j,    omega = gamma_l.
+// Mixed precision by reliable updates (Sleijpen & van der Vorst, Computing 56
+// (1996) 141): one BiCGstab(l) recurrence runs in the inner precision; at a
+// cycle's end, when the iterated residual has fallen by delta (p->delta in
+// (0, 1), else 0.1) since the last update, looks converged, or the recurrence
+// broke down, the increment is added to the FP64 x_e and r_0 is replaced by
+// the FP64 true residual c_e - M x_e (float-float operator), keeping u_0 and
+// the scalars (after a breakdown the recurrence restarts). The shadow
+// residual is a fixed Z4 vector. Convergence is declared on the full true
+// residual |b - D x| / |b|.
+
+// gamma solving A gamma = c for the l x l Hermitian A (Gaussian elimination
+// with partial pivoting); false when A is singular
+static bool small_solve(int n, std::vector<std::complex<double>> A, std::vector<std::complex<double>> c,
+                        std::vector<std::complex<double>> &x)
+{
+  for (int k = 0; k < n; k++) {
+    int piv = k;
+    for (int i = k + 1; i < n; i++)
+      if (std::abs(A[i * n + k]) > std::abs(A[piv * n + k])) piv = i;
+    if (std::abs(A[piv * n + k]) == 0.0) return false;
+    if (piv != k) {
+      for (int j = 0; j < n; j++) std::swap(A[k * n + j], A[piv * n + j]);
+      std::swap(c[k], c[piv]);
+    }
+    for (int i = k + 1; i < n; i++) {
+      const std::complex<double> f = A[i * n + k] / A[k * n + k];
+      for (int j = k; j < n; j++) A[i * n + j] -= f * A[k * n + j];
+      c[i] -= f * c[k];
+    }
+  }
+  x.assign(n, 0.0);
+  for (int i = n - 1; i >= 0; i--) {
+    std::complex<double> t = c[i];
+    for (int j = i + 1; j < n; j++) t -= A[i * n + j] * x[j];
+    x[i] = t / A[i * n + i];
+  }
+  return true;
+}
+
+int solve_bicgstabl_eo(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, double tm,
+                       qcdgpu_solve_params *p)
+{
+  using cplx = std::complex<double>;
+  if (b->L[0] % 2 != 0) {
+    set_error("even/odd solve: the t extent must be even");
+    return 3;
+  }
+  Held w;
+  p->iters = 0;
+  p->reliable_updates = 0;
+  p->true_residual = 1.0;
+  double bn2;
+  if (!blas_norm2(b, &bn2)) return 3;
+  if (bn2 == 0.0) {
+    p->true_residual = 0.0;
+    return blas_zero(x) ? 0 : 3;
+  }
+  const int ell = p->restart >= 1 && p->restart <= 16 ? p->restart : 8;
+  const int prec = p->inner_prec;
+  const int xprec = prec == QCDGPU_F16 ? QCDGPU_F32 : prec;  // the inner increment keeps FP32 at least
+  const int ar = QCDGPU_ARITH_DF64;
+  qcdgpu_field bd = system_rhs(w, b, p->op);
+  qcdgpu_gauge gi = gauge_at(g, prec);
+  const int Lh[4] = {b->L[0] / 2, b->L[1], b->L[2], b->L[3]};
+  qcdgpu_field be = w.get(Lh, QCDGPU_F64), bo = w.get(Lh, QCDGPU_F64), to = w.get(Lh, QCDGPU_F64);
+  qcdgpu_field ce = w.get(Lh, QCDGPU_F64), xe = w.get(Lh, QCDGPU_F64), xo = w.get(Lh, QCDGPU_F64);
+  qcdgpu_field re = w.get(Lh, QCDGPU_F64), t64 = w.get(Lh, QCDGPU_F64), e64 = w.get(Lh, QCDGPU_F64);
+  qcdgpu_field ti = w.get(Lh, prec), rh = w.get(Lh, prec), xi = w.get(Lh, xprec);
+  // FP16 vectors reach the FP32 increment through this conversion buffer
+  qcdgpu_field cv = xprec != prec ? w.get(Lh, xprec) : nullptr;
+  if (xprec != prec && !cv) return 3;
+  auto add_to_x = [&](cplx a, qcdgpu_field v) {
+    if (cv) {
+      if (!convert_field(cv, v)) return false;
+      v = cv;
+    }
+    return blas_axpby(xi, a.real(), a.imag(), v, 1.0, 0.0, xi);
+  };
+  std::vector<qcdgpu_field> R(ell + 1), U(ell + 1);
+  for (int j = 0; j <= ell; j++) {
+    R[j] = w.get(Lh, prec);
+    U[j] = w.get(Lh, prec);
+    if (!R[j] || !U[j]) return 3;
+  }
+  if (!bd || !gi || !be || !bo || !to || !ce || !xe || !xo || !re || !t64 || !e64 || !ti || !rh || !xi) return 3;
+  // the Gram matrix's dots land in one device buffer and come back together
+  static double *gram_dev = nullptr, *gram_host = nullptr;
+  const int npair = (ell + 1) * (ell + 2) / 2;
+  if (!gram_dev) {
+    if (!QG_CUDA(cudaMalloc(&gram_dev, sizeof(double) * 2 * 153)) ||
+        !QG_CUDA(cudaMallocHost(&gram_host, sizeof(double) * 2 * 153)))
+      return 3;
+  }
+  // c_e = b_e + H_eo A^{-1} b_o / 2
+  if (!eo_split(be, bo, bd) || !eo_diag(to, bo, mp4, tm, true)) return 3;
+  if (!dslash_eo(ce, to, be, g, mp4, tm, false, 0, 0.5, false, 1, nullptr, ar)) return 3;
+  auto M = [&](qcdgpu_field o, qcdgpu_field i) {
+    return dslash_eo(ti, i, nullptr, gi, mp4, tm, false, 1, 1.0, true, 0, nullptr, ar) &&
+           dslash_eo(o, ti, i, gi, mp4, tm, false, 0, -0.25, false, 2, nullptr, ar);
+  };
+  auto M64 = [&](qcdgpu_field o, qcdgpu_field i) {
+    return dslash_eo(t64, i, nullptr, g, mp4, tm, false, 1, 1.0, true, 0, nullptr, ar) &&
+           dslash_eo(o, t64, i, g, mp4, tm, false, 0, -0.25, false, 2, nullptr, ar);
+  };
+  auto dotc = [&](qcdgpu_field a, qcdgpu_field c, cplx *d) {
+    double r[2];
+    if (!blas_dot(a, c, r)) return false;
+    *d = cplx(r[0], r[1]);
+    return true;
+  };
+  const double bn = sqrt(bn2), target = p->tol * bn;
+  // reliable-update threshold: FP64 iterations update only to confirm convergence
+  const double delta = prec == QCDGPU_F64 ? 0.0 : (p->delta > 0.0 && p->delta < 1.0 ? p->delta : 0.1);
+  if (!blas_zero(xe) || !blas_copy(re, ce) || !field_z4(rh, 0x5EEDull)) return 3;
+  double rn2;
+  if (!blas_norm2(re, &rn2)) return 3;
+  double rn = sqrt(rn2);
+  if (!convert_field(R[0], re) || !blas_zero(U[0]) || !blas_zero(xi)) return 3;
+  cplx rho0 = 1.0, alpha = 0.0, omega = 1.0;
+  double rmax = rn, best = rn;  // largest iterated residual since the last update; smallest true residual
+  int st = rn <= target ? 0 : 1, since = 0, stall = 0;
+  while (st != 0 && p->iters < p->maxiter) {
+    bool breakdown = false;
+    rho0 = -omega * rho0;
+    for (int j = 0; j < ell && !breakdown; j++) {
+      cplx rho1, gam;
+      if (!dotc(rh, R[j], &rho1)) return 3;
+      if (std::abs(rho1) == 0.0 || std::abs(rho0) == 0.0) {
+        breakdown = true;
+        break;
+      }
+      const cplx beta = alpha * rho1 / rho0;
+      rho0 = rho1;
+      for (int i = 0; i <= j; i++)  // u_i = r_i - beta u_i
+        if (!blas_axpby(U[i], 1.0, 0.0, R[i], -beta.real(), -beta.imag(), U[i])) return 3;
+      if (!M(U[j + 1], U[j])) return 3;
+      if (!dotc(rh, U[j + 1], &gam)) return 3;
+      if (std::abs(gam) == 0.0) {
+        breakdown = true;
+        break;
+      }
+      alpha = rho0 / gam;
+      for (int i = 0; i <= j; i++)  // r_i -= alpha u_{i+1}
+        if (!blas_axpby(R[i], -alpha.real(), -alpha.imag(), U[i + 1], 1.0, 0.0, R[i])) return 3;
+      if (!M(R[j + 1], R[j])) return 3;
+      if (!add_to_x(alpha, U[0])) return 3;
+      p->iters += 2;
+    }
+    double rr = 0.0;
+    if (!breakdown) {
+      // minimal-residual step from the Gram matrix of r_0 .. r_l
+      int k = 0;
+      for (int i = 0; i <= ell; i++)
+        for (int j = i; j <= ell; j++, k++)
+          if (!blas_dot_dev(R[i], R[j], gram_dev + 2 * k)) return 3;
+      if (!QG_CUDA(cudaMemcpyAsync(gram_host, gram_dev, sizeof(double) * 2 * npair, cudaMemcpyDeviceToHost,
+                                   stream())) ||
+          !QG_CUDA(cudaStreamSynchronize(stream())))
+        return 3;
+      std::vector<cplx> G((ell + 1) * (ell + 1));
+      k = 0;
+      for (int i = 0; i <= ell; i++)
+        for (int j = i; j <= ell; j++, k++) {
+          G[i * (ell + 1) + j] = cplx(gram_host[2 * k], gram_host[2 * k + 1]);
+          G[j * (ell + 1) + i] = std::conj(G[i * (ell + 1) + j]);
+        }
+      std::vector<cplx> A(ell * ell), c(ell), gm;
+      for (int i = 0; i < ell; i++) {
+        c[i] = G[(i + 1) * (ell + 1)];
+        for (int j = 0; j < ell; j++) A[i * ell + j] = G[(i + 1) * (ell + 1) + j + 1];
+      }
+      if (!small_solve(ell, A, c, gm) || std::abs(gm[ell - 1]) == 0.0) {
+        breakdown = true;
+      } else {
+        for (int j = 1; j <= ell; j++) {
+          const cplx gj = gm[j - 1];
+          if (!add_to_x(gj, R[j - 1]) || !blas_axpby(R[0], -gj.real(), -gj.imag(), R[j], 1.0, 0.0, R[0]) ||
+              !blas_axpby(U[0], -gj.real(), -gj.imag(), U[j], 1.0, 0.0, U[0]))
+            return 3;
+        }
+        omega = gm[ell - 1];
+        // |r_0 - R gamma|^2 = G_00 - c^+ gamma at the minimum
+        cplx cg = 0.0;
+        for (int i = 0; i < ell; i++) cg += std::conj(c[i]) * gm[i];
+        const double r2 = G[0].real() - cg.real();
+        rr = r2 > 0.0 ? sqrt(r2) : 0.0;
+      }
+    }
+    since++;
+    // reliable update: the iterated residual fell by delta (or looks
+    // converged, or the recurrence broke down, or a long plateau): fold the
+    // increment into x_e and continue from the FP64 true residual
+    if (breakdown || rr <= delta * rmax || rr <= target || since >= 256) {
+      if (!convert_field(e64, xi) || !blas_axpby(xe, 1.0, 0.0, e64, 1.0, 0.0, xe) || !blas_zero(xi)) return 3;
+      if (!M64(e64, xe) || !blas_axpby(re, 1.0, 0.0, ce, -1.0, 0.0, e64) || !blas_norm2(re, &rn2)) return 3;
+      rn = sqrt(rn2);
+      p->reliable_updates++;
+      since = 0;
+      if (rn <= target) {
+        st = 0;
+        break;
+      }
+      if (rn < 0.9 * best) {
+        best = rn;
+        stall = 0;
+      } else if (++stall >= 8) {
+        st = breakdown ? 2 : 1;
+        break;
+      }
+      if (!convert_field(R[0], re)) return 3;
+      rmax = rn;
+      if (breakdown) {  // start the recurrence afresh from the true residual
+        if (!blas_zero(U[0])) return 3;
+        rho0 = 1.0;
+        alpha = 0.0;
+        omega = 1.0;
+      }
+    } else if (rr > rmax) {
+      rmax = rr;
+    }
+  }
+  // x_o = A^{-1} b_o + A^{-1} H_oe x_e / 2, then the full true residual
+  if (!dslash_eo(xo, xe, to, g, mp4, tm, false, 1, 0.5, true, 1, nullptr, ar) || !eo_merge(x, xe, xo)) return 3;
+  qcdgpu_field rt = w.get(b->L, QCDGPU_F64);
+  double r2;
+  if (!rt || !dslash(rt, x, g, mp4, tm, QCDGPU_OP_D, QCDGPU_ARITH_DF64) ||
+      !blas_axpby(rt, 1.0, 0.0, bd, -1.0, 0.0, rt) || !blas_norm2(rt, &r2))
+    return 3;
+  p->true_residual = sqrt(r2 / bn2);
+  return st == 0 && p->true_residual > p->tol ? 1 : st;
 }
 
 }  // namespace qg

@@ -294,6 +294,8 @@ static int solve_bicgstab(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double
 
 // CGNR with device-resident scalars: cg.cu
 int solve_cgnr_eo(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, double tm, qcdgpu_solve_params *p);
+int solve_bicgstabl_eo(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, double tm,
+                       qcdgpu_solve_params *p);
 int solve_cgnr_engine(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, double tm,
                       qcdgpu_solve_params *p);
 
@@ -355,6 +357,7 @@ int solve(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, double tm,
   case QCDGPU_SOLVER_BICGSTAB: st = solve_bicgstab(x, b, g, mp4, tm, p); break;
   case QCDGPU_SOLVER_CGNR: st = solve_cgnr_engine(x, b, g, mp4, tm, p); break;
   case QCDGPU_SOLVER_CGNR_EO: st = solve_cgnr_eo(x, b, g, mp4, tm, p); break;
+  case QCDGPU_SOLVER_BICGSTABL_EO: st = solve_bicgstabl_eo(x, b, g, mp4, tm, p); break;
   default: set_error("solve: unknown solver %d", p->solver); st = 3;
   }
   p->status = st;
