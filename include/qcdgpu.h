@@ -196,6 +196,29 @@ int qcd_apeSmear3d(qcd_gaugeField *apeu, qcd_gaugeField *u, qcd_real_8 alpha);
 int qcd_gaussIteration3d(qcd_vector *v, qcd_gaugeField *u, qcd_real_8 alpha, qcd_uint_4 t);
 qcd_real_8 qcd_calculatePlaquette(qcd_gaugeField *u);
 
+/* include/qcd.h:16 and include/qcd_io.h:12-17: the string length the
+ * drivers use and the file type codes. */
+#ifndef qcd_MAX_STRING_LENGTH
+#define qcd_MAX_STRING_LENGTH 256
+#endif
+#ifndef qcd_GF_LIME
+#define qcd_GF_LIME 0
+#define qcd_PROP_CMI 0
+#define qcd_PROP_HMC 1
+#define qcd_PROP_HMCV 2
+#define qcd_PROP_LIME 3
+#define qcd_SOURCE_LIME 4
+#endif
+
+/* Parameter files, include/qcd_io.h:21-22 (lib/src/qcd_io.c:83-129).
+ * qcd_getParams returns the file in a malloc'd buffer (free it) with
+ * *len = size + 1 and a terminating zero; NULL if it cannot be read.
+ * qcd_getParam returns the text following the first occurrence of token,
+ * cut at the next '<' (written into params); an empty string if the token
+ * is absent (the reference returns the buffer's last bytes). */
+char *qcd_getParams(char *fname, int *len);
+char *qcd_getParam(char token[], char *params, int len);
+
 /* LIME files, include/qcd_io.h:26-43 (lib/src/qcd_io.c:204-540,984-1150,
  * 1766-1950). ILDG gauge configurations (precision 64 or 32, big-endian,
  * file order t,z,y,x and link directions x,y,z,t) and ETMC spinor files
@@ -207,7 +230,27 @@ int qcd_getGaugeLime(char *fname, qcd_gaugeField *u);
 int qcd_getGaugeField(char *fname, int type, qcd_gaugeField *u);
 int qcd_writeGaugeLime(char *fname, qcd_gaugeField *u, char *message);
 int qcd_getVectorLime(char *fname, qcd_vector *v);
+/* include/qcd_io.h:35-39 (lib/src/qcd_io.c:907-1340, dispatcher :1386): the
+ * legacy propagator vector files, big-endian [x][y][z][t][spin][colour]
+ * [re, im]: CMI float32 without header; HMC an ASCII line "beta kappa mu L
+ * T" then float64 data of all 12 source columns (column nu * 3 + c2 read);
+ * HMCV the same line and one column. The header line is read with the
+ * reference's fscanf format, whose trailing newline also skips whitespace
+ * bytes at the start of the data (the data offset follows it). Files
+ * shorter than the vector are an error (the reference reads past their
+ * end). qcd_getVector dispatches on type: qcd_PROP_CMI 0, qcd_PROP_HMC 1,
+ * qcd_PROP_HMCV 2, qcd_PROP_LIME 3. */
+int qcd_getVectorCMI(char *fname, qcd_uint_2 nu, qcd_uint_2 c2, qcd_vector *v);
+int qcd_getVectorHMC(char *fname, qcd_uint_2 nu, qcd_uint_2 c2, qcd_vector *v);
+int qcd_getVectorHMCV(char *fname, qcd_uint_2 nu, qcd_uint_2 c2, qcd_vector *v);
+int qcd_getVector(char *fname, int type, qcd_uint_2 nu, qcd_uint_2 c2, qcd_vector *v);
 int qcd_writeVectorLime(char *fname, int type, qcd_vector *v);
+/* include/qcd_io.h:42,44 (lib/src/qcd_io.c:1685, :1951): a CMI file
+ * (float32, rounded to nearest) and the writer dispatcher: qcd_PROP_CMI 0,
+ * qcd_PROP_LIME 3, qcd_SOURCE_LIME 4 (the reference's HMC writer is
+ * commented out). */
+int qcd_writeVectorCMI(char *fname, qcd_uint_2 nu, qcd_uint_2 c2, qcd_vector *v);
+int qcd_writeVector(char *fname, int type, qcd_uint_2 nu, qcd_uint_2 c2, qcd_vector *v);
 
 /* include/qcd_communication.h:12,21 (lib/src/qcd_communication.c:20,:343).
  * One GPU holds the whole lattice: no halo exists, both are no-ops that keep
@@ -381,6 +424,10 @@ int qcdgpu_release_work(void);
  * were exhausted, so that callers' out-of-memory paths run without
  * exhausting memory; n = 0 switches it off. */
 int qcdgpu_inject_alloc_failures(int n);
+/* Device bytes held by the lazily allocated partial-sum scratch of the
+ * reductions (dot products, norms, solver reductions); 0 until the first
+ * reduction. Lets a test see that an entry point allocated none. */
+int64_t qcdgpu_scratch_bytes(void);
 /* FMA throughput of this GPU in TFLOP/s (2 flops per FMA), kind 0 FP64 or 1
  * FP32, from a kernel of independent FMA chains on every SM (no reference
  * counterpart; the benchmark's compute ceilings). */
@@ -398,7 +445,9 @@ int qcdgpu_measure_fma_rate(int kind, double *tflops);
  * every call shares: n may not exceed 134,217,728 (larger n returns 1 with a
  * message), and calls that overlap on the GPU race on that array. The first
  * call on each device looks the array's address up; make it before any
- * stream capture. Returns 0, or 1 on error (qcdgpu_last_error). */
+ * stream capture. The address stays cached for the process, so the device
+ * may not be reset (cudaDeviceReset) while the library is in use. Returns 0,
+ * or 1 on error (qcdgpu_last_error). */
 int qcdgpu_dot_noalloc(const double *a, const double *b, int64_t n, double *result, void *stream);
 
 /* Source construction on device fields (FP64): n APE steps out <- in (out

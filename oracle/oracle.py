@@ -9,7 +9,11 @@ Two libraries:
 * ``Oracle`` -- the C restatement (``qcd_oracle.c``), built on any machine;
 * ``Reference`` -- the reference's own sources compiled unmodified
   (``_ref/libqcdref.so``); present only where the reference tree was
-  available at build time.
+  available at build time;
+* ``ReferenceIO`` -- the reference's file readers and writers
+  (``lib/src/qcd_io.c``) compiled unmodified (``_ref/libqcdio.so``), with a
+  single-rank MPI-IO stand-in and the LIME container restated from its
+  published format (``lime_format.c``; c-lime is not in the reference tree).
 
 All arrays use the reference host layout: spinors ``float64[V, 4, 3, 2]``,
 gauge fields ``float64[V, 4, 3, 3, 2]`` with site ``t + Lt*(x + Lx*(y + Ly*z))``.
@@ -25,6 +29,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libqcdref.so")
+REF_IO_SO = os.path.join(HERE, "_ref", "libqcdio.so")
 # where the reference's source tree lies, for `make ref`: the build entry
 # point passes it (environment variable QCD_REFERENCE_TREE)
 REF_TREE_ENV = "QCD_REFERENCE_TREE"
@@ -389,3 +394,46 @@ def site_rel_err(a, b):
     d = np.linalg.norm((a - b).reshape(V, -1), axis=1)
     n = np.linalg.norm(b.reshape(V, -1), axis=1)
     return float(np.max(d / np.where(n > 0, n, 1.0)))
+
+
+class ReferenceIO:
+    """The reference's own qcd_io.c readers and writers; single rank.
+    Vectors are float64[V, 4, 3, 2], gauge fields float64[V, 4, 3, 3, 2]."""
+
+    CMI, HMC, HMCV, PROP_LIME, SOURCE_LIME = 0, 1, 2, 3, 4
+
+    @staticmethod
+    def available() -> bool:
+        return os.path.exists(REF_IO_SO)
+
+    def __init__(self, path: str = REF_IO_SO):
+        lib = C.CDLL(path)
+        self.lib = lib
+        lib.refio_get_vector.argtypes = [_dp, C.c_char_p, _ip, C.c_int, C.c_int, C.c_int]
+        lib.refio_write_vector.argtypes = [_dp, C.c_char_p, _ip, C.c_int, C.c_int, C.c_int]
+        lib.refio_get_gauge.argtypes = [_dp, C.c_char_p, _ip]
+        lib.refio_write_gauge.argtypes = [_dp, C.c_char_p, _ip, C.c_char_p]
+        for n in ("refio_get_vector", "refio_write_vector", "refio_get_gauge", "refio_write_gauge"):
+            getattr(lib, n).restype = C.c_int
+
+    def get_vector(self, path, L, type_, nu=0, c2=0):
+        """(rc, vector); qcd_getVector (qcd_io.c:1386)"""
+        v = np.zeros((volume(L), 4, 3, 2))
+        rc = self.lib.refio_get_vector(v, os.fsencode(path), _L(L), type_, nu, c2)
+        return rc, v
+
+    def write_vector(self, v, path, L, type_, nu=0, c2=0) -> int:
+        """qcd_writeVector (qcd_io.c:1951): CMI or LIME"""
+        return self.lib.refio_write_vector(np.ascontiguousarray(v, dtype=np.float64), os.fsencode(path), _L(L),
+                                           type_, nu, c2)
+
+    def get_gauge(self, path, L):
+        """(rc, gauge); qcd_getGaugeField type qcd_GF_LIME (qcd_io.c:401)"""
+        u = np.zeros((volume(L), 4, 3, 3, 2))
+        rc = self.lib.refio_get_gauge(u, os.fsencode(path), _L(L))
+        return rc, u
+
+    def write_gauge(self, u, path, L, message="") -> int:
+        """qcd_writeGaugeLime (qcd_io.c:421)"""
+        return self.lib.refio_write_gauge(np.ascontiguousarray(u, dtype=np.float64), os.fsencode(path), _L(L),
+                                          message.encode())

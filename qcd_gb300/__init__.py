@@ -85,7 +85,8 @@ DROPIN_SYMBOLS = [
     "qcd_subVector", "qcd_addVector", "qcd_axpyVector", "qcd_mulAdjointVectorVector",
     "qcd_normVector", "qcd_gamma5Vector", "qcd_communicateVectorPMGaugeP", "qcd_waitall",
     "qcd_onePlusGamma", "qcd_oneMinusGamma", "qcd_applyU", "qcd_applyUDagger", "qcd_massTerms", "qcd_phaseMul",
-    "qcd_z2Vector",
+    "qcd_z2Vector", "qcd_getVectorCMI", "qcd_getVectorHMC", "qcd_getVectorHMCV", "qcd_getVector",
+    "qcd_writeVectorCMI", "qcd_writeVector", "qcd_getParams", "qcd_getParam",
     "gcr", "bicgstab", "cgnr",
 ]
 

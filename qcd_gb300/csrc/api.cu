@@ -788,6 +788,52 @@ qcd_real_8 qcd_calculatePlaquette(qcd_gaugeField *u)
   return plaquette(g);
 }
 
+// ------------------------------------------------------- parameter files
+// include/qcd_io.h:21 (lib/src/qcd_io.c:83-110): the whole file in a new
+// buffer (the caller frees it); *len = file size + 1, as the reference counts
+// it. The last byte is a terminating zero (the reference leaves it unset).
+char *qcd_getParams(char *fname, int *len)
+{
+  FILE *f = fname ? fopen(fname, "rb") : nullptr;
+  if (!f) {
+    set_error("Error, cannot open %s for reading", fname ? fname : "(null)");
+    return nullptr;
+  }
+  long n = -1;
+  if (fseek(f, 0, SEEK_END) == 0) n = ftell(f);
+  char *p = n >= 0 && n < INT32_MAX ? (char *)malloc((size_t)n + 1) : nullptr;
+  if (!p || fseek(f, 0, SEEK_SET) != 0 || fread(p, 1, (size_t)n, f) != (size_t)n) {
+    set_error("Error, cannot read %s", fname);
+    free(p);
+    fclose(f);
+    return nullptr;
+  }
+  fclose(f);
+  p[n] = '\0';
+  *len = (int)n + 1;
+  return p;
+}
+
+// include/qcd_io.h:22 (lib/src/qcd_io.c:114-129): the text after the first
+// occurrence of token, cut at the next '<' (written into params, as the
+// reference does). A missing token gives an empty string (the reference
+// returns the buffer's last bytes).
+char *qcd_getParam(char token[], char *params, int len)
+{
+  const int tl = (int)strlen(token);
+  for (int i = 0; i + tl < len; i++) {
+    if (memcmp(token, params + i, (size_t)tl) == 0) {
+      char *v = params + i + tl;
+      char *end = (char *)memchr(v, '<', (size_t)(len - i - tl));
+      if (end) *end = '\0';
+      return v;
+    }
+  }
+  static char empty[1];
+  empty[0] = '\0';
+  return empty;
+}
+
 // ------------------------------------------------------------ LIME files
 // include/qcd_io.h:26 (lib/src/qcd_io.c:204): ILDG configuration into u
 int qcd_getGaugeLime(char *fname, qcd_gaugeField *u)
@@ -852,6 +898,40 @@ int qcd_getVectorLime(char *fname, qcd_vector *v)
   return ok && vec_done(v) ? 0 : 1;
 }
 
+// include/qcd_io.h:35-39 (lib/src/qcd_io.c:907-1340, :1386): the legacy
+// vector formats and the dispatcher by type (0 CMI, 1 HMC, 2 HMCV, 3 LIME)
+static int get_legacy(char *fname, int type, qcd_uint_2 nu, qcd_uint_2 c2, qcd_vector *v)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  qcdgpu_field f = vec_out(v);
+  if (!f) return 1;
+  const size_t bytes = (size_t)f->V * 24 * sizeof(double);
+  void *dev = nullptr;
+  bool ok = QG_CUDA(cudaMalloc(&dev, bytes)) && legacy_read_spinor(fname, f->L, type, nu * 3 + c2, dev) &&
+            spinor_from_aos_dev(f, dev);
+  if (dev) {
+    cudaStreamSynchronize(stream());
+    cudaFree(dev);
+  }
+  return ok && vec_done(v) ? 0 : 1;
+}
+
+int qcd_getVectorCMI(char *fname, qcd_uint_2 nu, qcd_uint_2 c2, qcd_vector *v) { return get_legacy(fname, 0, nu, c2, v); }
+int qcd_getVectorHMC(char *fname, qcd_uint_2 nu, qcd_uint_2 c2, qcd_vector *v) { return get_legacy(fname, 1, nu, c2, v); }
+int qcd_getVectorHMCV(char *fname, qcd_uint_2 nu, qcd_uint_2 c2, qcd_vector *v) { return get_legacy(fname, 2, nu, c2, v); }
+
+int qcd_getVector(char *fname, int type, qcd_uint_2 nu, qcd_uint_2 c2, qcd_vector *v)
+{
+  if (!v || !v->initialized) {
+    set_error("Error in qcd_getVector! Vector must be properly initialized.");
+    return 1;
+  }
+  if (type >= 0 && type <= 2) return get_legacy(fname, type, nu, c2, v);
+  if (type == 3) return qcd_getVectorLime(fname, v);
+  set_error("process %i: Error in qcd_getVector! Unknown type.", v->geo ? (int)v->geo->myid : 0);
+  return 1;
+}
+
 // include/qcd_io.h:43 (lib/src/qcd_io.c:1766): type qcd_PROP_LIME (3) or qcd_SOURCE_LIME (4)
 int qcd_writeVectorLime(char *fname, int type, qcd_vector *v)
 {
@@ -868,6 +948,36 @@ int qcd_writeVectorLime(char *fname, int type, qcd_vector *v)
             lime_write_spinor(fname, f->L, dev, type == 4);
   if (dev) cudaFree(dev);
   return ok ? 0 : 1;
+}
+
+// include/qcd_io.h:42 (lib/src/qcd_io.c:1685): one vector as a CMI file;
+// nu and c2 are unused there too
+int qcd_writeVectorCMI(char *fname, qcd_uint_2 nu, qcd_uint_2 c2, qcd_vector *v)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  (void)nu;
+  (void)c2;
+  qcdgpu_field f = vec_in(v);
+  if (!f) return 1;
+  const size_t bytes = (size_t)f->V * 24 * sizeof(double);
+  void *dev = nullptr;
+  bool ok = QG_CUDA(cudaMalloc(&dev, bytes)) && spinor_to_aos_dev(f, dev) && cmi_write_spinor(fname, f->L, dev);
+  if (dev) cudaFree(dev);
+  return ok ? 0 : 1;
+}
+
+// include/qcd_io.h:44 (lib/src/qcd_io.c:1951): 0 CMI, 3 / 4 LIME propagator
+// / source (the reference's HMC writer is commented out)
+int qcd_writeVector(char *fname, int type, qcd_uint_2 nu, qcd_uint_2 c2, qcd_vector *v)
+{
+  if (!v || !v->initialized) {
+    set_error("Error in qcd_writeVector! Vector must be properly initialized.");
+    return 1;
+  }
+  if (type == 0) return qcd_writeVectorCMI(fname, nu, c2, v);
+  if (type == 3 || type == 4) return qcd_writeVectorLime(fname, type, v);
+  set_error("process %i: Error in qcd_writeVector! Unknown type.", v->geo ? (int)v->geo->myid : 0);
+  return 1;
 }
 
 // --------------------------------------------------------------- solvers

@@ -9,6 +9,8 @@
 // on scheduling (the reference's MPI_Allreduce becomes this second pass).
 #include <string.h>
 
+#include <complex>
+
 #include "internal.h"
 
 namespace qg {
@@ -365,6 +367,157 @@ bool blas_dot(qcdgpu_field a, qcdgpu_field b, double out[2])
   if (!r) return false;
   r += 2 * kMaxPartials;
   return blas_dot_dev(a, b, r) && fetch(r, out, 2);
+}
+
+
+// ------------------------------------------------ multi-dot, multi-axpy
+// Gram-Schmidt and solution updates of the Krylov solvers: k dot products
+// against one field in one pass, and one field plus k scaled fields in one
+// pass (FP64 fields of one shape, taken as flat arrays of 12 x stride complex
+// numbers: the padding holds zeros). Up to kMulti fields per launch; block
+// partial sums are added in a fixed order, so the results are deterministic.
+constexpr int kMulti = 8, kMultiThreads = 256, kMultiBlocks = 1024;
+
+struct MultiPtr {
+  const double2 *p[kMulti];
+  double2 a[kMulti];
+};
+
+template <int J>
+__global__ void __launch_bounds__(kMultiThreads) k_multi_dot(MultiPtr x, const double2 *y, int64_t n, double *part)
+{
+  double re[J], im[J];
+#pragma unroll
+  for (int j = 0; j < J; j++) re[j] = im[j] = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * kMultiThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kMultiThreads) {
+    const double2 b = y[i];
+#pragma unroll
+    for (int j = 0; j < J; j++) {
+      const double2 a = x.p[j][i];  // conj(a) b
+      re[j] = fma(a.x, b.x, fma(a.y, b.y, re[j]));
+      im[j] = fma(a.x, b.y, fma(-a.y, b.x, im[j]));
+    }
+  }
+  __shared__ double sh[kMultiThreads / 32][2 * kMulti];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < J; j++) {
+    for (int o = 16; o > 0; o >>= 1) {
+      re[j] += __shfl_xor_sync(0xffffffffu, re[j], o);
+      im[j] += __shfl_xor_sync(0xffffffffu, im[j], o);
+    }
+    if (lane == 0) {
+      sh[w][2 * j] = re[j];
+      sh[w][2 * j + 1] = im[j];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 2 * J) {
+    double t = 0.0;
+    for (int k = 0; k < kMultiThreads / 32; k++) t += sh[k][threadIdx.x];
+    part[(int64_t)blockIdx.x * 2 * kMulti + threadIdx.x] = t;
+  }
+}
+
+template <int J>
+__global__ void __launch_bounds__(kMultiThreads) k_multi_axpy(MultiPtr x, double2 *y, int64_t n)
+{
+  for (int64_t i = (int64_t)blockIdx.x * kMultiThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kMultiThreads) {
+    double2 v = y[i];
+#pragma unroll
+    for (int j = 0; j < J; j++) {
+      const double2 b = x.p[j][i], c = x.a[j];
+      v.x = fma(c.x, b.x, fma(-c.y, b.y, v.x));
+      v.y = fma(c.x, b.y, fma(c.y, b.x, v.y));
+    }
+    y[i] = v;
+  }
+}
+
+static unsigned multi_blocks(int64_t n)
+{
+  const int64_t b = (n + kMultiThreads - 1) / kMultiThreads;
+  return (unsigned)(b < kMultiBlocks ? b : kMultiBlocks);
+}
+
+bool blas_multi_dot(const qcdgpu_field *x, int k, qcdgpu_field y, std::complex<double> *out)
+{
+  if (k <= 0) return true;
+  for (int j = 0; j < k; j++)
+    if (!same_shape(x[j], y) || x[j]->prec != QCDGPU_F64 || y->prec != QCDGPU_F64) {
+      set_error("multi-dot: FP64 fields of one shape");
+      return false;
+    }
+  static double *part = nullptr, *host = nullptr;
+  if (!part) {
+    if (!QG_CUDA(cudaMalloc(&part, sizeof(double) * 2 * kMulti * kMultiBlocks))) return false;
+    if (!QG_CUDA(cudaMallocHost(&host, sizeof(double) * 2 * kMulti * kMultiBlocks))) return false;
+  }
+  const int64_t n = 12 * y->stride;
+  const unsigned nb = multi_blocks(n);
+  cudaStream_t st = stream();
+  for (int j0 = 0; j0 < k; j0 += kMulti) {
+    const int J = k - j0 < kMulti ? k - j0 : kMulti;
+    MultiPtr mp{};
+    for (int j = 0; j < J; j++) mp.p[j] = (const double2 *)x[j0 + j]->data;
+    const double2 *yy = (const double2 *)y->data;
+    switch (J) {
+    case 1: k_multi_dot<1><<<nb, kMultiThreads, 0, st>>>(mp, yy, n, part); break;
+    case 2: k_multi_dot<2><<<nb, kMultiThreads, 0, st>>>(mp, yy, n, part); break;
+    case 3: k_multi_dot<3><<<nb, kMultiThreads, 0, st>>>(mp, yy, n, part); break;
+    case 4: k_multi_dot<4><<<nb, kMultiThreads, 0, st>>>(mp, yy, n, part); break;
+    case 5: k_multi_dot<5><<<nb, kMultiThreads, 0, st>>>(mp, yy, n, part); break;
+    case 6: k_multi_dot<6><<<nb, kMultiThreads, 0, st>>>(mp, yy, n, part); break;
+    case 7: k_multi_dot<7><<<nb, kMultiThreads, 0, st>>>(mp, yy, n, part); break;
+    default: k_multi_dot<8><<<nb, kMultiThreads, 0, st>>>(mp, yy, n, part); break;
+    }
+    if (!QG_LAUNCHED("multi_dot")) return false;
+    if (!QG_CUDA(cudaMemcpyAsync(host, part, sizeof(double) * 2 * kMulti * nb, cudaMemcpyDeviceToHost, st)) ||
+        !QG_CUDA(cudaStreamSynchronize(st)))
+      return false;
+    for (int j = 0; j < J; j++) {
+      double re = 0.0, im = 0.0;  // block order: deterministic
+      for (unsigned b = 0; b < nb; b++) {
+        re += host[(size_t)b * 2 * kMulti + 2 * j];
+        im += host[(size_t)b * 2 * kMulti + 2 * j + 1];
+      }
+      out[j0 + j] = std::complex<double>(re, im);
+    }
+  }
+  return true;
+}
+
+bool blas_multi_axpy(qcdgpu_field y, const qcdgpu_field *x, const std::complex<double> *a, int k)
+{
+  for (int j = 0; j < k; j++)
+    if (!same_shape(x[j], y) || x[j]->prec != QCDGPU_F64 || y->prec != QCDGPU_F64) {
+      set_error("multi-axpy: FP64 fields of one shape");
+      return false;
+    }
+  const int64_t n = 12 * y->stride;
+  const unsigned nb = multi_blocks(n);
+  cudaStream_t st = stream();
+  for (int j0 = 0; j0 < k; j0 += kMulti) {
+    const int J = k - j0 < kMulti ? k - j0 : kMulti;
+    MultiPtr mp{};
+    for (int j = 0; j < J; j++) {
+      mp.p[j] = (const double2 *)x[j0 + j]->data;
+      mp.a[j] = make_double2(a[j0 + j].real(), a[j0 + j].imag());
+    }
+    double2 *yy = (double2 *)y->data;
+    switch (J) {
+    case 1: k_multi_axpy<1><<<nb, kMultiThreads, 0, st>>>(mp, yy, n); break;
+    case 2: k_multi_axpy<2><<<nb, kMultiThreads, 0, st>>>(mp, yy, n); break;
+    case 3: k_multi_axpy<3><<<nb, kMultiThreads, 0, st>>>(mp, yy, n); break;
+    case 4: k_multi_axpy<4><<<nb, kMultiThreads, 0, st>>>(mp, yy, n); break;
+    case 5: k_multi_axpy<5><<<nb, kMultiThreads, 0, st>>>(mp, yy, n); break;
+    case 6: k_multi_axpy<6><<<nb, kMultiThreads, 0, st>>>(mp, yy, n); break;
+    case 7: k_multi_axpy<7><<<nb, kMultiThreads, 0, st>>>(mp, yy, n); break;
+    default: k_multi_axpy<8><<<nb, kMultiThreads, 0, st>>>(mp, yy, n); break;
+    }
+    if (!QG_LAUNCHED("multi_axpy")) return false;
+  }
+  return true;
 }
 
 }  // namespace qg

@@ -25,6 +25,7 @@
 #include <stdio.h>
 
 #include <atomic>
+#include <complex>
 #include <string>
 
 #include "../../include/qcdgpu.h"
@@ -142,6 +143,10 @@ bool dslash_sites_aos(void *out_aos, const void *in_aos, qcdgpu_field shape, qcd
 bool lime_read_gauge(const char *fname, const int L[4], void *dev_aos);
 bool lime_write_gauge(const char *fname, const int L[4], const void *dev_aos, const char *message);
 bool lime_read_spinor(const char *fname, const int L[4], void *dev_aos);
+// legacy CMI (type 0), HMC (1) and HMCV (2) vector files, column col (HMC)
+bool legacy_read_spinor(const char *fname, const int L[4], int type, int col, void *dev_aos);
+// CMI vector file (big-endian float32, [x][y][z][t][spin][colour][re, im])
+bool cmi_write_spinor(const char *fname, const int L[4], const void *dev_aos);
 bool lime_write_spinor(const char *fname, const int L[4], const void *dev_aos, bool source);
 
 // dslash.cu: out = op(in) with diagonal mp4 = m + 4 and twisted mass tm
@@ -179,6 +184,10 @@ bool blas_norm2_dev(qcdgpu_field x, double *res);
 bool blas_dot_dev(qcdgpu_field a, qcdgpu_field b, double *res);
 // host-returning versions (synchronise)
 bool blas_norm2(qcdgpu_field x, double *out);
+// FP64 fields: out[j] = <x_j, y> for j < k in one pass per 8 fields (host
+// results, fixed summation order); y += sum_j a_j x_j in one pass per 8
+bool blas_multi_dot(const qcdgpu_field *x, int k, qcdgpu_field y, std::complex<double> *out);
+bool blas_multi_axpy(qcdgpu_field y, const qcdgpu_field *x, const std::complex<double> *a, int k);
 bool blas_dot(qcdgpu_field a, qcdgpu_field b, double out[2]);
 // fused: y = y + a*x  followed by |y|^2 (device result)
 bool blas_axpy_norm2_dev(qcdgpu_field y, double ar, double ai, qcdgpu_field x, double *res);

@@ -60,6 +60,11 @@ bool lime_scan(FILE *f, std::vector<LimeRec> &recs)
 {
   unsigned char h[kLimeHeader];
   int64_t pos = 0;
+  if (fseeko(f, 0, SEEK_END) != 0) {
+    set_error("LIME: cannot size the file");
+    return false;
+  }
+  const int64_t fsize = (int64_t)ftello(f);
   while (true) {
     if (fseeko(f, pos, SEEK_SET) != 0) break;
     size_t n = fread(h, 1, kLimeHeader, f);
@@ -72,6 +77,12 @@ bool lime_scan(FILE *f, std::vector<LimeRec> &recs)
     r.len = get_be(h + 8, 8);
     r.type.assign((const char *)h + 16, strnlen((const char *)h + 16, 128));
     r.data_off = pos + kLimeHeader;
+    // a corrupt length must not run past the file (nor overflow the next offset)
+    if (r.len > (uint64_t)(fsize - r.data_off)) {
+      set_error("LIME: record at byte %lld claims %llu bytes, past the end of the file", (long long)pos,
+                (unsigned long long)r.len);
+      return false;
+    }
     recs.push_back(r);
     pos = r.data_off + (int64_t)((r.len + 7) / 8 * 8);
   }
@@ -377,6 +388,120 @@ bool lime_write_spinor(const char *fname, const int L[4], const void *dev_aos, b
     return false;
   }
   return true;
+}
+
+// Legacy propagator vector files (lib/src/qcd_io.c:907-1340, dispatcher
+// :1386). All three hold big-endian reals in the order [x][y][z][t][spin]
+// [colour][re, im] (x slowest, t fastest): CMI (type 0) float32 with no
+// header; HMC (type 1) an ASCII line "beta kappa mu L T" and then float64
+// data of all twelve source columns, column nu * 3 + c2 at (nu * 3 + c2) x 24 V
+// reals after the line; HMCV (type 2) the same line and one column.
+// file site i = ((x * Ly + y) * Lz + z) * Lt + t -> host layout (24 reals)
+__global__ void k_xyzt_to_aos(double *dst, const unsigned char *src, Dims d, int64_t nsites, int prec)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nsites) return;
+  int64_t s = i;
+  const int t = (int)(s % d.L[0]);
+  s /= d.L[0];
+  const int z = (int)(s % d.L[3]);
+  s /= d.L[3];
+  const int y = (int)(s % d.L[2]);
+  const int x = (int)(s / d.L[2]);
+  const int64_t site = t + (int64_t)d.L[0] * (x + (int64_t)d.L[1] * (y + (int64_t)d.L[2] * z));
+  const int w = prec / 8;
+#pragma unroll
+  for (int k = 0; k < 24; k++) dst[site * 24 + k] = be_real(src + (i * 24 + k) * w, prec);
+}
+
+// host layout -> CMI file order, big-endian float32 (rounded to nearest
+// as qcd_writeVectorCMI's double-to-float assignment, qcd_io.c:1741-1750)
+__global__ void k_aos_to_xyzt32(unsigned char *dst, const double *src, Dims d, int64_t nsites)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nsites) return;
+  int64_t s = i;
+  const int t = (int)(s % d.L[0]);
+  s /= d.L[0];
+  const int z = (int)(s % d.L[3]);
+  s /= d.L[3];
+  const int y = (int)(s % d.L[2]);
+  const int x = (int)(s / d.L[2]);
+  const int64_t site = t + (int64_t)d.L[0] * (x + (int64_t)d.L[1] * (y + (int64_t)d.L[2] * z));
+#pragma unroll
+  for (int k = 0; k < 24; k++)
+    *(unsigned *)(dst + (i * 24 + k) * 4) = __byte_perm(__float_as_uint((float)src[site * 24 + k]), 0, 0x0123);
+}
+
+bool cmi_write_spinor(const char *fname, const int L[4], const void *dev_aos)
+{
+  const int64_t V = (int64_t)L[0] * L[1] * L[2] * L[3];
+  const uint64_t bytes = (uint64_t)V * 24 * 4;
+  Bytes b;
+  if (!b.alloc(bytes)) return false;
+  Dims d;
+  memcpy(d.L, L, sizeof(d.L));
+  k_aos_to_xyzt32<<<(unsigned)((V + 127) / 128), 128, 0, stream()>>>((unsigned char *)b.dev, (const double *)dev_aos,
+                                                                      d, V);
+  if (!QG_LAUNCHED("aos_to_xyzt32") ||
+      !QG_CUDA(cudaMemcpyAsync(b.host, b.dev, bytes, cudaMemcpyDeviceToHost, stream())) ||
+      !QG_CUDA(cudaStreamSynchronize(stream())))
+    return false;
+  File file(fname, "wb");
+  if (!file.f) {
+    set_error("process 0: Error in qcd_writeVectorCMI! Cannot open %s for writing", fname);
+    return false;
+  }
+  if (fwrite(b.host, 1, bytes, file.f) != bytes) {
+    set_error("qcd_writeVectorCMI: short write to %s", fname);
+    return false;
+  }
+  return true;
+}
+
+bool legacy_read_spinor(const char *fname, const int L[4], int type, int col, void *dev_aos)
+{
+  const char *name = type == 0 ? "qcd_getVectorCMI" : type == 1 ? "qcd_getVectorHMC" : "qcd_getVectorHMCV";
+  if (type < 0 || type > 2 || col < 0 || col > 11) {
+    set_error("%s: type 0..2 and a source column 0..11", name);
+    return false;
+  }
+  File file(fname, "rb");
+  if (!file.f) {
+    set_error("%s! Cannot open %s for reading", name, fname);
+    return false;
+  }
+  const int64_t V = (int64_t)L[0] * L[1] * L[2] * L[3];
+  const int prec = type == 0 ? 32 : 64;
+  int64_t off = 0;
+  if (type != 0) {  // the header line, read as the reference reads it
+    double beta, kappa, mu;
+    int fL = -1, fT = -1;
+    if (fscanf(file.f, "%lf %lf %lf %d %d\n", &beta, &kappa, &mu, &fL, &fT) != 5 || fL != L[1] || fT != L[0]) {
+      set_error("%s! Dimensions in file %s don't match geometry!", name, fname);
+      return false;
+    }
+    off = (int64_t)ftello(file.f);
+    if (type == 1) off += (int64_t)col * 24 * V * 8;
+  }
+  const uint64_t need = (uint64_t)V * 24 * (prec / 8);
+  if (fseeko(file.f, 0, SEEK_END) != 0 || (int64_t)ftello(file.f) < off + (int64_t)need) {
+    set_error("%s! %s is shorter than a %lldx%lldx%lldx%lld vector%s", name, fname, (long long)L[1],
+              (long long)L[2], (long long)L[3], (long long)L[0], type == 1 ? " column" : "");
+    return false;
+  }
+  Bytes b;
+  if (!b.alloc(need)) return false;
+  if (fseeko(file.f, off, SEEK_SET) != 0 || fread(b.host, 1, need, file.f) != need) {
+    set_error("%s! short read of %s", name, fname);
+    return false;
+  }
+  if (!QG_CUDA(cudaMemcpyAsync(b.dev, b.host, need, cudaMemcpyHostToDevice, stream()))) return false;
+  Dims d;
+  memcpy(d.L, L, sizeof(d.L));
+  k_xyzt_to_aos<<<(unsigned)((V + 127) / 128), 128, 0, stream()>>>((double *)dev_aos, (const unsigned char *)b.dev,
+                                                                    d, V, prec);
+  return QG_LAUNCHED("legacy_to_aos") && QG_CUDA(cudaStreamSynchronize(stream()));
 }
 
 }  // namespace qg

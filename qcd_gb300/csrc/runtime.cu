@@ -277,6 +277,12 @@ int qcdgpu_inject_alloc_failures(int n)
   return 0;
 }
 
+int64_t qcdgpu_scratch_bytes(void)
+{
+  return (qg::g_scratch ? (int64_t)sizeof(double) * (2 * qg::kMaxPartials + 64) : 0) +
+         (int64_t)sizeof(double) * qg::g_big_n;
+}
+
 int qcdgpu_release_work(void)
 {
   qg::work_trim();

@@ -136,11 +136,15 @@ int gcr_dropin(qcdgpu_field sol, qcdgpu_field src, qcdgpu_gauge g, double mp4, d
   for (int k = 1; k < n; k++) {
     if (!caxpy(res[(size_t)k], -c[(size_t)k - 1], chi[(size_t)k - 1], res[(size_t)k - 1])) return 1;
     if (!dslash(chi[(size_t)k], res[(size_t)k], g, mp4, tm, QCDGPU_OP_Q, -1)) return 1;
-    for (int j = 0; j < k; j++) {
-      cplx t;
-      if (!dot(chi[(size_t)j], chi[(size_t)k], &t)) return 1;
-      A(k, j) = -t;
-      if (!caxpy(chi[(size_t)k], A(k, j), chi[(size_t)j], chi[(size_t)k])) return 1;
+    // Gram-Schmidt against the orthonormal chi_0 .. chi_{k-1}: the k
+    // projections in one pass, then one batched update (classical form; for
+    // an orthonormal basis its coefficients are modified Gram-Schmidt's,
+    // invert.c:68-79)
+    {
+      std::vector<cplx> t((size_t)k);
+      if (!blas_multi_dot(chi.data(), k, chi[(size_t)k], t.data())) return 1;
+      for (int j = 0; j < k; j++) A(k, j) = -t[(size_t)j];
+      if (!blas_multi_axpy(chi[(size_t)k], chi.data(), &A(k, 0), k)) return 1;
     }
     if (!norm(chi[(size_t)k], &nv)) return 1;
     A(k, k) = 1.0 / nv;
@@ -155,8 +159,11 @@ int gcr_dropin(qcdgpu_field sol, qcdgpu_field src, qcdgpu_gauge g, double mp4, d
       for (int l = j + 1; l < k; l++) A(k, j) += A(k, l) * A(l, j);
     }
     if (!dot(chi[(size_t)k], src, &c[(size_t)k])) return 1;
-    for (int j = 0; j <= k; j++)
-      if (!caxpy(sol, c[(size_t)k] * A(k, j), res[(size_t)j], sol)) return 1;
+    {
+      std::vector<cplx> coef((size_t)k + 1);
+      for (int j = 0; j <= k; j++) coef[(size_t)j] = c[(size_t)k] * A(k, j);
+      if (!blas_multi_axpy(sol, res.data(), coef.data(), k + 1)) return 1;
+    }
   }
   return 0;
 }

@@ -51,6 +51,15 @@ def ref():
 
 
 @pytest.fixture(scope="session")
+def refio():
+    from oracle.oracle import ReferenceIO
+
+    if not ReferenceIO.available():
+        pytest.skip("reference file readers not built here (needs the reference source tree)")
+    return ReferenceIO()
+
+
+@pytest.fixture(scope="session")
 def qlib():
     import qcd_gb300
     from qcd_gb300 import build

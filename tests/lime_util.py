@@ -44,6 +44,13 @@ def etmc_payload(v: np.ndarray, L, prec=64) -> bytes:
     return np.ascontiguousarray(a).astype(">f8" if prec == 64 else ">f4").tobytes()
 
 
+def etmc_array(data: bytes, L, prec=64) -> np.ndarray:
+    """ETMC payload -> (V, 4, 3, 2) in qcd_lib order (the inverse of etmc_payload)"""
+    Lt, Lx, Ly, Lz = L
+    a = np.frombuffer(data, dtype=">f8" if prec == 64 else ">f4").astype(np.float64)
+    return np.ascontiguousarray(a.reshape(Lt, Lz, Ly, Lx, 4, 3, 2).transpose(1, 2, 3, 0, 4, 5, 6)).reshape(-1, 4, 3, 2)
+
+
 def ildg_file(u, L, prec=64) -> bytes:
     xml = (f"<?xml version=\"1.0\"?>\n<ildgFormat>\n<field>su3gauge</field>\n<precision>{prec}</precision>\n"
            f"<lx>{L[1]}</lx><ly>{L[2]}</ly><lz>{L[3]}</lz><lt>{L[0]}</lt>\n</ildgFormat>").encode()

@@ -234,3 +234,64 @@ def test_site_helpers_algebra(qlib):
     assert np.allclose(cx(a), vc @ uc.conj(), atol=1e-14)
     lib.qcd_massTerms(a, vec, 4.3, -0.27)
     assert np.allclose(cx(a), 4.3 * vc + 1j * -0.27 * (G[5] @ vc), atol=1e-14)
+
+
+@pytest.mark.parametrize("driver", ["invert", "b_minus_Dx"])
+def test_reference_drivers_link_unmodified(qlib, tmp_path, driver):
+    """the reference's own drivers, compiled unmodified against include/qcd.h
+    (oracle/Makefile ref), link against the library with nothing else: every
+    qcd_lib call they make is exported (invert.c keeps its own gcr())"""
+    import subprocess
+
+    from oracle.oracle import HERE
+
+    obj = os.path.join(HERE, "_ref", f"{driver}_dropin.o")
+    if not os.path.exists(obj):
+        pytest.skip("reference drivers not built here (needs the reference source tree)")
+    exe = tmp_path / driver
+    out = subprocess.run(["gcc", obj, "-o", str(exe), q.LIB_PATH, "-lm"], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+
+
+PARAMS = (b"<processors_txyz>1 1 1 1</processors_txyz>\n<lattice_txyz>16 8 8 8</lattice_txyz>\n"
+          b"<source_type>HMC_PROPAGATOR</source_type>\n<source>/data/prop.src</source>\n"
+          b"<solution>/data/prop.src_inverted</solution>\n<cfg_name>/data/conf.2000</cfg_name>\n"
+          b"<N_restart>32</N_restart>\n<kappa>0.160856</kappa>\n<mu>0.0085</mu>\n")
+TAGS = ["<lattice_txyz>", "<source>", "<solution>", "<cfg_name>", "<N_restart>", "<kappa>", "<mu>",
+        "<processors_txyz>"]
+
+
+def _params(lib, path):
+    lib.qcd_getParams.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
+    lib.qcd_getParams.restype = C.c_void_p
+    lib.qcd_getParam.argtypes = [C.c_char_p, C.c_void_p, C.c_int]
+    lib.qcd_getParam.restype = C.c_char_p
+    n = C.c_int()
+    buf = lib.qcd_getParams(str(path).encode(), C.byref(n))
+    return buf, n.value
+
+
+def test_parameter_file_parsing(qlib, tmp_path):
+    """qcd_getParams / qcd_getParam (qcd_io.c:83-129): len = size + 1, values
+    cut at the next '<', tags found in any order; a missing file is NULL"""
+    p = tmp_path / "invert.ini"
+    p.write_bytes(PARAMS)
+    buf, n = _params(qlib, p)
+    assert buf and n == len(PARAMS) + 1
+    got = {t: qlib.qcd_getParam(t.encode(), buf, n) for t in TAGS}
+    assert got["<lattice_txyz>"] == b"16 8 8 8" and got["<source>"] == b"/data/prop.src"
+    assert got["<solution>"] == b"/data/prop.src_inverted" and got["<mu>"] == b"0.0085"
+    assert got["<processors_txyz>"] == b"1 1 1 1"  # found after later tags were cut
+    assert qlib.qcd_getParam(b"<absent>", buf, n) == b""
+    assert _params(qlib, tmp_path / "missing.ini")[0] is None
+
+
+def test_parameter_file_parsing_matches_reference(qlib, refio, tmp_path):
+    """the same values as the reference's own qcd_getParams / qcd_getParam"""
+    p = tmp_path / "invert.ini"
+    p.write_bytes(PARAMS)
+    mine, n = _params(qlib, p)
+    theirs, m = _params(refio.lib, p)
+    assert n == m
+    for t in TAGS:
+        assert qlib.qcd_getParam(t.encode(), mine, n) == refio.lib.qcd_getParam(t.encode(), theirs, m), t
