@@ -516,7 +516,7 @@ int qcdgpu_mrhs_tc_timeouts(unsigned *n);
 int qcdgpu_mrhs_tc_reset(void);
 /* Test hook: with skip_mma != 0 the tcgen05 kernel issues no MMA, so its
  * waits run out after `polls` mbarrier polls and the launch reports the
- * timeout; (0, 0) restores normal operation (2^24 polls). */
+ * timeout; (0, 0) restores normal operation (2^20 polls). */
 int qcdgpu_mrhs_tc_test_hook(int skip_mma, int polls);
 
 /* Batched solver with continuous admission (no reference counterpart). A

@@ -563,40 +563,74 @@ __global__ void k_mnorm(const __half2 *d, const float *dn, int V, int N, int nac
 
 // ------------------------------------------------- tensor cores (tcgen05)
 // One GEMM per site and 16-slot group holds all eight hops:
-//   D^T (24 x 16) = L (24 x 96) H^T (96 x 16),
-// FP16 operands, FP32 accumulator in tensor memory. Row o = (spin S, colour
-// i, re/im) of L is the site's link matrix: in K block h (12 values: input
-// spin s, colour j, re/im) it holds the realified c M_ij, where M = U_mu (or
-// U_mu^+ for backward hops, boundary phase folded in) and c the entry (0, 1,
-// +-1 or +-i) of the 4 x 2 matrix that rebuilds spin S from the projected
-// upper half of (1 +- g_mu); L is built once per site for all slots. Row n of
-// H is slot n's projected half spinor at each of the eight neighbours (packed
-// half pairs, as the FP16 kernels project them), scaled by that neighbour's
-// norm over the slot's largest. The MMA is issued with M = 64 (the smallest
-// M): rows 24..63 of the A operand read whatever follows in shared memory and
-// land in accumulator rows that are never read. Per tile of 8 sites: 128
-// threads build L (two threads per site and hop) and H (one thread per site
-// and slot), one thread issues 8 x 6 MMAs (M = 64, N = 16, K = 16) into 128
-// tensor-memory columns and commits them to an mbarrier, warps 0 and 1 read
-// the 24 accumulator rows back, and the epilogue (diagonal term, A^{-1}, FP16
-// rounding with per-site norm, per-slot |out|^2) runs one thread per site and
-// slot. The slot's rescale factor multiplies the accumulator back.
-constexpr int kTcSites = 8;     // sites per tile (one MMA chain each)
-constexpr int kTcTiles = 16;    // tiles per CTA
-constexpr int kTcThreads = 128;
-constexpr int kTcK = 96;                                       // 8 hops x 12
-constexpr uint32_t kTcSbo = (kTcK / 8) * 128;                  // bytes per 8-row group
-constexpr size_t kTcLBytes = (size_t)kTcSites * 3 * kTcSbo;    // 24 rows per site
-constexpr size_t kTcHBytes = (size_t)kTcSites * 2 * kTcSbo;    // 16 rows per site
-constexpr size_t kTcSmem = kTcLBytes + kTcHBytes + sizeof(double) * kTcSites * 16;
-// the M = 64 operand of the last site reads 64 rows from its start: inside the allocation
-static_assert((kTcSites - 1) * 3 * kTcSbo + 8 * kTcSbo <= kTcSmem, "tcgen05 A operand overruns shared memory");
+//   D^T (24 x 16) = L (24 x 128) H^T (128 x 16),
+// FP16 operands, FP32 accumulator in tensor memory. K = (hop h, input spin
+// s, colour j, re/im) in blocks of 8: each (hop, spin) is the six values of
+// three colours and two zero pads, one 16-byte core-matrix row, so every
+// operand row is written with aligned 16-byte stores. Row o = (spin S,
+// colour i, re/im) of L holds, in block (h, src), the realified c M_ij
+// (row re: (Re z, -Im z), row im: (Im z, Re z), z = c M_ij), where M = U_mu
+// (or U_mu^+ for backward hops, boundary phase folded in) and c (1, -1, i or
+// -i) and src the coefficient and source spin that rebuild spin S from the
+// projected upper half of (1 +- g_mu) (the rules of accumulate<MU, S>); the
+// blocks of the other source spin are zero. L is built once per site for all
+// slot groups. Row n of H is slot n's projected half spinor at each of the
+// eight neighbours (packed half pairs, as the FP16 kernels project them),
+// scaled by that neighbour's norm over the slot's largest. The MMA is issued
+// with M = 64 (the smallest): rows 24..63 of the A operand read whatever
+// follows in shared memory and land in accumulator rows that are never read.
+//
+// A CTA (two per SM, persistent over tiles of 4 sites) is a pipeline of warp
+// roles over work items (tile, slot group), with the operand buffers and the
+// tensor-memory accumulators double-buffered:
+//  - warps 0..3 build L (first group of a tile) and H of item n into buffer
+//    n % 2, once the MMAs of item n - 2 have completed (every global load of
+//    the item is issued before that wait), and arrive on full;
+//  - one thread of warp 6 issues the item's 4 sites x 8 MMAs (M = 64, N = 16,
+//    K = 16, no-swizzle K-major descriptors) into 64 tensor-memory columns
+//    once full has completed and the epilogue has drained that accumulator
+//    buffer, and commits them to the item's done barrier (it also arrives on
+//    sready, which hands the producers' per-slot rescale factors, read from
+//    shared memory, on to the epilogue with release / acquire ordering);
+//  - warps 4 and 5 wait for done, copy the 24 accumulator rows (TMEM lanes
+//    0..15 and 32..39) to shared memory, release the accumulator buffer and
+//    run the epilogue (slot rescale, diagonal term, A^{-1}, FP16 rounding with
+//    the per-site norm, per-slot |out|^2 in a fixed order), one thread per
+//    site and slot.
+// Every mbarrier wait is bounded (ctl.polls); a wait that runs out sets the
+// failure flag and its thread stops waiting, so the launch always ends (with
+// its output invalid and the failure reported to the host).
+constexpr int kTcSites = 4;                                 // sites per tile
+constexpr int kTcK = 128;                                   // 8 hops x 2 spins x 8
+constexpr uint32_t kTcSbo = (kTcK / 8) * 128;               // bytes per 8-row group
+constexpr uint32_t kTcLSite = 3 * kTcSbo;                   // 24 rows of L per site
+constexpr uint32_t kTcHSite = 2 * kTcSbo;                   // 16 rows of H per site
+constexpr uint32_t kTcLBuf = kTcSites * kTcLSite, kTcHBuf = kTcSites * kTcHSite;
+constexpr int kTcPairs = kTcSites * 16;                     // (site, slot) pairs of an item
+constexpr int kTcProd = 2 * kTcPairs, kTcEpi = kTcPairs;    // producer and epilogue threads
+constexpr int kTcThreads = kTcProd + kTcEpi + 32;           // + the MMA warp
+constexpr int kTcEpiWarp0 = kTcProd / 32;                   // warps 4, 5 (TMEM lanes 0..31, 32..63)
+constexpr int kTcMmaWarp = kTcEpiWarp0 + kTcEpi / 32;       // warp 6
+constexpr uint32_t kTcCols = 2 * kTcSites * 16;             // tensor-memory columns (two buffers)
+static_assert(kTcEpiWarp0 % 4 == 0 && kTcEpi == 64, "epilogue warps must cover TMEM lanes 0..63");
+// dynamic shared memory: L[2], H[2], X (accumulators for the epilogue), the
+// slots' rescale factors of four items, per-slot partial sums, neighbours
+constexpr uint32_t kTcOffH = 2 * kTcLBuf;
+constexpr uint32_t kTcOffX = kTcOffH + 2 * kTcHBuf;
+constexpr uint32_t kTcOffScl = kTcOffX + kTcSites * 16 * 24 * 4;
+constexpr uint32_t kTcOffRed = kTcOffScl + 4 * kTcPairs * 4;
+constexpr uint32_t kTcOffNb = kTcOffRed + kTcPairs * 8;
+constexpr size_t kTcSmem = kTcOffNb + kTcSites * 9 * 4;
+// the M = 64 operand of the last site of L[1] reads 64 rows from its start:
+// inside the allocation
+static_assert(kTcLBuf + (kTcSites - 1) * kTcLSite + 8 * kTcSbo <= kTcSmem, "tcgen05 A operand overruns shared memory");
+static_assert(2 * kTcSmem <= 226 * 1024, "tcgen05 kernel: two CTAs per SM");
 
-__device__ unsigned g_mrhs_tc_timeouts;  // rounds abandoned after a bounded mbarrier wait
+__device__ unsigned g_mrhs_tc_timeouts;  // launches that abandoned work after a bounded wait
 
-// launch controls of the tensor-core kernel: the bound of each wait for the
-// MMAs (mbarrier polls), a test hook that issues no MMA (so the waits run
-// out), and a host-mapped flag the kernel sets when a wait ran out
+// launch controls of the tensor-core kernel: the bound of each wait (mbarrier
+// polls), a test hook that issues no MMA (so the waits run out), and a
+// host-mapped flag the kernel sets when a wait ran out
 struct TcCtl {
   int polls;
   int skip_mma;
@@ -625,55 +659,74 @@ __device__ __forceinline__ uint32_t pack_h2(float a, float b)
   return *(const uint32_t *)&h;
 }
 
-// shared stores that the compiler may reorder against global loads (the
-// tensor cores read them after a fence and a barrier)
+// shared stores of the operands: volatile asm, so they stay in order with
+// the fences and barriers that hand the operands to the tensor cores, while
+// global loads may move across them
 __device__ __forceinline__ void sts128(uint32_t a, uint32_t x, uint32_t y, uint32_t z, uint32_t w)
 {
   asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(a), "r"(x), "r"(y), "r"(z), "r"(w));
 }
-__device__ __forceinline__ void sts64(uint32_t a, uint32_t x, uint32_t y)
+
+__device__ __forceinline__ void tc_named_bar(int id, int n)
 {
-  asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(a), "r"(x), "r"(y));
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
 
-// the 12 halves (6 words) v of K block h in the row at `row` (address of
-// the row inside its core-matrix group): block h starts at K = 12 h, i.e.
-// at a whole core matrix (h even) or half-way through one (h odd)
-__device__ __forceinline__ void tc_put12(uint32_t row, int h, const uint32_t v[6])
+__device__ __forceinline__ void mbar_init(uint32_t bar, unsigned count)
 {
-  const uint32_t c = (uint32_t)(12 * h) >> 3;  // first core matrix
-  if ((h & 1) == 0) {
-    sts128(row + c * 128, v[0], v[1], v[2], v[3]);
-    sts64(row + (c + 1) * 128, v[4], v[5]);
-  } else {
-    sts64(row + c * 128 + 8, v[0], v[1]);
-    sts128(row + (c + 1) * 128, v[2], v[3], v[4], v[5]);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}" ::"r"(bar) : "memory");
+}
+
+// wait for the phase of parity `parity` of the barrier to complete, at most
+// `polls` polls; false if the wait ran out
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int polls)
+{
+  uint32_t done = 0;
+  for (int it = 0; it < polls && !done; it++)
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+  return done != 0;
+}
+
+// a bounded wait of a pipeline role; after one wait ran out the thread stops
+// waiting (its work is void, the launch reports the failure)
+__device__ __forceinline__ void tc_wait(uint32_t bar, uint32_t parity, const TcCtl &ctl, bool &failed)
+{
+  if (failed) return;
+  if (!mbar_wait(bar, parity, ctl.polls)) {
+    failed = true;
+    *ctl.fail = 1u;
   }
 }
 
-// entry (c, source spin) of the matrix that rebuilds spin sp (0..3) from the
-// projected upper half of (1 + S g_mu) (the rules of accumulate<MU, S>)
-__device__ __forceinline__ void tc_rebuild(int mu, int S, int sp, int &src, float &cr, float &ci)
+// a row of H, K blocks of hop DD: the projected half spinor of the
+// neighbour's three 16-byte words w, scaled by sc2
+template <bool DAG, int DD>
+__device__ __forceinline__ void tc_h_block(const uint4 w[3], __half2 sc2, uint32_t row)
 {
-  const float s = (float)S;
-  cr = 0.f;
-  ci = 0.f;
-  if (sp < 2) {
-    src = sp;
-    cr = 1.f;
-  } else if (mu == 0) {
-    src = sp - 2;
-    cr = -s;
-  } else if (mu == 1) {
-    src = 3 - sp;
-    ci = s;
-  } else if (mu == 2) {
-    src = 3 - sp;
-    cr = sp == 2 ? s : -s;
-  } else {
-    src = sp - 2;
-    ci = sp == 2 ? s : -s;
+  constexpr int MU = DD >> 1, SF = DAG ? +1 : -1, S = (DD & 1) ? -SF : SF;
+  constexpr bool IM = MU & 1;
+  constexpr int B0 = (MU == 0 || MU == 3) ? 2 : 3, B1 = 5 - B0;
+  constexpr int SG0 = S > 0 ? -1 : 1, SG1 = MU < 2 ? SG0 : -SG0;
+  const __half2 *hv = reinterpret_cast<const __half2 *>(w);
+  uint32_t v0[3], v1[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const __half2 h0 = __hmul2(hcomb<IM>(hv[c], hv[3 * B0 + c], SG0), sc2);
+    const __half2 h1 = __hmul2(hcomb<IM>(hv[3 + c], hv[3 * B1 + c], SG1), sc2);
+    v0[c] = *(const uint32_t *)&h0;
+    v1[c] = *(const uint32_t *)&h1;
   }
+  sts128(row + (2 * DD) * 128, v0[0], v0[1], v0[2], 0u);
+  sts128(row + (2 * DD + 1) * 128, v1[0], v1[1], v1[2], 0u);
 }
 
 // neighbour of x in hop dd (2 mu + backward)
@@ -682,51 +735,62 @@ __device__ __forceinline__ int tc_nb(const Geom &g, int x, const int c[4], int d
   return (dd & 1) ? bwd(g, x, c, dd >> 1) : fwd(g, x, c, dd >> 1);
 }
 
-// slot r's row of H, K block DD: the projected half spinor at neighbour ys,
-// scaled by sc2
-template <bool DAG, int DD>
-__device__ __forceinline__ void tc_h_block(const MArgs &a, int ys, int r, __half2 sc2, uint32_t row)
+// source spin and coefficient (0: 1, 1: -1, 2: i, 3: -i) that rebuild spin sp
+// from the projected upper half of (1 + S g_mu)
+__device__ __forceinline__ void tc_rebuild(int mu, int S, int sp, int &src, int &kind)
 {
-  constexpr int MU = DD >> 1, SF = DAG ? +1 : -1, S = (DD & 1) ? -SF : SF;
-  constexpr bool IM = MU & 1;
-  constexpr int B0 = (MU == 0 || MU == 3) ? 2 : 3, B1 = 5 - B0;
-  constexpr int SG0 = S > 0 ? -1 : 1, SG1 = MU < 2 ? SG0 : -SG0;
-  const uint4 *p = (const uint4 *)a.in;
-  uint4 w[3];
-#pragma unroll
-  for (int j = 0; j < 3; j++) w[j] = p[((int64_t)j * a.V + ys) * a.N + r];
-  const __half2 *hv = reinterpret_cast<const __half2 *>(w);
-  uint32_t v[6];
-#pragma unroll
-  for (int c = 0; c < 3; c++) {
-    const __half2 h0 = __hmul2(hcomb<IM>(hv[c], hv[3 * B0 + c], SG0), sc2);
-    const __half2 h1 = __hmul2(hcomb<IM>(hv[3 + c], hv[3 * B1 + c], SG1), sc2);
-    v[c] = *(const uint32_t *)&h0;
-    v[3 + c] = *(const uint32_t *)&h1;
+  const int neg = S > 0 ? 0 : 1;  // c = S or i S: negative when S < 0
+  if (sp < 2) {
+    src = sp;
+    kind = 0;
+  } else if (mu == 0) {  // c = -S
+    src = sp - 2;
+    kind = 1 - neg;
+  } else if (mu == 1) {  // c = i S
+    src = 3 - sp;
+    kind = 2 + neg;
+  } else if (mu == 2) {  // c = S (spin 2), -S (spin 3)
+    src = 3 - sp;
+    kind = sp == 2 ? neg : 1 - neg;
+  } else {  // c = i S (spin 2), -i S (spin 3)
+    src = sp - 2;
+    kind = sp == 2 ? 2 + neg : 3 - neg;
   }
-  tc_put12(row, DD, v);
 }
 
 template <bool DAG, int MODE>
-__global__ void __launch_bounds__(kTcThreads, 3) k_wilson_mrhs_tc(const MArgs a, double *partials, const TcCtl ctl)
+__global__ void __launch_bounds__(kTcThreads, 2) k_wilson_mrhs_tc(const MArgs a, double *partials, const TcCtl ctl)
 {
-  extern __shared__ __align__(16) unsigned char tc_dyn[];
-  unsigned char *Ls = tc_dyn, *Hs = tc_dyn + kTcLBytes;
-  double *red = (double *)(tc_dyn + kTcLBytes + kTcHBytes);
-  float *X = (float *)Hs;  // accumulators [site][slot][24], over H once the MMAs are done
-  __shared__ __align__(8) uint64_t mbar;
+  extern __shared__ __align__(128) unsigned char tc_dyn[];
+  __shared__ __align__(8) uint64_t bars[8];  // full[2], done[2], tfree[2], sready[2]
   __shared__ uint32_t tbase;
   constexpr bool EO = MODE != 0;
   constexpr int SF = DAG ? +1 : -1;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int s = tid >> 4, rl = tid & 15;  // this thread's site in the tile and slot in the group
-  const uint32_t Lb = tc_smem(Ls), Hb = tc_smem(Hs);
+  const uint32_t Lb = tc_smem(tc_dyn), Hb = Lb + kTcOffH;
+  float *X = (float *)(tc_dyn + kTcOffX);
+  float *scl = (float *)(tc_dyn + kTcOffScl);
+  double *red = (double *)(tc_dyn + kTcOffRed);
+  int *nb = (int *)(tc_dyn + kTcOffNb);
+  const uint32_t bfull = tc_smem(&bars[0]), bdone = tc_smem(&bars[2]), btfree = tc_smem(&bars[4]);
+  const uint32_t bsready = tc_smem(&bars[6]);
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&mbar)));
+    mbar_init(bfull, kTcProd);
+    mbar_init(bfull + 8, kTcProd);
+    mbar_init(bdone, 1);
+    mbar_init(bdone + 8, 1);
+    mbar_init(btfree, 2);
+    mbar_init(btfree + 8, 2);
+    mbar_init(bsready, 1);
+    mbar_init(bsready + 8, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(tc_smem(&tbase)));
+  // zero both L buffers: the blocks of the other source spin and the pads
+  // are never written again
+  for (uint32_t i = tid; i < 2 * kTcLBuf / 16; i += kTcThreads) sts128(Lb + 16 * i, 0u, 0u, 0u, 0u);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  if (warp == kTcMmaWarp) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&tbase)), "n"(kTcCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -734,249 +798,325 @@ __global__ void __launch_bounds__(kTcThreads, 3) k_wilson_mrhs_tc(const MArgs a,
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tbase;
   const int G = a.N >> 4;
-  uint32_t phase = 0;
-  double run[4] = {0.0, 0.0, 0.0, 0.0};  // per-slot |out|^2 of the CTA (threads 0..15)
+  const int ntiles = (a.V + kTcSites - 1) / kTcSites;
+  const int my_tiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
   bool failed = false;
-  for (int tile = 0; tile < kTcTiles && !failed; tile++) {
-    const int base = (blockIdx.x * kTcTiles + tile) * kTcSites;
-    if (base >= a.V) break;
-    const int e = base + s;  // output index
-    const bool act = e < a.V;
-    int c[4], x = e;
-    if (act) {
-      if (EO) {
-        coords(a.geo, 2 * e, c);
-        const int b = (a.eo_par ^ c[1] ^ c[2] ^ c[3]) & 1;
-        x = 2 * e + b;
-        c[0] += b;
-      } else {
-        coords(a.geo, x, c);
+  int last_item = -1;  // MMA thread: the last item committed
+
+  if (warp < kTcEpiWarp0) {
+    // ------------------------------------------------------ producers
+    const int pt = tid;
+    int n = 0;
+    for (int lt = 0; lt < my_tiles; lt++) {
+      const int base = ((int)blockIdx.x + lt * (int)gridDim.x) * kTcSites;
+      tc_named_bar(2, kTcProd);  // the previous tile's neighbours are no longer read
+      if (pt < kTcSites) {
+        const int e = base + pt;
+        int x = -1;
+        if (e < a.V) {
+          int c[4];
+          x = e;
+          if (EO) {
+            coords(a.geo, 2 * e, c);
+            const int b = (a.eo_par ^ c[1] ^ c[2] ^ c[3]) & 1;
+            x = 2 * e + b;
+            c[0] += b;
+          } else {
+            coords(a.geo, x, c);
+          }
+#pragma unroll
+          for (int dd = 0; dd < 8; dd++) nb[pt * 9 + dd] = tc_nb(a.geo, x, c, dd);
+        }
+        nb[pt * 9 + 8] = x;
       }
-    }
-    // L: thread (site s, hop h, half) writes the rows of output spins 2 half, 2 half + 1
-    {
-      const int h = rl >> 1, half = rl & 1, mu = h >> 1;
-      const bool back = h & 1;
-      const int S = back ? -SF : SF;
-      C<float> M[9];
-      if (act) {
-        const int y = tc_nb(a.geo, x, c, h);
-        C<float> U[9];
-        Link<QCDGPU_F32, 18, float>::load(a.gauge, a.gstride, back ? y : x, mu, U);
-        const bool tw = (a.twist_mask >> mu) & 1;
-        const C<float> ph{tw ? a.phr[mu] : 1.f, tw ? (back ? -a.phi[mu] : a.phi[mu]) : 0.f};
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-#pragma unroll
-          for (int j = 0; j < 3; j++) M[3 * i + j] = ph * (back ? conj(U[3 * j + i]) : U[3 * i + j]);
-      } else {
-#pragma unroll
-        for (int k = 0; k < 9; k++) M[k] = C<float>{0.f, 0.f};
-      }
-#pragma unroll
-      for (int q = 0; q < 2; q++) {
-        const int sp = 2 * half + q;
-        int src;
-        float cr, ci;
-        tc_rebuild(mu, S, sp, src, cr, ci);
-#pragma unroll
-        for (int i = 0; i < 3; i++) {
-          uint32_t vre[6], vim[6];
+      tc_named_bar(2, kTcProd);
+      for (int g = 0; g < G; g++, n++) {
+        const int b = n & 1;
+        // every global load of the item first, so that their latency overlaps
+        // the wait for the buffers and one another
+        // L: thread (site, hop, colour row i) of the first 192 reads row i of its link
+        const bool lbuild = g == 0 && pt < kTcSites * 24;
+        const int ls = pt / 24, lh = (pt % 24) / 3, li = pt % 3;
+        const int lx = lbuild ? nb[ls * 9 + 8] : -1;
+        C<float> m[3];
+        if (lx >= 0) {
+          const int mu = lh >> 1;
+          const bool back = lh & 1;
+          const int y = nb[ls * 9 + lh];
+          const float2 *gp = a.gauge + (int64_t)mu * 9 * a.gstride + (back ? y : lx);
 #pragma unroll
           for (int j = 0; j < 3; j++) {
-            // z = c M_ij; row re: (Re z, -Im z), row im: (Im z, Re z), in the source spin's columns
-            const float zr = cr * M[3 * i + j].re - ci * M[3 * i + j].im;
-            const float zi = cr * M[3 * i + j].im + ci * M[3 * i + j].re;
-            const uint32_t pre = pack_h2(zr, -zi), pim = pack_h2(zi, zr);
-            vre[j] = src == 0 ? pre : 0u;
-            vre[3 + j] = src == 1 ? pre : 0u;
-            vim[j] = src == 0 ? pim : 0u;
-            vim[3 + j] = src == 1 ? pim : 0u;
+            const float2 v = __ldg(gp + (int64_t)(back ? 3 * j + li : 3 * li + j) * a.gstride);
+            m[j] = C<float>{v.x, back ? -v.y : v.y};
           }
-          const int o = 6 * sp + 2 * i;  // rows o (re) and o + 1 (im)
-          const uint32_t site = Lb + (uint32_t)s * 3 * kTcSbo;
-          tc_put12(site + (uint32_t)(o >> 3) * kTcSbo + (uint32_t)(o & 7) * 16, h, vre);
-          tc_put12(site + (uint32_t)((o + 1) >> 3) * kTcSbo + (uint32_t)((o + 1) & 7) * 16, h, vim);
         }
-      }
-    }
-    // neighbours are the same for every slot group
-    int ys[8];
-#pragma unroll
-    for (int dd = 0; dd < 8; dd++) {
-      const int y = act ? tc_nb(a.geo, x, c, dd) : 0;
-      ys[dd] = EO ? (y >> 1) : y;
-    }
-    for (int grp = 0; grp < G && !failed; grp++) {
-      const int r = grp * 16 + rl;
-      // H row rl of site s
-      const uint32_t hrow = Hb + (uint32_t)s * 2 * kTcSbo + (uint32_t)(rl >> 3) * kTcSbo + (uint32_t)(rl & 7) * 16;
-      float sc = 0.f;  // the slot's rescale: its largest neighbour norm
-      if (act) {
+        // H: thread (site, slot) of the first half of the producers takes hops 0..3, of the second hops 4..7
+        const int pair = pt % kTcPairs, hh = pt / kTcPairs;
+        const int hs = pair >> 4, rl = pair & 15, r = g * 16 + rl;
+        const int hx = nb[hs * 9 + 8];
         float nr[8];
+        uint4 w[4][3];
+        if (hx >= 0) {
 #pragma unroll
-        for (int dd = 0; dd < 8; dd++) {
-          nr[dd] = a.in_norm[(int64_t)ys[dd] * a.N + r];
-          sc = fmaxf(sc, nr[dd]);
+          for (int dd = 0; dd < 8; dd++) {
+            const int y = nb[hs * 9 + dd];
+            nr[dd] = a.in_norm[(int64_t)(EO ? (y >> 1) : y) * a.N + r];
+          }
+          const uint4 *p = (const uint4 *)a.in;
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            const int y = nb[hs * 9 + 4 * hh + q];
+            const int64_t ys = EO ? (y >> 1) : y;
+#pragma unroll
+            for (int j = 0; j < 3; j++) w[q][j] = p[((int64_t)j * a.V + ys) * a.N + r];
+          }
         }
-        const float inv = sc > 0.f ? 1.0f / sc : 0.f;
-        tc_h_block<DAG, 0>(a, ys[0], r, __float2half2_rn(nr[0] * inv), hrow);
-        tc_h_block<DAG, 1>(a, ys[1], r, __float2half2_rn(nr[1] * inv), hrow);
-        tc_h_block<DAG, 2>(a, ys[2], r, __float2half2_rn(nr[2] * inv), hrow);
-        tc_h_block<DAG, 3>(a, ys[3], r, __float2half2_rn(nr[3] * inv), hrow);
-        tc_h_block<DAG, 4>(a, ys[4], r, __float2half2_rn(nr[4] * inv), hrow);
-        tc_h_block<DAG, 5>(a, ys[5], r, __float2half2_rn(nr[5] * inv), hrow);
-        tc_h_block<DAG, 6>(a, ys[6], r, __float2half2_rn(nr[6] * inv), hrow);
-        tc_h_block<DAG, 7>(a, ys[7], r, __float2half2_rn(nr[7] * inv), hrow);
-      } else {
-        const uint32_t z[6] = {0u, 0u, 0u, 0u, 0u, 0u};
+        if (n >= 2) tc_wait(bdone + 8 * b, ((n >> 1) & 1) ^ 1, ctl, failed);  // the MMAs of item n - 2
+        if (lx >= 0) {
+          const int mu = lh >> 1;
+          const bool back = lh & 1;
+          if ((a.twist_mask >> mu) & 1) {
+            const C<float> ph{a.phr[mu], back ? -a.phi[mu] : a.phi[mu]};
 #pragma unroll
-        for (int dd = 0; dd < 8; dd++) tc_put12(hrow, dd, z);
+            for (int j = 0; j < 3; j++) m[j] = ph * m[j];
+          }
+          uint32_t p1[3], p2[3];  // (Re, -Im) and (Im, Re) of M_ij
+#pragma unroll
+          for (int j = 0; j < 3; j++) {
+            p1[j] = pack_h2(m[j].re, -m[j].im);
+            p2[j] = pack_h2(m[j].im, m[j].re);
+          }
+          const int S = back ? -SF : SF;
+          const uint32_t Ls = Lb + (uint32_t)(lt & 1) * kTcLBuf + (uint32_t)ls * kTcLSite;
+#pragma unroll
+          for (int sp = 0; sp < 4; sp++) {
+            int src, kind;
+            tc_rebuild(mu, S, sp, src, kind);
+            // c M in the two rows: 1: (P1, P2); -1: (-P1, -P2); i: (-P2, P1); -i: (P2, -P1)
+            const bool swap = kind >= 2;
+            const uint32_t nre = (kind == 1 || kind == 2) ? 0x80008000u : 0u;
+            const uint32_t nim = (kind == 1 || kind == 3) ? 0x80008000u : 0u;
+            uint32_t wr[3], wi[3];
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+              wr[j] = (swap ? p2[j] : p1[j]) ^ nre;
+              wi[j] = (swap ? p1[j] : p2[j]) ^ nim;
+            }
+            const int o = 6 * sp + 2 * li;  // rows o (re) and o + 1 (im)
+            const uint32_t core = (uint32_t)(2 * lh + src) * 128;
+            sts128(Ls + (uint32_t)(o >> 3) * kTcSbo + (uint32_t)(o & 7) * 16 + core, wr[0], wr[1], wr[2], 0u);
+            sts128(Ls + (uint32_t)((o + 1) >> 3) * kTcSbo + (uint32_t)((o + 1) & 7) * 16 + core, wi[0], wi[1], wi[2],
+                   0u);
+          }
+        }
+        if (hx >= 0) {
+          float mx = 0.f;
+#pragma unroll
+          for (int dd = 0; dd < 8; dd++) mx = fmaxf(mx, nr[dd]);
+          const float inv = mx > 0.f ? 1.0f / mx : 0.f;
+          const uint32_t hrow = Hb + (uint32_t)b * kTcHBuf + (uint32_t)hs * kTcHSite + (uint32_t)(rl >> 3) * kTcSbo +
+                                (uint32_t)(rl & 7) * 16;
+          if (hh == 0) {
+            scl[(n & 3) * kTcPairs + pair] = mx;
+            tc_h_block<DAG, 0>(w[0], __float2half2_rn(nr[0] * inv), hrow);
+            tc_h_block<DAG, 1>(w[1], __float2half2_rn(nr[1] * inv), hrow);
+            tc_h_block<DAG, 2>(w[2], __float2half2_rn(nr[2] * inv), hrow);
+            tc_h_block<DAG, 3>(w[3], __float2half2_rn(nr[3] * inv), hrow);
+          } else {
+            tc_h_block<DAG, 4>(w[0], __float2half2_rn(nr[4] * inv), hrow);
+            tc_h_block<DAG, 5>(w[1], __float2half2_rn(nr[5] * inv), hrow);
+            tc_h_block<DAG, 6>(w[2], __float2half2_rn(nr[6] * inv), hrow);
+            tc_h_block<DAG, 7>(w[3], __float2half2_rn(nr[7] * inv), hrow);
+          }
+        }
+        // the tensor cores read what this thread wrote
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arrive(bfull + 8 * b);
       }
-      // the tensor cores read what the threads wrote
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncthreads();
-      if (tid == 0 && !ctl.skip_mma) {
+    }
+  } else if (warp == kTcMmaWarp) {
+    // ------------------------------------------------------ MMA issue
+    if (lane == 0) {
+      constexpr uint32_t idesc = tc_idesc(64, 16);
+      int n = 0;
+      for (int lt = 0; lt < my_tiles; lt++) {
+        for (int g = 0; g < G; g++, n++) {
+          const int b = n & 1;
+          tc_wait(bfull + 8 * b, (n >> 1) & 1, ctl, failed);
+          if (n >= 2) tc_wait(btfree + 8 * b, ((n >> 1) & 1) ^ 1, ctl, failed);  // epilogue of item n - 2
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          // the producers' rescale factors of item n, released to the epilogue
+          mbar_arrive(bsready + 8 * b);
+          if (ctl.skip_mma) continue;
+          // descriptors of the item's first operands; later sites and K steps
+          // add their byte offsets / 16 to the 14-bit address field
+          const uint64_t ad0 = tc_sdesc(Lb + (uint32_t)(lt & 1) * kTcLBuf, 128, kTcSbo);
+          const uint64_t bd0 = tc_sdesc(Hb + (uint32_t)b * kTcHBuf, 128, kTcSbo);
+#pragma unroll
+          for (int t = 0; t < kTcSites; t++) {
+#pragma unroll
+            for (int kk = 0; kk < kTcK / 16; kk++) {
+              const uint64_t ad = ad0 + (uint64_t)((t * kTcLSite + kk * 256) >> 4);
+              const uint64_t bd = bd0 + (uint64_t)((t * kTcHSite + kk * 256) >> 4);
+              const uint32_t dt = tmem + (uint32_t)(b * kTcSites * 16 + t * 16);
+              if (kk == 0)
+                asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, 0;" ::"r"(dt), "l"(ad), "l"(bd),
+                             "r"(idesc));
+              else
+                asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, 1;" ::"r"(dt), "l"(ad), "l"(bd),
+                             "r"(idesc));
+            }
+          }
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bdone + 8 * b)
+                       : "memory");
+          last_item = n;
+        }
+      }
+    }
+    __syncwarp();
+  } else {
+    // ------------------------------------------------------ epilogue
+    const int et = tid - kTcEpiWarp0 * 32;  // (site, slot) pair
+    const int s = et >> 4, rl = et & 15;
+    // warp sub = 0 reads accumulator rows 0..15 (lanes 0..15), sub = 1 rows
+    // 16..23 (lanes 32..39) of the M = 64 layout (row i in lane 32 (i / 16) + i % 16)
+    const int sub = warp & 3;
+    const bool reader = true;
+    constexpr int zmode = MODE == 1 ? 0 : 2;
+    constexpr bool ainv = MODE == 1;
+    constexpr float ch = MODE == 0 ? -0.5f : MODE == 1 ? 1.0f : -0.25f;
+    double run[4] = {0.0, 0.0, 0.0, 0.0};  // per-slot |out|^2 of the CTA (threads 0..15)
+    int n = 0;
+    for (int lt = 0; lt < my_tiles; lt++) {
+      const int base = ((int)blockIdx.x + lt * (int)gridDim.x) * kTcSites;
+      const int e = base + s;
+      const bool act = e < a.V;
+      for (int g = 0; g < G; g++, n++) {
+        const int b = n & 1, r = g * 16 + rl;
+        // the diagonal term does not wait for the tensor cores
+        C<float> zs[1][12];
+        float znrm[1] = {0.f};
+        if (zmode && act) mload_rp<1>(a, EO ? a.z : a.in, EO ? a.z_norm : a.in_norm, e, r, zs, znrm);
+        tc_wait(bdone + 8 * b, (n >> 1) & 1, ctl, failed);
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        constexpr uint32_t idesc = tc_idesc(64, 16);
-#pragma unroll 1
-        for (int t = 0; t < kTcSites; t++) {
+        tc_wait(bsready + 8 * b, (n >> 1) & 1, ctl, failed);
+        const float sc = scl[(n & 3) * kTcPairs + et];
+        if (reader) {
 #pragma unroll
-          for (int kk = 0; kk < kTcK / 16; kk++) {
-            const uint64_t ad = tc_sdesc(Lb + (uint32_t)t * 3 * kTcSbo + kk * 256, 128, kTcSbo);
-            const uint64_t bd = tc_sdesc(Hb + (uint32_t)t * 2 * kTcSbo + kk * 256, 128, kTcSbo);
-            const uint32_t dt = tmem + (uint32_t)(t * 16), acc = kk > 0;
-            asm volatile(
-                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(dt),
-                "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+          for (int t0 = 0; t0 < kTcSites; t0 += 4) {  // four sites per batch of loads
+            uint32_t v[4][16];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+              const uint32_t ta = tmem + ((uint32_t)(sub * 32) << 16) + (uint32_t)(b * kTcSites * 16 + (t0 + q) * 16);
+              asm volatile(
+                  "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                  "[%16];"
+                  : "=r"(v[q][0]), "=r"(v[q][1]), "=r"(v[q][2]), "=r"(v[q][3]), "=r"(v[q][4]), "=r"(v[q][5]),
+                    "=r"(v[q][6]), "=r"(v[q][7]), "=r"(v[q][8]), "=r"(v[q][9]), "=r"(v[q][10]), "=r"(v[q][11]),
+                    "=r"(v[q][12]), "=r"(v[q][13]), "=r"(v[q][14]), "=r"(v[q][15])
+                  : "r"(ta));
+            }
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            const int o = sub * 16 + lane;  // accumulator row
+            if (lane < 16 && o < 24) {
+#pragma unroll
+              for (int q = 0; q < 4; q++)
+#pragma unroll
+                for (int c = 0; c < 16; c++) X[((t0 + q) * 16 + c) * 24 + o] = __uint_as_float(v[q][c]);
+            }
           }
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                         tc_smem(&mbar))
-                     : "memory");
-      }
-      // the z term of the epilogue does not wait for the tensor cores
-      constexpr int zmode = MODE == 1 ? 0 : 2;
-      C<float> zs[1][12];
-      float znrm[1] = {0.f};
-      if (zmode && act) mload_rp<1>(a, EO ? a.z : a.in, EO ? a.z_norm : a.in_norm, e, r, zs, znrm);
-      // bounded wait for the commit; a timeout abandons the kernel's work
-      uint32_t done = 0;
-      for (int it = 0; it < ctl.polls && !done; it++)
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-            : "=r"(done)
-            : "r"(tc_smem(&mbar)), "r"(phase)
-            : "memory");
-      if (__syncthreads_or(!done)) {
-        // the MMAs may still be in flight: wait once more, bounded, before
-        // the tensor memory is released
-        for (int it = 0; it < ctl.polls && !done; it++)
-          asm volatile(
-              "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-              : "=r"(done)
-              : "r"(tc_smem(&mbar)), "r"(phase)
-              : "memory");
-        if (tid == 0) {
-          atomicAdd(&g_mrhs_tc_timeouts, 1u);
-          *ctl.fail = 1u;
-        }
-        failed = true;
-        break;
-      }
-      phase ^= 1u;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      // accumulator rows 0..23 (warp 0 lanes 0..15, warp 1 lanes 0..7) -> X[site][slot][row]
-      if (warp < 2) {
+        tc_named_bar(1, kTcEpi);  // X complete, every thread has read its rescale
+        if (reader && lane == 0) mbar_arrive(btfree + 8 * b);
+        double n2 = 0.0;
+        if (act) {
+          C<float> acc[12];
+          const float *xi = X + et * 24;
 #pragma unroll
-        for (int t = 0; t < kTcSites; t++) {
-          uint32_t v[16];
-          const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(t * 16);
-          asm volatile(
-              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-              : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-              : "r"(ta));
-          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-          const int o = warp * 16 + lane;  // accumulator row
-          if (lane < 16 && o < 24) {
-#pragma unroll
-            for (int n = 0; n < 16; n++) X[(t * 16 + n) * 24 + o] = __uint_as_float(v[n]);
-          }
-        }
-      }
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncthreads();
-      // epilogue: one thread per (site, slot)
-      double n2 = 0.0;
-      if (act) {
-        C<float> acc[12];
-        const float *xi = X + (s * 16 + rl) * 24;
-#pragma unroll
-        for (int k = 0; k < 12; k++) acc[k] = C<float>{sc * xi[2 * k], sc * xi[2 * k + 1]};
-        constexpr bool ainv = MODE == 1;
-        constexpr float ch = MODE == 0 ? -0.5f : MODE == 1 ? 1.0f : -0.25f;
-        const float mp4r = a.mp4s ? a.mp4s[r] : a.mp4;
-        const float tmr = a.tms ? (DAG ? -a.tms[r] : a.tms[r]) : a.tm;
-        if (ainv) {  // A^{-1} = (mp4 - i tm g5) / (mp4^2 + tm^2)
-          const float den = 1.0f / (mp4r * mp4r + tmr * tmr), ar = mp4r * den, ai = -tmr * den;
-#pragma unroll
-          for (int k = 0; k < 12; k++) {
-            const float g5ai = k < 6 ? ai : -ai;
-            acc[k] = C<float>{ar * acc[k].re - g5ai * acc[k].im, ar * acc[k].im + g5ai * acc[k].re};
-          }
-        }
-        const float zsc = zmode ? znrm[0] : 0.f;
-        const float zm = zmode == 2 ? mp4r * zsc : zsc, zt = zmode == 2 ? tmr * zsc : 0.f;
-        float mx = 0.f;
-#pragma unroll
-        for (int k = 0; k < 12; k++) {
-          const float g5tm = k < 6 ? zt : -zt;
-          const C<float> zk = zmode ? zs[0][k] : C<float>{0.f, 0.f};
-          acc[k] = C<float>{zm * zk.re - g5tm * zk.im + ch * acc[k].re, zm * zk.im + g5tm * zk.re + ch * acc[k].im};
-          mx = fmaxf(mx, fmaxf(fabsf(acc[k].re), fabsf(acc[k].im)));
-        }
-        if (!(mx >= 1.17549435e-38f)) mx = 0.f;
-        const float inv = mx > 0.f ? 1.0f / mx : 0.f;
-        if (r < a.nact) {
-          float2 o[12];
-#pragma unroll
-          for (int k = 0; k < 12; k++) o[k] = make_float2(acc[k].re, acc[k].im);
-          mstore_raw(a.out, a.V, a.N, e, r, o, inv);
-          a.out_norm[(int64_t)e * a.N + r] = mx;
-          if (partials) {  // |out|^2 of the stored (rounded) values
-            float s2 = 0.f;
+          for (int k = 0; k < 12; k++) acc[k] = C<float>{sc * xi[2 * k], sc * xi[2 * k + 1]};
+          const float mp4r = a.mp4s ? a.mp4s[r] : a.mp4;
+          const float tmr = a.tms ? (DAG ? -a.tms[r] : a.tms[r]) : a.tm;
+          if (ainv) {  // A^{-1} = (mp4 - i tm g5) / (mp4^2 + tm^2)
+            const float den = 1.0f / (mp4r * mp4r + tmr * tmr), ar = mp4r * den, ai = -tmr * den;
 #pragma unroll
             for (int k = 0; k < 12; k++) {
-              const float2 f = __half22float2(__floats2half2_rn(o[k].x * inv, o[k].y * inv));
-              s2 += f.x * f.x + f.y * f.y;
+              const float g5ai = k < 6 ? ai : -ai;
+              acc[k] = C<float>{ar * acc[k].re - g5ai * acc[k].im, ar * acc[k].im + g5ai * acc[k].re};
             }
-            n2 = (double)(s2 * mx * mx);
+          }
+          const float zsc = zmode ? znrm[0] : 0.f;
+          const float zm = zmode == 2 ? mp4r * zsc : zsc, zt = zmode == 2 ? tmr * zsc : 0.f;
+          float mx = 0.f;
+#pragma unroll
+          for (int k = 0; k < 12; k++) {
+            const float g5tm = k < 6 ? zt : -zt;
+            const C<float> zk = zmode ? zs[0][k] : C<float>{0.f, 0.f};
+            acc[k] = C<float>{zm * zk.re - g5tm * zk.im + ch * acc[k].re, zm * zk.im + g5tm * zk.re + ch * acc[k].im};
+            mx = fmaxf(mx, fmaxf(fabsf(acc[k].re), fabsf(acc[k].im)));
+          }
+          if (!(mx >= 1.17549435e-38f)) mx = 0.f;
+          const float inv = mx > 0.f ? 1.0f / mx : 0.f;
+          if (r < a.nact) {
+            float2 o[12];
+#pragma unroll
+            for (int k = 0; k < 12; k++) o[k] = make_float2(acc[k].re, acc[k].im);
+            mstore_raw(a.out, a.V, a.N, e, r, o, inv);
+            a.out_norm[(int64_t)e * a.N + r] = mx;
+            if (partials) {  // |out|^2 of the stored (rounded) values
+              float s2 = 0.f;
+#pragma unroll
+              for (int k = 0; k < 12; k++) {
+                const float2 f = __half22float2(__floats2half2_rn(o[k].x * inv, o[k].y * inv));
+                s2 += f.x * f.x + f.y * f.y;
+              }
+              n2 = (double)(s2 * mx * mx);
+            }
           }
         }
-      }
-      if (partials) {  // the CTA's per-slot sums, in a fixed order
-        red[s * 16 + rl] = n2;
-        __syncthreads();
-        if (tid < 16) {
-          double t = 0.0;
-          for (int i = 0; i < kTcSites; i++) t += red[i * 16 + tid];
-          run[grp] += t;
+        if (partials) {  // the CTA's per-slot sums, in a fixed order
+          red[et] = n2;
+          tc_named_bar(1, kTcEpi);
+          if (et < 16) {
+            double t = 0.0;
+            for (int i = 0; i < kTcSites; i++) t += red[i * 16 + et];
+            run[g] += t;
+          }
         }
+        tc_named_bar(1, kTcEpi);  // X and red are rewritten by the next item
       }
-      __syncthreads();  // X (over H) and red are rewritten by the next group
     }
+    if (partials && et < 16)
+      for (int g = 0; g < G; g++) partials[(int64_t)blockIdx.x * a.N + g * 16 + et] = run[g];
   }
-  if (partials && tid < 16)
-    for (int grp = 0; grp < G; grp++) partials[(int64_t)blockIdx.x * a.N + grp * 16 + tid] = run[grp];
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
+  if (warp == kTcMmaWarp) {
+    // a role that stopped waiting may have left MMAs in flight: wait for the
+    // last commit (bounded) before the tensor memory is released
+    if (lane == 0 && last_item >= 0) {
+      const int b = last_item & 1;
+      tc_wait(bdone + 8 * b, (last_item >> 1) & 1, ctl, failed);
+    }
+    __syncwarp();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(kTcCols));
+  }
+  if (failed) atomicAdd(&g_mrhs_tc_timeouts, 1u);
 }
 
-unsigned mrhs_tc_grid(int64_t V) { return (unsigned)((V + kTcSites * kTcTiles - 1) / (kTcSites * kTcTiles)); }
+// two CTAs per SM (the kernel's shared memory allows no third), at most one per tile
+unsigned mrhs_tc_grid(int64_t V)
+{
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+      sms = 1;
+  }
+  const int64_t tiles = (V + kTcSites - 1) / kTcSites;
+  return (unsigned)(tiles < 2 * sms ? tiles : 2 * sms);
+}
 
 template <bool D, int M>
 static void launch_tc(const MArgs &a, double *partials, unsigned grid, cudaStream_t s, const TcCtl &ctl)
@@ -990,7 +1130,7 @@ static void launch_tc(const MArgs &a, double *partials, unsigned grid, cudaStrea
 }
 
 // host side of the tensor-core kernel's failure reporting
-static int g_tc_polls = 1 << 24;
+static int g_tc_polls = 1 << 20;
 static int g_tc_skip_mma = 0;
 static volatile unsigned *g_tc_fail_host = nullptr;  // page-locked, mapped
 static unsigned *g_tc_fail_dev = nullptr;
@@ -1376,7 +1516,7 @@ int qcdgpu_mrhs_tc_reset(void)
 int qcdgpu_mrhs_tc_test_hook(int skip_mma, int polls)
 {
   qg::g_tc_skip_mma = skip_mma ? 1 : 0;
-  qg::g_tc_polls = polls > 0 ? polls : 1 << 24;
+  qg::g_tc_polls = polls > 0 ? polls : 1 << 20;
   return 0;
 }
 
