@@ -257,11 +257,11 @@ __device__ __forceinline__ void mload_rp(const MArgs &a, const __half2 *d, const
   }
 }
 
-// h = nrm * upper half of (1 + S g_mu) s for the spinor s held as its three
-// 16-byte words, projected on packed half pairs (as the single-RHS FP16
-// kernel does)
+// h = upper half of (1 + S g_mu) s for the spinor s held as its three
+// 16-byte words (without its norm, which the accumulation applies),
+// projected on packed half pairs (as the single-RHS FP16 kernel does)
 template <int MU, int S>
-__device__ __forceinline__ void project_words(const uint4 w[3], float nrm, C<float> h[6])
+__device__ __forceinline__ void project_words(const uint4 w[3], C<float> h[6])
 {
   const __half2 *hv = reinterpret_cast<const __half2 *>(w);
   constexpr bool IM = MU & 1;
@@ -271,21 +271,20 @@ __device__ __forceinline__ void project_words(const uint4 w[3], float nrm, C<flo
   for (int c = 0; c < 3; c++) {
     const float2 f0 = __half22float2(hcomb<IM>(hv[c], hv[3 * B0 + c], SG0));
     const float2 f1 = __half22float2(hcomb<IM>(hv[3 + c], hv[3 * B1 + c], SG1));
-    h[c] = C<float>{nrm * f0.x, nrm * f0.y};
-    h[3 + c] = C<float>{nrm * f1.x, nrm * f1.y};
+    h[c] = C<float>{f0.x, f0.y};
+    h[3 + c] = C<float>{f1.x, f1.y};
   }
 }
 
 // the same for slot r of the multi-RHS spinor at y
 template <int MU, int S>
-__device__ __forceinline__ void mload_project(const __half2 *d, int64_t V, int N, int y, int r, float nrm,
-                                              C<float> h[6])
+__device__ __forceinline__ void mload_project(const __half2 *d, int64_t V, int N, int y, int r, C<float> h[6])
 {
   const uint4 *p = (const uint4 *)d;
   uint4 w[3];
 #pragma unroll
   for (int j = 0; j < 3; j++) w[j] = p[((int64_t)j * V + y) * N + r];
-  project_words<MU, S>(w, nrm, h);
+  project_words<MU, S>(w, h);
 }
 
 template <int MU, bool DAG, int RP, bool EO>
@@ -312,9 +311,9 @@ __device__ __forceinline__ void mhop_pair(const MArgs &a, int x, const int c[4],
     for (int q = 0; q < RP; q++) {
       C<float> h[6], uh[6];
       // the projection adds the stored half pairs, then the six projected
-      // components are converted and scaled by the slot's site norm
-      if (back) mload_project<MU, -SF>(a.in, a.V, a.N, ys, r0 + q, nrm[q], h);
-      else mload_project<MU, SF>(a.in, a.V, a.N, ys, r0 + q, nrm[q], h);
+      // components are converted; the slot's site norm scales the accumulation
+      if (back) mload_project<MU, -SF>(a.in, a.V, a.N, ys, r0 + q, h);
+      else mload_project<MU, SF>(a.in, a.V, a.N, ys, r0 + q, h);
 #pragma unroll
       for (int j = 0; j < 2; j++)
 #pragma unroll
@@ -326,8 +325,8 @@ __device__ __forceinline__ void mhop_pair(const MArgs &a, int x, const int c[4],
 #pragma unroll
         for (int k = 0; k < 6; k++) uh[k] = uh[k] * ph;
       }
-      if (back) accumulate<MU, -SF>(acc[q], uh);
-      else accumulate<MU, SF>(acc[q], uh);
+      if (back) accumulate_scaled<MU, -SF>(acc[q], uh, nrm[q]);
+      else accumulate_scaled<MU, SF>(acc[q], uh, nrm[q]);
     }
   }
 }

@@ -63,16 +63,47 @@ __device__ __forceinline__ void accumulate(C<R> acc[12], const C<R> h[6])
   }
 }
 
+// acc += sc (1 + S g_mu) spinor rebuilt from its upper half h: the same as
+// accumulate<MU, S> applied to sc h, with the scale folded into the
+// multiply-adds
+template <int MU, int S>
+__device__ __forceinline__ void accumulate_scaled(C<float> acc[12], const C<float> h[6], float sc)
+{
+  const float p = S > 0 ? sc : -sc;  // sign of the rebuilt lower spins' terms
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const C<float> h0 = h[c], h1 = h[3 + c];
+    acc[c] = C<float>{qfma(sc, h0.re, acc[c].re), qfma(sc, h0.im, acc[c].im)};
+    acc[3 + c] = C<float>{qfma(sc, h1.re, acc[3 + c].re), qfma(sc, h1.im, acc[3 + c].im)};
+    if (MU == 0) {  // -S h0, -S h1
+      acc[6 + c] = C<float>{qfma(-p, h0.re, acc[6 + c].re), qfma(-p, h0.im, acc[6 + c].im)};
+      acc[9 + c] = C<float>{qfma(-p, h1.re, acc[9 + c].re), qfma(-p, h1.im, acc[9 + c].im)};
+    } else if (MU == 1) {  // S i h1, S i h0
+      acc[6 + c] = C<float>{qfma(-p, h1.im, acc[6 + c].re), qfma(p, h1.re, acc[6 + c].im)};
+      acc[9 + c] = C<float>{qfma(-p, h0.im, acc[9 + c].re), qfma(p, h0.re, acc[9 + c].im)};
+    } else if (MU == 2) {  // S h1, -S h0
+      acc[6 + c] = C<float>{qfma(p, h1.re, acc[6 + c].re), qfma(p, h1.im, acc[6 + c].im)};
+      acc[9 + c] = C<float>{qfma(-p, h0.re, acc[9 + c].re), qfma(-p, h0.im, acc[9 + c].im)};
+    } else {  // S i h0, -S i h1
+      acc[6 + c] = C<float>{qfma(-p, h0.im, acc[6 + c].re), qfma(p, h0.re, acc[6 + c].im)};
+      acc[9 + c] = C<float>{qfma(p, h1.im, acc[9 + c].re), qfma(-p, h1.re, acc[9 + c].im)};
+    }
+  }
+}
+
 // h = upper half of (1 + S g_mu) s for the spinor s at index y: any storage
-// loads the twelve components, then projects
+// loads the twelve components, then projects. kScaled: h is returned
+// without the site's norm, which comes back in sc for the accumulation.
 template <int MU, int S, int SP, typename R>
 struct LoadProject {
+  static constexpr bool kScaled = false;
   __device__ __forceinline__ static void run(const void *base, const float *norm, int64_t stride, int64_t y,
-                                             C<R> h[6])
+                                             C<R> h[6], float &sc)
   {
     C<R> s[12];
     Spinor<SP, R>::load(base, norm, stride, y, s);
     project<MU, S>(s, h);
+    sc = 1.0f;
   }
 };
 
@@ -88,15 +119,17 @@ __device__ __forceinline__ __half2 hcomb(__half2 a, __half2 b, int sg)
 // of the site's three 16-byte words): the projection adds the stored half
 // pairs directly (one FP16 rounding per projected component, below the
 // storage's own 2^-11), and only the six projected components are converted
-// and scaled by the site norm -- half the conversions and multiplies of
-// decoding all twelve (measured: 57.4 -> 54.0 us per 24^3x48 apply)
+// -- half the conversions of decoding all twelve (measured: 57.4 -> 54.0 us
+// per 24^3x48 apply). The site norm is applied in the accumulation
+// (accumulate_scaled), not to the six components.
 template <int MU, int S>
 struct LoadProject<MU, S, QCDGPU_F16, float> {
+  static constexpr bool kScaled = true;
   __device__ __forceinline__ static void run(const void *base, const float *norm, int64_t stride, int64_t y,
-                                             C<float> h[6])
+                                             C<float> h[6], float &sc)
   {
     const uint4 *p = (const uint4 *)base + y;
-    const float nrm = __ldg(norm + y);
+    sc = __ldg(norm + y);
     uint4 w[3];
 #pragma unroll
     for (int j = 0; j < 3; j++) w[j] = __ldg(p + j * stride);
@@ -109,8 +142,8 @@ struct LoadProject<MU, S, QCDGPU_F16, float> {
     for (int c = 0; c < 3; c++) {
       const float2 f0 = __half22float2(hcomb<IM>(hv[c], hv[3 * B0 + c], SG0));
       const float2 f1 = __half22float2(hcomb<IM>(hv[3 + c], hv[3 * B1 + c], SG1));
-      h[c] = C<float>{nrm * f0.x, nrm * f0.y};
-      h[3 + c] = C<float>{nrm * f1.x, nrm * f1.y};
+      h[c] = C<float>{f0.x, f0.y};
+      h[3 + c] = C<float>{f1.x, f1.y};
     }
   }
 };
@@ -123,7 +156,8 @@ __device__ __forceinline__ void hop_pair(const DArgs &a, int x, const int c[4], 
   {
     int y = fwd(a.geo, x, c, MU);
     C<R> h[6], uh[6], U[9];
-    LoadProject<MU, SF, SP, R>::run(a.in, a.in_norm, a.stride, EO ? (y >> 1) : y, h);
+    float sc;
+    LoadProject<MU, SF, SP, R>::run(a.in, a.in_norm, a.stride, EO ? (y >> 1) : y, h, sc);
     Link<GP, RECON, R>::load(a.gauge, a.gstride, x, MU, U);
 #pragma unroll
     for (int j = 0; j < 2; j++)
@@ -135,12 +169,14 @@ __device__ __forceinline__ void hop_pair(const DArgs &a, int x, const int c[4], 
 #pragma unroll
       for (int k = 0; k < 6; k++) uh[k] = uh[k] * ph;
     }
-    accumulate<MU, SF>(acc, uh);
+    if constexpr (LoadProject<MU, SF, SP, R>::kScaled) accumulate_scaled<MU, SF>(acc, uh, sc);
+    else accumulate<MU, SF>(acc, uh);
   }
   {
     int y = bwd(a.geo, x, c, MU);
     C<R> h[6], uh[6], U[9];
-    LoadProject<MU, -SF, SP, R>::run(a.in, a.in_norm, a.stride, EO ? (y >> 1) : y, h);
+    float sc;
+    LoadProject<MU, -SF, SP, R>::run(a.in, a.in_norm, a.stride, EO ? (y >> 1) : y, h, sc);
     Link<GP, RECON, R>::load(a.gauge, a.gstride, y, MU, U);
 #pragma unroll
     for (int j = 0; j < 2; j++)
@@ -152,7 +188,8 @@ __device__ __forceinline__ void hop_pair(const DArgs &a, int x, const int c[4], 
 #pragma unroll
       for (int k = 0; k < 6; k++) uh[k] = uh[k] * ph;
     }
-    accumulate<MU, -SF>(acc, uh);
+    if constexpr (LoadProject<MU, -SF, SP, R>::kScaled) accumulate_scaled<MU, -SF>(acc, uh, sc);
+    else accumulate<MU, -SF>(acc, uh);
   }
 }
 
