@@ -65,8 +65,10 @@ inline int64_t pad_stride(int64_t V) { return (V + 127) / 128 * 128; }
 // links of every direction whose theta is non-zero.
 constexpr int kGaugeFF = 3;
 // Internal key of the FP32 copy with all 18 reals per link (4 mu x 9 float2),
-// read by the tensor-core multi-RHS operator (it needs every entry).
+// read by the multi-RHS operator kernels, with the boundary phase
+// e^{i theta_mu / L_mu} multiplied into the links (gauge_fold_phases).
 constexpr int kGaugeF32Full = 4;
+bool gauge_fold_phases(qcdgpu_gauge g);
 
 }  // namespace qg
 

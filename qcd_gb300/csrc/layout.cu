@@ -366,6 +366,45 @@ bool download_gauge_aos(qcdgpu_gauge g, double *host)
 
 bool gauge_to_ff(qcdgpu_gauge d, qcdgpu_gauge s);  // dslash_df64.cu
 
+// links of direction mu times e^{i theta_mu / L_mu} (FP32, all 18 reals):
+// the multi-RHS kernels' copy carries the boundary phases, so its forward
+// hops need no phase multiply and its backward hops get the conjugate from U^+
+__global__ void k_fold_phases(float2 *d, int64_t stride, int64_t V, float4 phr, float4 phi)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= V * 4) return;
+  const int mu = (int)(i / V);
+  const int64_t x = i % V;
+  const float pr = mu == 0 ? phr.x : mu == 1 ? phr.y : mu == 2 ? phr.z : phr.w;
+  const float pi = mu == 0 ? phi.x : mu == 1 ? phi.y : mu == 2 ? phi.z : phi.w;
+  float2 *p = d + (int64_t)mu * 9 * stride + x;
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const float2 u = p[k * stride];
+    p[k * stride] = make_float2(pr * u.x - pi * u.y, pr * u.y + pi * u.x);
+  }
+}
+
+bool gauge_fold_phases(qcdgpu_gauge g)
+{
+  if (g->prec != QCDGPU_F32 || g->recon != 18) {
+    set_error("phase folding: FP32 18-real gauge copies only");
+    return false;
+  }
+  double pr[4], pi[4];
+  bool any = false;
+  for (int mu = 0; mu < 4; mu++) {
+    pr[mu] = cos(g->theta[mu] / (double)g->L[mu]);
+    pi[mu] = sin(g->theta[mu] / (double)g->L[mu]);
+    any = any || g->theta[mu] != 0.0;
+  }
+  if (!any) return true;
+  const float4 fr = make_float4((float)pr[0], (float)pr[1], (float)pr[2], (float)pr[3]);
+  const float4 fi = make_float4((float)pi[0], (float)pi[1], (float)pi[2], (float)pi[3]);
+  k_fold_phases<<<grid_for(g->V * 4, 128), 128, 0, stream()>>>((float2 *)g->data, g->stride, g->V, fr, fi);
+  return QG_LAUNCHED("fold_phases");
+}
+
 bool convert_gauge(qcdgpu_gauge d, qcdgpu_gauge s, int force_recon)
 {
   if (d->prec == kGaugeFF) return gauge_to_ff(d, s);

@@ -1375,15 +1375,11 @@ bool dslash_mrhs(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_gauge g, double mp4
   a.N = in->N;
   a.nact = nact;
   a.gstride = g32->stride;
+  // the FP32 copy holds the boundary phases folded into its links
   a.twist_mask = 0;
   for (int mu = 0; mu < 4; mu++) {
     a.phr[mu] = 1.f;
     a.phi[mu] = 0.f;
-    if (g->theta[mu] != 0.0) {
-      a.twist_mask |= 1 << mu;
-      a.phr[mu] = (float)cos(g->theta[mu] / (double)g->L[mu]);
-      a.phi[mu] = (float)sin(g->theta[mu] / (double)g->L[mu]);
-    }
   }
   a.mp4 = (float)mp4;
   a.tm = (float)(dag ? -tm : tm);
@@ -1436,15 +1432,11 @@ bool dslash_mrhs_eo(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_mfield z, qcdgpu
   a.N = in->N;
   a.nact = nact;
   a.gstride = g32->stride;
+  // the FP32 copy holds the boundary phases folded into its links
   a.twist_mask = 0;
   for (int mu = 0; mu < 4; mu++) {
     a.phr[mu] = 1.f;
     a.phi[mu] = 0.f;
-    if (g->theta[mu] != 0.0) {
-      a.twist_mask |= 1 << mu;
-      a.phr[mu] = (float)cos(g->theta[mu] / (double)g->L[mu]);
-      a.phi[mu] = (float)sin(g->theta[mu] / (double)g->L[mu]);
-    }
   }
   a.mp4 = 4.f;
   a.tm = 0.f;

@@ -85,7 +85,9 @@ qcdgpu_gauge gauge_at(qcdgpu_gauge g, int prec)
   const bool full32 = prec == kGaugeF32Full;
   qcdgpu_gauge lo = gauge_new(g->L, g->theta, full32 ? QCDGPU_F32 : prec, 18);
   if (!lo) return nullptr;
-  if (!convert_gauge(lo, g, full32 ? 18 : 0)) {
+  // the full FP32 copy serves the multi-RHS kernels only; it carries the
+  // boundary phases in its links
+  if (!convert_gauge(lo, g, full32 ? 18 : 0) || (full32 && !gauge_fold_phases(lo))) {
     gauge_free(lo);
     return nullptr;
   }
