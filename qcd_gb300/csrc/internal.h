@@ -261,6 +261,24 @@ __device__ __forceinline__ C<R> cdot(C<R> a, C<R> b)
 {
   return {a.re * b.re + a.im * b.im, a.re * b.im - a.im * b.re};
 }
+// acc + a b, acc + conj(a) b and acc - a b as multiply-add chains into the
+// accumulator: four FMAs, no separate product and add (a sum of three
+// complex products costs 2 multiplies + 10 FMAs instead of 6 + 6 + 4 adds)
+template <typename R>
+__device__ __forceinline__ C<R> cmadd(C<R> a, C<R> b, C<R> acc)
+{
+  return {qfma(-a.im, b.im, qfma(a.re, b.re, acc.re)), qfma(a.im, b.re, qfma(a.re, b.im, acc.im))};
+}
+template <typename R>
+__device__ __forceinline__ C<R> cmadd_conj(C<R> a, C<R> b, C<R> acc)
+{
+  return {qfma(a.im, b.im, qfma(a.re, b.re, acc.re)), qfma(-a.im, b.re, qfma(a.re, b.im, acc.im))};
+}
+template <typename R>
+__device__ __forceinline__ C<R> cmsub(C<R> a, C<R> b, C<R> acc)
+{
+  return {qfma(a.im, b.im, qfma(-a.re, b.re, acc.re)), qfma(-a.im, b.re, qfma(-a.re, b.im, acc.im))};
+}
 
 // ---------------------------------------------------------- spinor access
 // Spinor<P, R>::load fills s[12] (k = spin*3 + colour) in working precision R.
@@ -363,9 +381,9 @@ template <typename R>
 __device__ __forceinline__ void rebuild_row2(C<R> U[9])
 {
   // row2 = conj(row0 x row1), exact for U in SU(3)
-  U[6] = conj(U[1] * U[5] - U[2] * U[4]);
-  U[7] = conj(U[2] * U[3] - U[0] * U[5]);
-  U[8] = conj(U[0] * U[4] - U[1] * U[3]);
+  U[6] = conj(cmsub(U[2], U[4], U[1] * U[5]));
+  U[7] = conj(cmsub(U[0], U[5], U[2] * U[3]));
+  U[8] = conj(cmsub(U[1], U[3], U[0] * U[4]));
 }
 
 template <typename R>

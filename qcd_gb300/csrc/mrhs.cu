@@ -318,8 +318,9 @@ __device__ __forceinline__ void mhop_pair(const MArgs &a, int x, const int c[4],
       for (int j = 0; j < 2; j++)
 #pragma unroll
         for (int i = 0; i < 3; i++)
-          uh[3 * j + i] = back ? cdot(U[i], h[3 * j]) + cdot(U[3 + i], h[3 * j + 1]) + cdot(U[6 + i], h[3 * j + 2])
-                               : U[3 * i] * h[3 * j] + U[3 * i + 1] * h[3 * j + 1] + U[3 * i + 2] * h[3 * j + 2];
+          uh[3 * j + i] =
+              back ? cmadd_conj(U[6 + i], h[3 * j + 2], cmadd_conj(U[3 + i], h[3 * j + 1], cdot(U[i], h[3 * j])))
+                   : cmadd(U[3 * i + 2], h[3 * j + 2], cmadd(U[3 * i + 1], h[3 * j + 1], U[3 * i] * h[3 * j]));
       if (twisted) {
         C<float> ph{a.phr[MU], back ? -a.phi[MU] : a.phi[MU]};
 #pragma unroll

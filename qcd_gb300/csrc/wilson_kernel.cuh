@@ -163,7 +163,7 @@ __device__ __forceinline__ void hop_pair(const DArgs &a, int x, const int c[4], 
     for (int j = 0; j < 2; j++)
 #pragma unroll
       for (int i = 0; i < 3; i++)
-        uh[3 * j + i] = U[3 * i] * h[3 * j] + U[3 * i + 1] * h[3 * j + 1] + U[3 * i + 2] * h[3 * j + 2];
+        uh[3 * j + i] = cmadd(U[3 * i + 2], h[3 * j + 2], cmadd(U[3 * i + 1], h[3 * j + 1], U[3 * i] * h[3 * j]));
     if (twisted) {
       C<R> ph{Scalar<R>::get(a.phr[MU], a.phr_h[MU], a.phr_l[MU]), Scalar<R>::get(a.phi[MU], a.phi_h[MU], a.phi_l[MU])};
 #pragma unroll
@@ -182,7 +182,7 @@ __device__ __forceinline__ void hop_pair(const DArgs &a, int x, const int c[4], 
     for (int j = 0; j < 2; j++)
 #pragma unroll
       for (int i = 0; i < 3; i++)
-        uh[3 * j + i] = cdot(U[i], h[3 * j]) + cdot(U[3 + i], h[3 * j + 1]) + cdot(U[6 + i], h[3 * j + 2]);
+        uh[3 * j + i] = cmadd_conj(U[6 + i], h[3 * j + 2], cmadd_conj(U[3 + i], h[3 * j + 1], cdot(U[i], h[3 * j])));
     if (twisted) {
       C<R> ph{Scalar<R>::get(a.phr[MU], a.phr_h[MU], a.phr_l[MU]), -Scalar<R>::get(a.phi[MU], a.phi_h[MU], a.phi_l[MU])};
 #pragma unroll
