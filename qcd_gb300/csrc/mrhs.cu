@@ -375,24 +375,26 @@ __global__ void __launch_bounds__(256, 2) k_wilson_mrhs_simt(const MArgs a, doub
       // slots past nact hold zeros; their results are not stored
       const float mp4r = a.mp4s ? a.mp4s[r] : a.mp4;
       const float tmr = a.tms ? (DAG ? -a.tms[r] : a.tms[r]) : a.tm;
-      if (ainv) {  // A^{-1} = (mp4 - i tm g5) / (mp4^2 + tm^2)
-        const float den = 1.0f / (mp4r * mp4r + tmr * tmr), ar = mp4r * den, ai = -tmr * den;
+      float mx = 0.f;
+      if constexpr (ainv) {  // ch A^{-1} = ch (mp4 - i tm g5) / (mp4^2 + tm^2), no addend
+        const float den = ch / (mp4r * mp4r + tmr * tmr), ar = mp4r * den, ai = -tmr * den;
 #pragma unroll
         for (int k = 0; k < 12; k++) {
           const float g5ai = k < 6 ? ai : -ai;
           acc[q][k] = C<float>{ar * acc[q][k].re - g5ai * acc[q][k].im, ar * acc[q][k].im + g5ai * acc[q][k].re};
+          mx = fmaxf(mx, fmaxf(fabsf(acc[q][k].re), fabsf(acc[q][k].im)));
         }
-      }
-      const float zs = zmode ? nrm[q] : 0.f;
-      const float zm = zmode == 2 ? mp4r * zs : zs, zt = zmode == 2 ? tmr * zs : 0.f;
-      float mx = 0.f;
+      } else {  // ch H in + A z
+        const float zs = nrm[q];
+        const float zm = zmode == 2 ? mp4r * zs : zs, zt = zmode == 2 ? tmr * zs : 0.f;
 #pragma unroll
-      for (int k = 0; k < 12; k++) {
-        const float g5tm = k < 6 ? zt : -zt;
-        const C<float> zk = zmode ? s[q][k] : C<float>{0.f, 0.f};
-        acc[q][k] = C<float>{zm * zk.re - g5tm * zk.im + ch * acc[q][k].re,
-                             zm * zk.im + g5tm * zk.re + ch * acc[q][k].im};
-        mx = fmaxf(mx, fmaxf(fabsf(acc[q][k].re), fabsf(acc[q][k].im)));
+        for (int k = 0; k < 12; k++) {
+          const float g5tm = k < 6 ? zt : -zt;
+          const C<float> zk = s[q][k];
+          acc[q][k] = C<float>{qfma(ch, acc[q][k].re, qfma(-g5tm, zk.im, zm * zk.re)),
+                               qfma(ch, acc[q][k].im, qfma(g5tm, zk.re, zm * zk.im))};
+          mx = fmaxf(mx, fmaxf(fabsf(acc[q][k].re), fabsf(acc[q][k].im)));
+        }
       }
       if (!(mx >= 1.17549435e-38f)) mx = 0.f;
       const float inv = mx > 0.f ? 1.0f / mx : 0.f;

@@ -259,16 +259,17 @@ __global__ void __launch_bounds__(128) k_wilson_eo(const DArgs a)
     hop_pair<2, DAG, SP, GP, RECON, R, true>(a, x, c, acc);
     hop_pair<3, DAG, SP, GP, RECON, R, true>(a, x, c, acc);
     const R ch = Scalar<R>::get(a.ch, a.ch_h, a.ch_l);
-    if (a.ainv) {
-      const R ar = Scalar<R>::get(a.ai_r, a.ai_r_h, a.ai_r_l), ai = Scalar<R>::get(a.ai_i, a.ai_i_h, a.ai_i_l);
+    if (a.ainv) {  // ch A^{-1}: the scale folded into the coefficients
+      const R ar = ch * Scalar<R>::get(a.ai_r, a.ai_r_h, a.ai_r_l), ai = ch * Scalar<R>::get(a.ai_i, a.ai_i_h, a.ai_i_l);
 #pragma unroll
       for (int k = 0; k < 12; k++) {
         const R g5ai = k < 6 ? ai : -ai;
         acc[k] = C<R>{ar * acc[k].re - g5ai * acc[k].im, ar * acc[k].im + g5ai * acc[k].re};
       }
-    }
+    } else if (!a.zmode) {
 #pragma unroll
-    for (int k = 0; k < 12; k++) acc[k] = C<R>{ch * acc[k].re, ch * acc[k].im};
+      for (int k = 0; k < 12; k++) acc[k] = C<R>{ch * acc[k].re, ch * acc[k].im};
+    }
     if (a.zmode) {
       C<R> s[12];
       Spinor<SP, R>::load(a.z, a.z_norm, a.stride, e, s);
@@ -280,8 +281,13 @@ __global__ void __launch_bounds__(128) k_wilson_eo(const DArgs a)
           s[k] = C<R>{mp4 * s[k].re - g5tm * s[k].im, mp4 * s[k].im + g5tm * s[k].re};
         }
       }
+      if (a.ainv) {
 #pragma unroll
-      for (int k = 0; k < 12; k++) acc[k] = acc[k] + s[k];
+        for (int k = 0; k < 12; k++) acc[k] = acc[k] + s[k];
+      } else {  // ch H in + z as one multiply-add per real
+#pragma unroll
+        for (int k = 0; k < 12; k++) acc[k] = C<R>{qfma(ch, acc[k].re, s[k].re), qfma(ch, acc[k].im, s[k].im)};
+      }
     }
     Spinor<SP, R>::store(a.out, a.out_norm, a.stride, e, acc);
     if (a.partials) {
