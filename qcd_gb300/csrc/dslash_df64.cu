@@ -57,15 +57,19 @@ __device__ __forceinline__ F2 split_d(double d)
 {
   const unsigned lo32 = (unsigned)__double2loint(d), hi32 = (unsigned)__double2hiint(d);
   const unsigned e = (hi32 >> 20) & 0x7ffu;
-  const unsigned sign = hi32 & 0x80000000u;
   F2 r;
-  if (e >= 949u && e <= 1150u) {
-    r.h = __uint_as_float(sign | ((e - 896u) << 23) | ((hi32 & 0xfffffu) << 3) | (lo32 >> 29));
-    // the 23 bits below hi as an exact integer-valued float, scaled by 2^(e - 1069)
+  if (e - 949u <= 201u) {  // e in [949, 1150]
+    // (hi32:lo32) << 3 holds the exponent's low 9 bits and the top 23
+    // significand bits in float position; e - 896 = (e mod 512) - 384 here,
+    // so one subtraction rebiases the exponent, and the sign goes back in
+    const unsigned hb = (__funnelshift_l(lo32, hi32, 3) - (384u << 23)) | (hi32 & 0x80000000u);
+    r.h = __uint_as_float(hb);
+    // the 23 bits below hi as an exact integer-valued float, scaled by
+    // 2^(e - 1069) with hi's sign: hi's sign and exponent field less 46
     const float f1 = __fsub_rn(__uint_as_float(0x4B000000u | ((lo32 >> 6) & 0x7fffffu)), 8388608.0f);
-    r.l = __fmul_rn(f1, __uint_as_float(sign | ((e - 942u) << 23)));
+    r.l = __fmul_rn(f1, __uint_as_float((hb & 0xff800000u) - (46u << 23)));
   } else if (e == 0u) {
-    r.h = __uint_as_float(sign);
+    r.h = __uint_as_float(hi32 & 0x80000000u);
     r.l = 0.0f;
   } else {
     r = split_slow(d);
