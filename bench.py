@@ -720,16 +720,16 @@ def run_ours(args, rank, world, local_rank):
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds, 1)
         if not args.no_solve:
             line["config1_8x16"] = config1_solves(q, args.cpu_seconds / 2)
-    line["north_star"] = north_star(precision, serving32)
+    line["solve_summary_32x64"] = solve_summary(precision, serving32)
     return line
 
 
-def north_star(precision, serving32):
-    """the spec comparison at 32^3 x 64, kappa 0.155, true residual
-    1e-10 (last key of the line): RHS-solves/s of the plain FP64 GPU solve
-    (the drop-in), of the batched and the single even/odd mixed-precision
-    solves and of the served stream on that volume, their ratios to the plain
-    solve (target 4), and the served p50 / p99 latency"""
+def solve_summary(precision, serving32):
+    """the solve comparison at 32^3 x 64, kappa 0.155, true residual 1e-10
+    (last key of the line): RHS-solves/s of the plain FP64 GPU solve (the
+    drop-in), of the batched and the single even/odd mixed-precision solves
+    and of the served stream on that volume, their ratios to the plain solve
+    (target 4), and the served p50 / p99 latency"""
     if not precision:
         return None
     base = precision["fp64_cgnr"]["rhs_solves_per_s"]

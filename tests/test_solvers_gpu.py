@@ -1,5 +1,5 @@
 """GPU solver parity. GCR against the reference's own gcr() (golden) and the
-oracle; every other solve is judged the b_minus_Dx.c way (:152-169): the
+oracle; every other solve is checked the b_minus_Dx.c way (:152-169): the
 true residual |b - D x|/|b| recomputed by the CPU oracle in FP64, plus the
 error against an oracle solve."""
 import numpy as np
