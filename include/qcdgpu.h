@@ -569,6 +569,7 @@ typedef struct {
   double max_true_residual; /* largest FP64 |b - op x| / |b| among the RHS */
   double queue_s;           /* submission -> admission */
   double latency_s;         /* submission -> last RHS retired */
+  int total_iters;          /* iterations summed over the RHS */
 } qcdgpu_server_result;
 int qcdgpu_server_create(qcdgpu_server *s, size_t hbm_budget_bytes, int slots);
 int qcdgpu_server_destroy(qcdgpu_server s);

@@ -576,7 +576,8 @@ class Batch:
 
 class ServerResult(C.Structure):
     _fields_ = [("tag", C.c_int), ("status", C.c_int), ("nrhs", C.c_int), ("max_iters", C.c_int),
-                ("max_true_residual", C.c_double), ("queue_s", C.c_double), ("latency_s", C.c_double)]
+                ("max_true_residual", C.c_double), ("queue_s", C.c_double), ("latency_s", C.c_double),
+                ("total_iters", C.c_int)]
 
 
 class Server:
@@ -608,7 +609,8 @@ class Server:
         out = (ServerResult * max_n)()
         n = lib().qcdgpu_server_poll(self.h, C.cast(out, C.c_void_p), max_n)
         return [dict(tag=r.tag, status=r.status, nrhs=r.nrhs, max_iters=r.max_iters,
-                     max_true_residual=r.max_true_residual, queue_s=r.queue_s, latency_s=r.latency_s)
+                     max_true_residual=r.max_true_residual, queue_s=r.queue_s, latency_s=r.latency_s,
+                     total_iters=r.total_iters)
                 for r in out[:n]]
 
     def fetch(self, tag: int, col: int, dst: Field) -> Field:

@@ -32,7 +32,7 @@ struct SrvRequest {
   std::vector<qcdgpu_field> src;  // caller's sources (may be empty)
   std::vector<qcdgpu_field> x, b;
   bool admitted = false, complete = false;
-  int next_col = 0, retired = 0, status = 0, max_iters = 0;
+  int next_col = 0, retired = 0, status = 0, max_iters = 0, total_iters = 0;
   double max_res = 0;
   double t_submit = 0, t_admit = 0, t_done = 0;
   size_t bytes = 0;
@@ -151,6 +151,7 @@ static void complete(qcdgpu_server S, SrvRequest &r)
   res.max_true_residual = r.max_res;
   res.queue_s = r.t_admit - r.t_submit;
   res.latency_s = r.t_done - r.t_submit;
+  res.total_iters = r.total_iters;
   S->results.push_back(res);
 }
 
@@ -168,6 +169,7 @@ static void collect(qcdgpu_server S, SrvGauge &G)
       r.retired++;
       if (st[i] > r.status) r.status = st[i];
       if (it[i] > r.max_iters) r.max_iters = it[i];
+      r.total_iters += it[i];
       if (tr[i] > r.max_res) r.max_res = tr[i];
       if (r.retired == r.nrhs) complete(S, r);
     }

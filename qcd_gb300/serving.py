@@ -58,7 +58,7 @@ def run_stream(server: Server, gauge_ids: list[int], arrivals: list[Arrival], ma
                maxiter: int = 20000) -> dict:
     t0 = time.perf_counter()
     pending = list(arrivals)
-    submitted = completed = rhs_done = 0
+    submitted = completed = rhs_done = rhs_iters = 0
     lat, queue, worst_res, statuses, iters = [], [], 0.0, {}, []
     while True:
         now = time.perf_counter() - t0
@@ -74,6 +74,7 @@ def run_stream(server: Server, gauge_ids: list[int], arrivals: list[Arrival], ma
             lat.append(r["latency_s"])
             queue.append(r["queue_s"])
             iters.append(r["max_iters"])
+            rhs_iters += r["total_iters"]
             worst_res = max(worst_res, r["max_true_residual"])
             statuses[r["status"]] = statuses.get(r["status"], 0) + 1
             server.release(r["tag"])
@@ -90,4 +91,6 @@ def run_stream(server: Server, gauge_ids: list[int], arrivals: list[Arrival], ma
                 rhs_solves_per_s=rhs_done / wall if wall > 0 else 0.0,
                 p50_s=float(np.percentile(lat_a, 50)), p99_s=float(np.percentile(lat_a, 99)),
                 mean_queue_s=float(np.mean(queue)) if queue else None, worst_true_residual=worst_res,
-                statuses=statuses, max_iters=int(max(iters)) if iters else 0)
+                statuses=statuses, max_iters=int(max(iters)) if iters else 0, rhs_iterations=rhs_iters,
+                mean_iters_per_rhs=rhs_iters / rhs_done if rhs_done else None,
+                rhs_iterations_per_s=rhs_iters / wall if wall > 0 else 0.0)

@@ -80,6 +80,7 @@ def test_server_stream_of_mixed_requests(gpu, orc, gauges):
         assert r["status"] == 0, r
         assert r["max_true_residual"] <= tol, r
         assert 0.0 <= r["queue_s"] <= r["latency_s"]
+        assert 0 < r["max_iters"] <= r["total_iters"] <= n * r["max_iters"], r
         for c in range(n):
             sol = srv.fetch(tag, c, x[L]).store()
             opn = "Q" if op == q.OP_Q else "D"
