@@ -185,8 +185,8 @@ __device__ __forceinline__ CF coef(CF z, bool ifl, bool ng)
   return ng ? cneg(r) : r;
 }
 
-// Thread layout: a block of 384 threads covers 128 sites as four groups of
-// three warps; warp w of a group owns colour row i = w for its 32 sites and
+// Thread layout: a block of 96 * kFFGroups threads covers 32 * kFFGroups
+// sites as groups of three warps; warp w of a group owns colour row i = w for its 32 sites and
 // the four accumulators (spins 0..3) of that colour. Per hop each warp
 // projects the neighbour spinor of its colour, the three warps share the
 // half spinors through shared memory, and each warp multiplies its link row.
@@ -212,12 +212,21 @@ __device__ __forceinline__ CF coef(CF z, bool ifl, bool ng)
 // conversions it saves are integer work on the issue-bound FP32 side.
 // Each thread's four spinor components of the next hop are copied into
 // shared memory with cp.async while the current hop computes (two stages,
-// 48 KB per block), so the loads hold no registers.
+// 128 bytes per thread), so the loads hold no registers.
 // (Measured on GB300, 24^3x48: 0.505 -> 0.440 ms per apply; unrolled hops
 // and the 47-bit split: 0.425 ms; staged loads: 0.417 ms. Moving more --
 // the epilogue, whole hops, or whole site groups -- onto the FP64 pipe was
 // slower.)
-constexpr int kFFSites = 128;
+// Block geometry, measured on GB300 at 24^3x48 (ms per apply, groups x
+// blocks per SM: registers): 4 x 3: 56 (spills) 0.372; 4 x 2: 80 0.379;
+// 3 x 4: 56 (spills) 0.376; 3 x 3: 72 0.364; 5 x 2: 64 0.391; 6 x 2: 56
+// 0.393; 2 x 5: 64 0.409; 2 x 6: 56 0.434; 1 x 10: 64 0.397; 1 x 12: 56
+// 0.395. The group barrier's id is a register, so ptxas reserves all 16
+// named barriers per block of more than one group; the forms with more
+// than four such blocks resident per SM were the slowest.
+constexpr int kFFGroups = 3;       // groups of three warps (32 sites) per block
+constexpr int kFFMinBlocks = 3;    // resident blocks per SM the registers are sized for
+constexpr int kFFSites = 32 * kFFGroups;
 
 __device__ __forceinline__ void group_bar(int grp) { asm volatile("bar.sync %0, 96;" ::"r"(grp + 1) : "memory"); }
 
@@ -275,7 +284,7 @@ __device__ __forceinline__ void cp_async_wait()
 
 // staging of the four spinor components a thread projects per hop: two
 // hops in flight, [stage][component][thread]
-constexpr int kFFThreads = 384;
+constexpr int kFFThreads = 96 * kFFGroups;
 constexpr size_t kFFStageBytes = 2 * 4 * kFFThreads * sizeof(double2);
 
 // the float-float operator for one group's 32 sites; returns the thread's |out|^2.
@@ -451,13 +460,13 @@ __device__ __forceinline__ double group_ff(const DArgs &a, int grp, int col, int
 // EO: even/odd kernel on half fields (sites of parity a.eo_par; neighbours
 // read at (full index) >> 1) with the epilogue ch * [A^{-1}] H in + {z | A z}
 template <bool DAG, bool EO, bool AOS>
-__global__ void __launch_bounds__(384, 3) k_wilson_ff(const DArgs a)
+__global__ void __launch_bounds__(kFFThreads, kFFMinBlocks) k_wilson_ff(const DArgs a)
 {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int grp = w / 3, col = w - 3 * grp;
   const int e = a.x0 + blockIdx.x * kFFSites + grp * 32 + lane;  // output index
   const bool act = e < a.V;
-  __shared__ CF hs[4][2][3][32];
+  __shared__ CF hs[kFFGroups][2][3][32];
   int c[4];
   const int x = ff_site<EO>(a, e, act, c);
   extern __shared__ double2 ff_stage[];
@@ -513,8 +522,9 @@ bool gauge_to_ff(qcdgpu_gauge d, qcdgpu_gauge s)
   return QG_LAUNCHED("gauge_to_ff");
 }
 
-// the staging buffer is dynamic shared memory (48 KB, above the default
-// limit): opted in once per instantiation
+// the staging buffer is dynamic shared memory (36 KB for three groups; the
+// attribute lifts the 48 KB default limit for larger blocks): opted in once
+// per instantiation
 template <bool D, bool E, bool A = false>
 static void launch_ff(const DArgs &a, unsigned grid)
 {
