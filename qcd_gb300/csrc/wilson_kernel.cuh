@@ -193,8 +193,12 @@ __device__ __forceinline__ void hop_pair(const DArgs &a, int x, const int c[4], 
   }
 }
 
+// FP32 / FP16 storage: registers capped for seven blocks per SM (72; 80
+// uncapped), measured at 24^3x48: FP16 48.9 -> 47.1 us, FP32 57.3 -> 55.3 us
+// per apply (a cap of 64 spills and loses). The even/odd kernel below keeps
+// the uncapped form, which solves 0.7 % faster.
 template <bool DAG, int SP, int GP, int RECON, typename R>
-__global__ void __launch_bounds__(128) k_wilson(const DArgs a)
+__global__ void __launch_bounds__(128, SP != QCDGPU_F64 ? 7 : 1) k_wilson(const DArgs a)
 {
   int x = a.x0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
   double n2 = 0.0;
