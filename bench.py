@@ -521,15 +521,15 @@ def precision_bench(q, L, kappa, n_batch, cap):
     return out
 
 
-def batching_bench(q, L, kappa, nrhs, caps=(4, 8, 16), sweep_rhs=16):
+def batching_bench(q, L, kappa, nrhs, caps=(4, 8, 16, 32), sweep_rhs=32):
     """The batching configuration at L (48^3 x 96), kappa: nrhs right-hand
     sides = 8 source positions x 12 spin-colour columns, solved to 1e-10 by
     even/odd batches with continuous admission. First the RHS-per-block sweep
     inside the solve (the first sweep_rhs columns at each batch capacity in
-    caps; 32 per block does not fit: every slot keeps ~5.4 GB of FP64
-    even/odd state at this volume besides its 4 GB of FP64 x and b), then all
-    nrhs columns at the fastest capacity. Beside them one even/odd FP16 solve
-    and one plain FP64 solve of the first column."""
+    caps; at 32 per block the batch holds ~100 GB and the 32 pairs of FP64 x
+    and b in flight ~131 GB), then all nrhs columns at the fastest capacity.
+    Beside them one even/odd FP16 solve and one plain FP64 solve of the first
+    column."""
     g = q.Gauge(L, THETA).synthetic(4, EPS_PLAQ_060)
     out = {"lattice_txyz": list(L), "kappa": kappa, "rhs": nrhs, "tol": 1e-10,
            "sources": "points at t in {0, L_t/2} x (x, y, z) in {0, (L/2,0,0), (0,L/2,0), (0,0,L/2)}, 12 columns each"}

@@ -529,14 +529,18 @@ typedef struct qcdgpu_batch_s *qcdgpu_batch;
 int qcdgpu_batch_create(qcdgpu_batch *b, qcdgpu_gauge g, int capacity);
 /* the same, solving each system through its even/odd Schur complement on
  * the half lattice (t extent even): fewer iterations, same FP64 true
- * residual test; each slot holds three more FP64 half-lattice fields */
+ * residual test; each slot holds one more FP64 half-lattice field (x_e),
+ * and keeps two more (c_e, A^{-1} b_o) in its x until it retires */
 int qcdgpu_batch_create_eo(qcdgpu_batch *b, qcdgpu_gauge g, int capacity);
 int qcdgpu_batch_destroy(qcdgpu_batch b);
 /* Solve op x = rhs (op QCDGPU_OP_D or QCDGPU_OP_Q; x, rhs FP64 fields that
- * stay owned by the caller and untouched by it until polled). maxiter <= 0:
- * 100000; delta <= 0: 0.1. Returns the slot, -1 when the batch is full, -2 on
- * error. A right-hand side already solved by x = 0 is reported by the next
- * poll without taking a slot. */
+ * stay owned by the caller and untouched by it until polled; x holds the
+ * slot's work state until then and the solution after; x may be neither the
+ * x nor the rhs of another right-hand side in the batch, rhs not another's
+ * x). maxiter <= 0: 100000;
+ * delta <= 0: 0.1. Returns the slot, -1 when the batch is full, -2 on error.
+ * A right-hand side already solved at x_e = 0 (x = 0 for full-lattice
+ * batches) is reported by the next poll without taking a slot. */
 int qcdgpu_batch_add(qcdgpu_batch b, qcdgpu_field x, qcdgpu_field rhs, double kappa, double mu, int op,
                      double tol, int maxiter, double delta, int tag);
 /* Run `iterations` (rounded up to a multiple of 16) iterations of every

@@ -80,6 +80,7 @@ struct qcdgpu_field_s {
   void *data;
   float *norm;  // F16 only
   size_t bytes;
+  bool view;    // data lies in another field's allocation (not freed with it)
 };
 
 struct qcdgpu_gauge_s {
@@ -97,6 +98,9 @@ namespace qg {
 
 // field allocation helpers (runtime.cu)
 qcdgpu_field field_new(const int L[4], int prec);
+// a field of lattice L whose data starts at `data`, inside an allocation
+// the caller keeps alive (F64 or F32); field_free releases only the handle
+qcdgpu_field field_view(const int L[4], int prec, void *data);
 void field_free(qcdgpu_field f);
 qcdgpu_gauge gauge_new(const int L[4], const double theta[4], int prec, int recon);
 void gauge_free(qcdgpu_gauge g);

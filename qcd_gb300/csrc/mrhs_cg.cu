@@ -243,7 +243,10 @@ struct BSlot {
   int tag;
   qcdgpu_field x, b;  // caller's FP64 fields
   // even/odd batches: the slot's FP64 half fields -- system right-hand side
-  // c_e = b_e + H_eo A^{-1} b_o / 2, A^{-1} b_o, and the solution x_e
+  // c_e = b_e + H_eo A^{-1} b_o / 2, A^{-1} b_o, and the solution x_e. x is
+  // written only when the slot retires, so c_e and A^{-1} b_o are kept in
+  // x's own memory until then (views; their own allocations when x has no
+  // room for two half fields); x_e comes from the batch's per-slot pool.
   qcdgpu_field ce, to, xe;
   int op;             // QCDGPU_OP_D or QCDGPU_OP_Q
   double mp4, tm, bn, tol, delta, maxr, hint, true_res;
@@ -269,7 +272,7 @@ struct qcdgpu_batch_s {
   float4 *xs;                  // FP32 solution increments (layout of MX)
   qcdgpu_field rt, r, up, bd;  // FP64 work shared by the slots' reliable updates
   qcdgpu_field u64, r32, u32, s32;  // even/odd: FP64 odd temp; FP32 restart fields
-  std::vector<std::vector<qcdgpu_field>> spare;  // even/odd: free (ce, to, xe) sets
+  std::vector<qcdgpu_field> spare;  // even/odd: free per-slot x_e fields
   double *s;                   // device scalars, (M_HIST + kMChunk) * cap
   float *mp4s, *tms;           // device per-slot diagonal
   double *part;                // device partials
@@ -302,8 +305,7 @@ static void batch_free(qcdgpu_batch b)
   for (auto f : {b->rt, b->r, b->up, b->bd, b->u64, b->r32, b->u32, b->s32}) field_free(f);
   for (auto &sl : b->slots)
     for (auto f : {sl.ce, sl.to, sl.xe}) field_free(f);
-  for (auto &set : b->spare)
-    for (auto f : set) field_free(f);
+  for (auto f : b->spare) field_free(f);
   cudaFree(b->s);
   cudaFree(b->mp4s);
   cudaFree(b->tms);
@@ -356,10 +358,8 @@ static qcdgpu_batch batch_new(qcdgpu_gauge g, int cap, bool eo)
     b->s32 = field_new(b->Ls, QCDGPU_F32);
     ok = ok && b->u && b->u64 && b->r32 && b->u32 && b->s32;
     for (int k = 0; ok && k < cap; k++) {
-      std::vector<qcdgpu_field> set;
-      for (int i = 0; i < 3; i++) set.push_back(field_new(b->Ls, QCDGPU_F64));
-      b->spare.push_back(set);
-      ok = set[0] && set[1] && set[2];
+      b->spare.push_back(field_new(b->Ls, QCDGPU_F64));
+      ok = b->spare.back() != nullptr;
     }
   }
   size_t ns = (size_t)(M_HIST + kMChunk) * cap;
@@ -452,6 +452,28 @@ static bool copy_slot(qcdgpu_batch B, int from, int to)
          QG_CUDA(cudaMemcpyAsync(B->tms + to, B->tms + from, sizeof(float), cudaMemcpyDeviceToDevice, stream()));
 }
 
+// an even/odd slot's half fields go back: x_e to the pool, the handles of
+// c_e and A^{-1} b_o freed (with their memory when they are not views)
+static void slot_release_eo(qcdgpu_batch B, BSlot &sl)
+{
+  if (sl.xe) B->spare.push_back(sl.xe);
+  field_free(sl.ce);
+  field_free(sl.to);
+  sl.ce = sl.to = sl.xe = nullptr;
+}
+
+// x = (x_e, x_o), x_o = A^{-1} b_o + A^{-1} H_oe x_e / 2, written over the
+// views of c_e and A^{-1} b_o in x (A^{-1} b_o is read into r first); then
+// the slot's half fields go back
+static bool slot_finish_eo(qcdgpu_batch B, BSlot &sl)
+{
+  const bool ok =
+      dslash_eo(B->r, sl.xe, sl.to, B->g, sl.mp4, sl.tm, false, 1, 0.5, true, 1, nullptr, QCDGPU_ARITH_DF64) &&
+      eo_merge(sl.x, sl.xe, B->r);
+  slot_release_eo(B, sl);
+  return ok;
+}
+
 int batch_add(qcdgpu_batch B, qcdgpu_field x, qcdgpu_field b, double kappa, double mu, int op, double tol,
               int maxiter, double delta, int tag)
 {
@@ -460,6 +482,11 @@ int batch_add(qcdgpu_batch B, qcdgpu_field x, qcdgpu_field b, double kappa, doub
     set_error("batch add: FP64 x, b on the batch's lattice, kappa > 0, op D or Q");
     return -2;
   }
+  for (const BSlot &o : B->slots)
+    if (o.x == x || o.x == b || o.b == x) {
+      set_error("batch add: x or b is a field of a right-hand side still in the batch");
+      return -2;
+    }
   if (B->nact >= B->cap) return -1;
   // the batch's stream starts after the caller's work on x and b
   if (!QG_CUDA(cudaEventRecord(B->ev_in, stream())) || !QG_CUDA(cudaStreamWaitEvent(B->st, B->ev_in, 0))) return -2;
@@ -483,23 +510,30 @@ int batch_add(qcdgpu_batch B, qcdgpu_field x, qcdgpu_field b, double kappa, doub
   const int k = B->nact;
   sl.ce = sl.to = sl.xe = nullptr;
   if (B->eo) {
-    // c_e = b_e + H_eo A^{-1} b_o / 2 with the slot's own half fields
-    std::vector<qcdgpu_field> set = B->spare.back();
+    // c_e = b_e + H_eo A^{-1} b_o / 2 with the slot's own half fields; c_e
+    // and A^{-1} b_o in x's memory when it holds two half fields
+    sl.xe = B->spare.back();
     B->spare.pop_back();
-    sl.ce = set[0];
-    sl.to = set[1];
-    sl.xe = set[2];
-    const bool ok = slot_bd(B, sl) && eo_split(B->rt, B->r, B->bd) && eo_diag(sl.to, B->r, sl.mp4, mu, true) &&
+    const size_t hb = B->rt->bytes;
+    if (x->bytes >= 2 * hb) {
+      sl.ce = field_view(B->Ls, QCDGPU_F64, x->data);
+      sl.to = field_view(B->Ls, QCDGPU_F64, (char *)x->data + hb);
+    } else {
+      sl.ce = field_new(B->Ls, QCDGPU_F64);
+      sl.to = field_new(B->Ls, QCDGPU_F64);
+    }
+    const bool ok = sl.ce && sl.to && slot_bd(B, sl) && eo_split(B->rt, B->r, B->bd) &&
+                    eo_diag(sl.to, B->r, sl.mp4, mu, true) &&
                     dslash_eo(sl.ce, sl.to, B->rt, B->g, sl.mp4, mu, false, 0, 0.5, false, 1, nullptr,
                               QCDGPU_ARITH_DF64) &&
                     blas_zero(sl.xe);
     if (!ok) {
-      B->spare.push_back(set);
+      slot_release_eo(B, sl);
       return -2;
     }
   }
   auto give_back = [&]() {
-    if (B->eo) B->spare.push_back({sl.ce, sl.to, sl.xe});
+    if (B->eo) slot_release_eo(B, sl);
   };
   if (!slot_residual(B, k, sl, B->rudev + 4 * k) ||
       !QG_CUDA(cudaMemcpyAsync(B->ruhost + 4 * k, B->rudev + 4 * k, sizeof(double) * 4, cudaMemcpyDeviceToHost,
@@ -524,8 +558,9 @@ int batch_add(qcdgpu_batch B, qcdgpu_field x, qcdgpu_field b, double kappa, doub
   // a fresh slot starts with beta = 0, so the shared p update leaves p = r
   if (!set_scalar(B, M_RR, k, rr) || !set_scalar(B, M_BETA, k, 0.0)) return -2;
   if (bn2 == 0.0 || rel <= tol) {
+    // solved by x_e = 0: x = (0, A^{-1} b_o) for even/odd batches
+    if (B->eo && !slot_finish_eo(B, sl)) return -2;
     B->done.push_back(BDone{tag, 0, 0, 0, rel});
-    give_back();
     return k;
   }
   B->slots.push_back(sl);
@@ -537,13 +572,7 @@ int batch_add(qcdgpu_batch B, qcdgpu_field x, qcdgpu_field b, double kappa, doub
 static bool retire(qcdgpu_batch B, int k, int status)
 {
   BSlot &sl = B->slots[(size_t)k];
-  if (B->eo) {
-    // x_o = A^{-1} b_o + A^{-1} H_oe x_e / 2, then x = (x_e, x_o)
-    if (!dslash_eo(B->r, sl.xe, sl.to, B->g, sl.mp4, sl.tm, false, 1, 0.5, true, 1, nullptr, QCDGPU_ARITH_DF64) ||
-        !eo_merge(sl.x, sl.xe, B->r))
-      return false;
-    B->spare.push_back({sl.ce, sl.to, sl.xe});
-  }
+  if (B->eo && !slot_finish_eo(B, sl)) return false;
   B->done.push_back(BDone{sl.tag, status, sl.iters, sl.updates, sl.true_res});
   const int last = B->nact - 1;
   if (k != last) {
@@ -811,7 +840,7 @@ size_t qcdgpu_batch_bytes(qcdgpu_batch b)
 {
   if (!b) return 0;
   size_t n = 4 * b->rs->bytes + (size_t)12 * b->Vs * b->cap * sizeof(float2) + 3 * b->rt->bytes + b->bd->bytes;
-  if (b->eo) n += b->u->bytes + b->u64->bytes + 3 * b->r32->bytes + (size_t)3 * b->cap * b->rt->bytes;
+  if (b->eo) n += b->u->bytes + b->u64->bytes + 3 * b->r32->bytes + (size_t)b->cap * b->rt->bytes;
   return n;
 }
 

@@ -109,10 +109,27 @@ qcdgpu_field field_new(const int L[4], int prec)
   return f;
 }
 
+qcdgpu_field field_view(const int L[4], int prec, void *data)
+{
+  if (prec != QCDGPU_F64 && prec != QCDGPU_F32) {
+    set_error("field view: F64 or F32 only");
+    return nullptr;
+  }
+  auto *f = new qcdgpu_field_s();
+  memcpy(f->L, L, sizeof(f->L));
+  f->V = (int64_t)L[0] * L[1] * L[2] * L[3];
+  f->stride = pad_stride(f->V);
+  f->prec = prec;
+  f->bytes = spinor_bytes(prec, f->stride);
+  f->data = data;
+  f->view = true;
+  return f;
+}
+
 void field_free(qcdgpu_field f)
 {
   if (!f) return;
-  cudaFree(f->data);
+  if (!f->view) cudaFree(f->data);
   delete f;
 }
 

@@ -82,7 +82,7 @@ static size_t batch_bytes_est(const int L[4], int slots)
   const size_t mf = (size_t)12 * Vs * slots * sizeof(__half2) + (size_t)Vs * slots * sizeof(float);
   const size_t f64 = field_bytes_f64(Ls), f32 = f64 / 2;
   size_t n = 4 * mf + (size_t)12 * Vs * slots * sizeof(float2) + 3 * f64 + field_bytes_f64(L);
-  if (eo) n += mf + f64 + 3 * f32 + (size_t)3 * slots * f64;
+  if (eo) n += mf + f64 + 3 * f32 + (size_t)slots * f64;
   return n;
 }
 

@@ -144,6 +144,38 @@ def test_batch_full_and_zero_rhs(gpu, orc):
         f.close()
 
 
+def test_batch_eo_zero_rhs_and_fields_in_use(gpu, orc):
+    """Even/odd batches keep a slot's c_e and A^{-1} b_o in its x until it
+    retires: a zero right-hand side still returns x = 0 exactly, x may not
+    be shared with a right-hand side in flight, and a converged x holds the
+    solution over the work state."""
+    u = orc.gauge_synthetic(L, 16, EPS_PLAQ_060)
+    g = q.Gauge(L, TH).load(u)
+    batch = q.Batch(g, 2, eo=True)
+    b = orc.gaussian_spinor(L, 710)
+    fb, fz = q.Field(L).load(b), q.Field(L)
+    x1, x2, xz = q.Field(L), q.Field(L), q.Field(L)
+    xz.load(orc.gaussian_spinor(L, 711))  # overwritten by the solve
+    assert batch.add(xz, fz, 0.15, tag=7) >= 0
+    assert batch.active == 0
+    assert batch.poll() == [(7, 0, 0, 0.0)]
+    assert not np.any(xz.store())
+    assert batch.add(x1, fb, 0.15, tag=1) == 0
+    with pytest.raises(q.QcdGpuError):
+        batch.add(x1, fz, 0.15, tag=2)  # x of a right-hand side in flight
+    with pytest.raises(q.QcdGpuError):
+        batch.add(x2, x1, 0.15, tag=3)  # its x as a right-hand side
+    with pytest.raises(q.QcdGpuError):
+        batch.add(fb, fz, 0.15, tag=4)  # its right-hand side as x
+    res = _run(batch, [])
+    assert res[1][0] == 0
+    tr = orc.true_residual(x1.store(), b, u, L, TH, 0.15)
+    assert tr <= 1e-10, tr
+    batch.close()
+    for f in (fb, fz, x1, x2, xz, g):
+        f.close()
+
+
 def test_batch_on_tcgen05_kernel(gpu, orc, eo):
     """The batched solver on the tcgen05 multi-RHS kernel (16-slot capacity):
     every request converges to its FP64 true residual, and a request solved
