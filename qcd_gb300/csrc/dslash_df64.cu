@@ -222,8 +222,10 @@ __device__ __forceinline__ CF coef(CF z, bool ifl, bool ng)
 // 3 x 4: 56 (spills) 0.376; 3 x 3: 72 0.364; 5 x 2: 64 0.391; 6 x 2: 56
 // 0.393; 2 x 5: 64 0.409; 2 x 6: 56 0.434; 1 x 10: 64 0.397; 1 x 12: 56
 // 0.395. The group barrier's id is a register, so ptxas reserves all 16
-// named barriers per block of more than one group; the forms with more
-// than four such blocks resident per SM were the slowest.
+// named barriers per block of more than one group, and ncu reports the
+// barriers as a limit of four resident blocks per SM. Immediate ids (a
+// warp-uniform switch over the groups) lift that limit but cost every form
+// 4-11 % (3 x 3: 0.406 ms; the branches sit in the unrolled hop loop).
 constexpr int kFFGroups = 3;       // groups of three warps (32 sites) per block
 constexpr int kFFMinBlocks = 3;    // resident blocks per SM the registers are sized for
 constexpr int kFFSites = 32 * kFFGroups;
