@@ -107,6 +107,24 @@ def test_vectors_allocate_and_checks_run_without_gpu(qlib):
     geo2.close()
 
 
+def test_server_result_layout_matches_the_header(tmp_path):
+    """the ctypes mirror of qcdgpu_server_result has the C struct's size and
+    field offsets (compiled from include/qcdgpu.h with gcc)"""
+    import subprocess
+
+    fields = [f[0] for f in q.ServerResult._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "qcdgpu.h"\nint main(void){\n'
+                   ' printf("%zu", sizeof(qcdgpu_server_result));\n'
+                   + "".join(f' printf(" %zu", offsetof(qcdgpu_server_result, {n}));\n' for n in fields)
+                   + ' printf("\\n"); return 0; }\n')
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=gnu99", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    out = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert out[0] == C.sizeof(q.ServerResult)
+    assert out[1:] == [getattr(q.ServerResult, n).offset for n in fields]
+
+
 def test_c_program_links_against_the_library(qlib, tmp_path):
     """A qcd_lib-style C driver compiles against include/qcdgpu.h and links."""
     import subprocess
