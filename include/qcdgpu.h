@@ -402,10 +402,12 @@ enum {
   QCDGPU_SOLVER_GCR = 0,
   QCDGPU_SOLVER_BICGSTAB = 1,
   QCDGPU_SOLVER_CGNR = 2,
-  /* CGNR on the even/odd (Schur) preconditioned system; the t extent must
-   * be even. Same convergence test on the full true residual. */
+  /* CGNR on the even/odd (Schur) preconditioned system; every lattice
+   * extent must be even (the periodic checkerboard). Same convergence test
+   * on the full true residual. */
   QCDGPU_SOLVER_CGNR_EO = 3,
-  /* BiCGstab(l) (Sleijpen-Fokkema) on the even/odd Schur complement, l =
+  /* BiCGstab(l) (Sleijpen-Fokkema) on the even/odd Schur complement (every
+   * extent even), l =
    * restart when 1..16 (else 8); inner iterations in inner_prec with FP64
    * defect correction. Plain BiCGstab stagnates near the critical kappa
    * (SOLVER_BICGSTAB reports that as status 1); this one converges there. */
@@ -528,7 +530,7 @@ int qcdgpu_mrhs_tc_test_hook(int skip_mma, int polls);
 typedef struct qcdgpu_batch_s *qcdgpu_batch;
 int qcdgpu_batch_create(qcdgpu_batch *b, qcdgpu_gauge g, int capacity);
 /* the same, solving each system through its even/odd Schur complement on
- * the half lattice (t extent even): fewer iterations, same FP64 true
+ * the half lattice (every extent even): fewer iterations, same FP64 true
  * residual test; each slot holds one more FP64 half-lattice field (x_e),
  * and keeps two more (c_e, A^{-1} b_o) in its x until it retires */
 int qcdgpu_batch_create_eo(qcdgpu_batch *b, qcdgpu_gauge g, int capacity);

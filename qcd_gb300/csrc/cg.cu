@@ -376,8 +376,8 @@ int solve_cgnr_engine(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4
 // A x_e - H_eo t_o / 4 (with |M x_e|^2 summed in the second epilogue).
 int solve_cgnr_eo(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp4, double tm, qcdgpu_solve_params *p)
 {
-  if (b->L[0] % 2 != 0) {
-    set_error("even/odd solve: the t extent must be even");
+  if (!eo_lattice(b->L)) {
+    set_error("even/odd solve: every lattice extent must be even");
     return 3;
   }
   Held w;
@@ -504,7 +504,7 @@ static Geom full_geom(const int L[4])
 static bool halves_of(qcdgpu_field e, qcdgpu_field o, qcdgpu_field full)
 {
   if (e->prec != QCDGPU_F64 || o->prec != QCDGPU_F64 || full->prec != QCDGPU_F64 || !same_shape(e, o) ||
-      full->L[0] % 2 != 0 || e->L[0] * 2 != full->L[0] || e->L[1] != full->L[1] || e->L[2] != full->L[2] ||
+      !eo_lattice(full->L) || e->L[0] * 2 != full->L[0] || e->L[1] != full->L[1] || e->L[2] != full->L[2] ||
       e->L[3] != full->L[3]) {
     set_error("even/odd split: FP64 half fields of the full field's lattice");
     return false;
@@ -605,8 +605,8 @@ int solve_bicgstabl_eo(qcdgpu_field x, qcdgpu_field b, qcdgpu_gauge g, double mp
                        qcdgpu_solve_params *p)
 {
   using cplx = std::complex<double>;
-  if (b->L[0] % 2 != 0) {
-    set_error("even/odd solve: the t extent must be even");
+  if (!eo_lattice(b->L)) {
+    set_error("even/odd solve: every lattice extent must be even");
     return 3;
   }
   Held w;

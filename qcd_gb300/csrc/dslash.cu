@@ -147,10 +147,11 @@ bool dslash_eo(qcdgpu_field out, qcdgpu_field in, qcdgpu_field z, qcdgpu_gauge g
                int par, double ch, bool ainv, int zmode, double *partials, int arith, const CgFuse *fuse)
 {
   if (!out || !in || !g || out == in || (zmode && (!z || z == out)) || in->prec != out->prec ||
-      in->prec != g->prec || (z && z->prec != in->prec) || g->L[0] % 2 != 0 || in->L[0] * 2 != g->L[0] ||
+      in->prec != g->prec || (z && z->prec != in->prec) || !eo_lattice(g->L) || in->L[0] * 2 != g->L[0] ||
       in->L[1] != g->L[1] || in->L[2] != g->L[2] || in->L[3] != g->L[3] || !same_shape(out, in) ||
       (z && !same_shape(z, in))) {
-    set_error("even/odd operator: half fields of one precision on the gauge field's half lattice");
+    set_error("even/odd operator: half fields of one precision on the gauge field's half lattice (every extent "
+              "even)");
     return false;
   }
   DArgs a;

@@ -59,6 +59,12 @@ struct StreamScope {
 // ------------------------------------------------------------------ fields
 inline int64_t pad_stride(int64_t V) { return (V + 127) / 128 * 128; }
 
+// The even/odd (checkerboard) decomposition holds on a periodic lattice only
+// when every extent is even: across the boundary of an odd extent a site's
+// neighbour has its own parity. The half fields pair the sites 2e, 2e + 1
+// of a t-row, which needs the even t extent as well.
+inline bool eo_lattice(const int L[4]) { return L[0] % 2 == 0 && L[1] % 2 == 0 && L[2] % 2 == 0 && L[3] % 2 == 0; }
+
 // Internal gauge storage used by the float-float operator: every link entry
 // as a float pair (re_hi, re_lo, im_hi, im_lo) in one float4, 4 mu x 9 blocks,
 // with the boundary phase e^{i theta_mu / L_mu} already multiplied into the

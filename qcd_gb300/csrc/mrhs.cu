@@ -1412,10 +1412,11 @@ bool dslash_mrhs_eo(qcdgpu_mfield out, qcdgpu_mfield in, qcdgpu_mfield z, qcdgpu
                     unsigned *nblocks)
 {
   if (!out || !in || !g || out == in || out->N != in->N || out->V != in->V || (zmode && (!z || z == out)) ||
-      (z && (z->N != in->N || z->V != in->V)) || g->prec != QCDGPU_F64 || g->L[0] % 2 != 0 ||
+      (z && (z->N != in->N || z->V != in->V)) || g->prec != QCDGPU_F64 || !eo_lattice(g->L) ||
       in->L[0] * 2 != g->L[0] || in->L[1] != g->L[1] || in->L[2] != g->L[2] || in->L[3] != g->L[3] ||
       memcmp(out->L, in->L, sizeof(in->L)) != 0 || nact < 0 || nact > in->N || !mp4s || !tms) {
-    set_error("even/odd multi-RHS operator: half-lattice fields of one shape, per-slot diagonal");
+    set_error("even/odd multi-RHS operator: half-lattice fields of one shape (every extent even), per-slot "
+              "diagonal");
     return false;
   }
   qcdgpu_gauge g32 = gauge_at(g, kGaugeF32Full);

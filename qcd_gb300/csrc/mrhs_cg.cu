@@ -324,8 +324,8 @@ static void batch_free(qcdgpu_batch b)
 
 static qcdgpu_batch batch_new(qcdgpu_gauge g, int cap, bool eo)
 {
-  if (!g || g->prec != QCDGPU_F64 || cap < 1 || cap > 64 || (eo && g->L[0] % 2 != 0)) {
-    set_error("batch: FP64 gauge field, 1..64 slots, even t extent for even/odd");
+  if (!g || g->prec != QCDGPU_F64 || cap < 1 || cap > 64 || (eo && !eo_lattice(g->L))) {
+    set_error("batch: FP64 gauge field, 1..64 slots, every extent even for even/odd");
     return nullptr;
   }
   auto *b = new qcdgpu_batch_s();
@@ -841,6 +841,9 @@ size_t qcdgpu_batch_bytes(qcdgpu_batch b)
   if (!b) return 0;
   size_t n = 4 * b->rs->bytes + (size_t)12 * b->Vs * b->cap * sizeof(float2) + 3 * b->rt->bytes + b->bd->bytes;
   if (b->eo) n += b->u->bytes + b->u64->bytes + 3 * b->r32->bytes + (size_t)b->cap * b->rt->bytes;
+  for (const auto &sl : b->slots)  // c_e, A^{-1} b_o outside x (x too small for both)
+    for (auto f : {sl.ce, sl.to})
+      if (f && !f->view) n += f->bytes;
   return n;
 }
 

@@ -70,8 +70,8 @@ static size_t field_bytes_f64(const int L[4])
   return (size_t)pad_stride((int64_t)L[0] * L[1] * L[2] * L[3]) * 12 * sizeof(double2);
 }
 
-// batches of lattices with an even t extent solve the even/odd system
-static bool use_eo(const int L[4]) { return L[0] % 2 == 0; }
+// batches of lattices with even extents solve the even/odd system
+static bool use_eo(const int L[4]) { return eo_lattice(L); }
 
 // device bytes of a batch of `slots` slots on lattice L (mirrors batch_new)
 static size_t batch_bytes_est(const int L[4], int slots)
@@ -82,7 +82,11 @@ static size_t batch_bytes_est(const int L[4], int slots)
   const size_t mf = (size_t)12 * Vs * slots * sizeof(__half2) + (size_t)Vs * slots * sizeof(float);
   const size_t f64 = field_bytes_f64(Ls), f32 = f64 / 2;
   size_t n = 4 * mf + (size_t)12 * Vs * slots * sizeof(float2) + 3 * f64 + field_bytes_f64(L);
-  if (eo) n += mf + f64 + 3 * f32 + (size_t)slots * f64;
+  if (eo) {
+    n += mf + f64 + 3 * f32 + (size_t)slots * f64;
+    // c_e and A^{-1} b_o get their own memory when x cannot hold both
+    if (2 * f64 > field_bytes_f64(L)) n += (size_t)2 * slots * f64;
+  }
   return n;
 }
 

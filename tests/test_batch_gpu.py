@@ -176,6 +176,52 @@ def test_batch_eo_zero_rhs_and_fields_in_use(gpu, orc):
         f.close()
 
 
+def test_batch_eo_lattice_whose_x_cannot_hold_the_slot_fields(gpu, orc):
+    """6x4x2x2: a full field pads to 128 sites and so does a half field, so x
+    cannot hold c_e and A^{-1} b_o and the slot allocates them itself"""
+    L2 = (6, 4, 2, 2)
+    u = orc.gauge_synthetic(L2, 17, EPS_PLAQ_060)
+    g = q.Gauge(L2, TH).load(u)
+    batch = q.Batch(g, 2, eo=True)
+    bs = [orc.gaussian_spinor(L2, 720 + i) for i in range(3)]
+    fbs = [q.Field(L2).load(b) for b in bs]
+    fxs = [q.Field(L2) for _ in bs]
+    held = batch.nbytes()
+    assert batch.add(fxs[0], fbs[0], 0.15, tag=0) == 0
+    assert batch.nbytes() > held  # the slot's own c_e and A^{-1} b_o
+    res = _run(batch, [(i, fxs[i], fbs[i], 0.14 + 0.005 * i, 0.01 * i, q.OP_D, 1e-10) for i in (1, 2)])
+    assert sorted(res) == [0, 1, 2]
+    for i in range(3):
+        assert res[i][0] == 0, res[i]
+        tr = orc.true_residual(fxs[i].store(), bs[i], u, L2, TH, 0.15 if i == 0 else 0.14 + 0.005 * i, 0.01 * i)
+        assert tr <= 1e-10, (i, tr)
+    assert batch.nbytes() == held
+    batch.close()
+    for f in fbs + fxs + [g]:
+        f.close()
+
+
+def test_even_odd_needs_every_extent_even(gpu, orc):
+    """across the periodic boundary of an odd extent a site's neighbour has
+    its own parity, so the checkerboard split does not hold: the even/odd
+    batch and solve refuse such lattices, the full-lattice ones solve them"""
+    L2 = (4, 3, 2, 2)
+    u = orc.gauge_synthetic(L2, 18, EPS_PLAQ_060)
+    g = q.Gauge(L2, TH).load(u)
+    b = orc.gaussian_spinor(L2, 730)
+    fb, fx = q.Field(L2).load(b), q.Field(L2)
+    with pytest.raises(q.QcdGpuError):
+        q.Batch(g, 2, eo=True)
+    for solver in (q.SOLVER_CGNR_EO, q.SOLVER_BICGSTABL_EO):
+        with pytest.raises(q.QcdGpuError):
+            q.solve(fx, fb, g, 0.15, 0.0, solver=solver, inner_prec=q.F64, tol=1e-10)
+    p = q.solve(fx, fb, g, 0.15, 0.0, solver=q.SOLVER_CGNR, inner_prec=q.F64, tol=1e-10)
+    assert p.status == 0
+    assert orc.true_residual(fx.store(), b, u, L2, TH, 0.15) <= 1e-10
+    for f in (fb, fx, g):
+        f.close()
+
+
 def test_batch_on_tcgen05_kernel(gpu, orc, eo):
     """The batched solver on the tcgen05 multi-RHS kernel (16-slot capacity):
     every request converges to its FP64 true residual, and a request solved
