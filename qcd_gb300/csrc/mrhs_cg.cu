@@ -548,15 +548,16 @@ int batch_add(qcdgpu_batch B, qcdgpu_field x, qcdgpu_field b, double kappa, doub
   sl.hint = tol * sl.maxr;
   unsigned g = (unsigned)((B->Vs + 127) / 128);
   k_mx_copy<<<g, 128, 0, stream()>>>(mx(B), 0, k, 1);
-  if (!QG_LAUNCHED("mrhs_zero_slot")) return -2;
-  // p = r (slot_residual left r in B->s32 for even/odd batches, else in B->r)
-  if (!mfield_set(B->ps, k, B->eo ? B->s32 : B->r)) return -2;
   float mp = (float)sl.mp4, tmf = (float)mu;
-  if (!QG_CUDA(cudaMemcpyAsync(B->mp4s + k, &mp, sizeof(float), cudaMemcpyHostToDevice, stream())) ||
-      !QG_CUDA(cudaMemcpyAsync(B->tms + k, &tmf, sizeof(float), cudaMemcpyHostToDevice, stream())))
-    return -2;
+  // p = r (slot_residual left r in B->s32 for even/odd batches, else in B->r);
   // a fresh slot starts with beta = 0, so the shared p update leaves p = r
-  if (!set_scalar(B, M_RR, k, rr) || !set_scalar(B, M_BETA, k, 0.0)) return -2;
+  if (!QG_LAUNCHED("mrhs_zero_slot") || !mfield_set(B->ps, k, B->eo ? B->s32 : B->r) ||
+      !QG_CUDA(cudaMemcpyAsync(B->mp4s + k, &mp, sizeof(float), cudaMemcpyHostToDevice, stream())) ||
+      !QG_CUDA(cudaMemcpyAsync(B->tms + k, &tmf, sizeof(float), cudaMemcpyHostToDevice, stream())) ||
+      !set_scalar(B, M_RR, k, rr) || !set_scalar(B, M_BETA, k, 0.0)) {
+    give_back();
+    return -2;
+  }
   if (bn2 == 0.0 || rel <= tol) {
     // solved by x_e = 0: x = (0, A^{-1} b_o) for even/odd batches
     if (B->eo && !slot_finish_eo(B, sl)) return -2;
