@@ -674,7 +674,7 @@ def run_ours(args, rank, world, local_rank):
     serving32 = None
     if rank == 0 and not args.no_serve:
         serving = serving_bench(q, args.serve_seconds, args.serve_rate, args.serve_slots, args.serve_budget_gb)
-        # the same stream on the 32^3 x 64 gauge field alone (the spec volume)
+        # the same stream on the 32^3 x 64 gauge field alone (the volume of the solve summary)
         serving32 = serving_bench(q, args.serve32_seconds, args.serve32_rate, args.serve_slots, args.serve_budget_gb,
                                   weights=(0, 0, 0, 1))
     ceiling = compute_ceiling(q, V, ms_native, ms_df64, clocks["sm_mhz"] if clocks else None) if rank == 0 else None
